@@ -1,0 +1,493 @@
+// Host-side algebra of the prove_fast path: the pieces that act on O(128)- to
+// O(m * 2^col_log)-sized objects and therefore never touch the committed data.
+//
+//  * Lagrange weights on the phi8 node sets S = phi8{0..63} and Lambda = phi8{64..127}
+//    (crates/flock-core/src/zerocheck/multilinear.rs:150-240).
+//  * The ring-switch reduction of one claim (crates/flock-core/src/pcs/ring_switch.rs:
+//    1406-1450, 1587-1603, 2724-2760) and the linearised form of its fold map
+//    (ring_switch.rs:1686-1775).
+//  * The multipoint twisted assist and its untwisted anchor
+//    (crates/flock-core/src/pcs/jagged.rs:146-260, 556-720, 1660-2020, 2790-3300),
+//    restated in closed form for the aligned full-height column layout every
+//    full-utilisation single-slot statement has (columns c < used_cols hold rows
+//    [0, 2^nu), dense index d = c * 2^nu + row).
+//  * The Ligerito induced-basis point weights (crates/flock-core/src/pcs/ligerito.rs:
+//    2396-2460) and the queried-row enforced sum (pcs/ligerito/extension.rs:2893-2916).
+#pragma once
+#include "field.h"
+#include "transcript.h"
+#include "proof.h"
+#include "setup.h"
+#include <thread>
+
+namespace flock {
+
+// ---------------------------------------------------------------- Lagrange on phi8 sets
+inline const std::pair<F128, F128>& subspace_den6() {
+  static std::pair<F128, F128> d = [] {
+    F128 den = F128::one();
+    for (int i = 1; i < 64; ++i) den = den * phi8((uint8_t)i);
+    return std::make_pair(den, inv(den));
+  }();
+  return d;
+}
+inline const std::pair<F128, F128>& subspace_den7() {
+  static std::pair<F128, F128> d = [] {
+    F128 den = F128::one();
+    for (int i = 1; i < 128; ++i) den = den * phi8((uint8_t)i);
+    return std::make_pair(den, inv(den));
+  }();
+  return d;
+}
+// Weights L_i(z) on the 64 nodes phi8(offset + i), offset in {0, 64}.
+inline std::vector<F128> lagrange_weights64(F128 z, int offset) {
+  std::vector<F128> w(64);
+  F128 zn = F128::one();
+  for (int i = 0; i < 64; ++i) zn = zn * (z + phi8((uint8_t)(offset + i)));
+  if (zn.is_zero()) {
+    for (int i = 0; i < 64; ++i) w[i] = (z == phi8((uint8_t)(offset + i))) ? F128::one() : F128();
+    return w;
+  }
+  F128 scale = zn * subspace_den6().second;
+  for (int i = 0; i < 64; ++i) w[i] = scale * inv(z + phi8((uint8_t)(offset + i)));
+  return w;
+}
+inline F128 interpolate_on_lambda(const std::vector<F128>& vals, F128 z) {
+  auto w = lagrange_weights64(z, 64);
+  F128 acc;
+  for (int i = 0; i < 64; ++i) acc += w[i] * vals[i];
+  return acc;
+}
+
+// ---------------------------------------------------------------- ring switch
+inline std::vector<F128> tensor_transpose128(const std::vector<F128>& v) {
+  std::vector<F128> u(128);
+  for (int i = 0; i < 128; ++i) {
+    for (int b = 0; b < 128; ++b) {
+      uint64_t bit = b < 64 ? (v[i].lo >> b) & 1 : (v[i].hi >> (b - 64)) & 1;
+      if (bit) { if (i < 64) u[b].lo |= 1ull << i; else u[b].hi |= 1ull << (i - 64); }
+    }
+  }
+  return u;
+}
+// 16 x 256 byte tables: tab[k*256 + v] = sum of eq[8k + bit] over set bits of v.
+inline std::vector<F128> fold_byte_table(const std::vector<F128>& eq128) {
+  std::vector<F128> t(16 * 256);
+  for (int k = 0; k < 16; ++k)
+    for (int v = 0; v < 256; ++v) {
+      F128 acc;
+      for (int b = 0; b < 8; ++b) if ((v >> b) & 1) acc += eq128[8 * k + b];
+      t[k * 256 + v] = acc;
+    }
+  return t;
+}
+inline F128 fold_one_slot(const F128& x, const F128* tab) {
+  F128 acc;
+  for (int k = 0; k < 8; ++k) acc += tab[k * 256 + ((x.lo >> (8 * k)) & 255)];
+  for (int k = 0; k < 8; ++k) acc += tab[(8 + k) * 256 + ((x.hi >> (8 * k)) & 255)];
+  return acc;
+}
+inline F128 bit_basis(int t) { return t < 64 ? F128(1ull << t, 0) : F128(0, 1ull << (t - 64)); }
+
+// Inverse of the Moore matrix M[t][j] = e_t^(2^j), row-major inv[j*128 + t].
+inline const std::vector<F128>& moore_inverse() {
+  static std::vector<F128> inv_m = [] {
+    const int N = 128;
+    std::vector<F128> m(N * N), iv(N * N);
+    for (int t = 0; t < N; ++t) {
+      F128 x = bit_basis(t);
+      for (int j = 0; j < N; ++j) { m[t * N + j] = x; x = x * x; }
+    }
+    for (int i = 0; i < N; ++i) iv[i * N + i] = F128::one();
+    for (int col = 0; col < N; ++col) {
+      int piv = col;
+      while (m[piv * N + col].is_zero()) ++piv;
+      if (piv != col)
+        for (int k = 0; k < N; ++k) { std::swap(m[col * N + k], m[piv * N + k]); std::swap(iv[col * N + k], iv[piv * N + k]); }
+      F128 p = inv(m[col * N + col]);
+      for (int k = 0; k < N; ++k) { m[col * N + k] = m[col * N + k] * p; iv[col * N + k] = iv[col * N + k] * p; }
+      for (int r = 0; r < N; ++r) {
+        if (r == col || m[r * N + col].is_zero()) continue;
+        F128 f = m[r * N + col];
+        for (int k = 0; k < N; ++k) { m[r * N + k] += f * m[col * N + k]; iv[r * N + k] += f * iv[col * N + k]; }
+      }
+    }
+    return iv;
+  }();
+  return inv_m;
+}
+inline std::vector<F128> linearized_coefficients(const std::vector<F128>& tab) {
+  const auto& mi = moore_inverse();
+  std::vector<F128> phi(128), c(128);
+  for (int t = 0; t < 128; ++t) phi[t] = fold_one_slot(bit_basis(t), tab.data());
+  for (int j = 0; j < 128; ++j) {
+    F128 acc;
+    for (int t = 0; t < 128; ++t) acc += mi[j * 128 + t] * phi[t];
+    c[j] = acc;
+  }
+  return c;
+}
+
+// One claim of the batched ring switch: absorb s_hat_v, sample r'' under PoW, return
+// the sumcheck claim <transpose(s_hat_v), eq(r'')> and the (unscaled) fold table.
+struct RingSwitchOut {
+  RingSwitchProof proof;
+  F128 sumcheck_claim;
+  std::vector<F128> table;
+};
+inline RingSwitchOut ring_switch_claim(Transcript& T, const std::vector<F128>& s_hat_v, uint32_t bits) {
+  RingSwitchOut o;
+  T.observe_label("flock-ring-switch-v0");
+  T.observe_f128_slice(s_hat_v);
+  std::vector<F128> rdp;
+  if (bits) { auto pr = T.grind_pow_and_sample_f128_vec(bits, 7); o.proof.grinding_nonce = pr.first; rdp = pr.second; }
+  else rdp = T.sample_f128_vec(7);
+  auto eq = build_eq(rdp);
+  auto u = tensor_transpose128(s_hat_v);
+  F128 acc;
+  for (int i = 0; i < 128; ++i) acc += u[i] * eq[i];
+  o.sumcheck_claim = acc;
+  o.table = fold_byte_table(eq);
+  o.proof.s_hat_v = s_hat_v;
+  return o;
+}
+
+// ---------------------------------------------------------------- aligned jagged layout
+struct AlignedJagged {
+  uint32_t n = 0;       // row variables (nu)
+  uint32_t k = 0;       // column variables (col_log)
+  uint32_t m = 0;       // dense variables = n + k
+  uint64_t used = 0;    // full-height columns [0, used)
+  uint64_t area() const { return used << n; }
+};
+
+// sum over boolean c < used of prod_b f_b(c_b), with f_b given as (f_b(0), f_b(1)).
+inline F128 prefix_product_sum(const std::vector<std::pair<F128, F128>>& f, uint64_t used) {
+  int k = (int)f.size();
+  if (used >= (uint64_t(1) << k)) {
+    F128 p = F128::one();
+    for (auto& q : f) p = p * (q.first + q.second);
+    return p;
+  }
+  // suffix totals of the free low bits
+  std::vector<F128> low_total(k + 1);
+  low_total[0] = F128::one();
+  for (int b = 0; b < k; ++b) low_total[b + 1] = low_total[b] * (f[b].first + f[b].second);
+  F128 acc, high = F128::one();
+  for (int j = k - 1; j >= 0; --j) {
+    if ((used >> j) & 1) {
+      acc += high * f[j].first * low_total[j];
+      high = high * f[j].second;
+    } else {
+      high = high * f[j].first;
+    }
+  }
+  return acc;
+}
+// eq(a, b) for boolean b as field value: (1 + a) or a.
+inline std::pair<F128, F128> eq_pair(F128 a) { return {a + F128::one(), a}; }
+
+// ---------------------------------------------------------------- the anchor assist
+// Width-4 branching program for g(a, b, c, d) = [b < d and b = a + c] read LSB-first
+// (jagged.rs:164-192). state = carry + 2 * comparison.
+inline int bp_transition(int row, int index, int curr, int next, int state) {
+  int carry = state & 1, cmp = (state >> 1) & 1;
+  int sum = row + carry + curr;
+  if (index != (sum & 1)) return -1;
+  int nc = sum >> 1;
+  int ncmp = index == next ? cmp : next;
+  return nc + (ncmp << 1);
+}
+constexpr int BP_INITIAL = 0, BP_SUCCESS = 2;
+
+// Layer matrix M(a, b; c, d)[s][s'] for boolean c, d, given eq4[row + 2 index] = eq((a,b), (row,index)).
+inline void bp_layer_matrix(const F128 eq4[4], int c, int d, F128 M[4][4]) {
+  for (int s = 0; s < 4; ++s) for (int t = 0; t < 4; ++t) M[s][t] = F128();
+  for (int s = 0; s < 4; ++s)
+    for (int row = 0; row < 2; ++row)
+      for (int idx = 0; idx < 2; ++idx) {
+        int o = bp_transition(row, idx, c, d, s);
+        if (o >= 0) M[s][o] += eq4[row + 2 * idx];
+      }
+}
+
+struct AssistStatement {
+  std::vector<F128> z_row;                    // length n (zero-padded beyond)
+  std::vector<F128> w;                        // per boundary-run weight
+  std::vector<std::pair<uint64_t, uint64_t>> t;  // (t_{y-1}, t_y) per run
+};
+
+// Prover of the batched (untwisted) assist over `sts` at `point` (length m): proves
+// V = sum_st sum_runs w * g_hat(z_row, point, t_c, t_next) with 2(m+1) degree-2 rounds.
+inline FrobeniusAssistProof prove_anchor_assist(Transcript& T, const std::vector<AssistStatement>& sts,
+                                                const std::vector<F128>& point, uint32_t m, uint32_t round_bits) {
+  const int L = (int)m + 1;  // layers 0..m
+  auto pbit = [](const std::vector<F128>& z, int l) { return l < (int)z.size() ? z[l] : F128(); };
+  struct St {
+    std::vector<std::array<F128, 4>> eq4;                // per layer
+    std::vector<std::vector<std::array<F128, 4>>> sfx;   // sfx[l][run] = S_l (state vector), l in 0..L
+    std::vector<F128> part;                              // per-run partial weights
+    std::array<F128, 4> prefix;
+  };
+  std::vector<St> S(sts.size());
+  for (size_t si = 0; si < sts.size(); ++si) {
+    const AssistStatement& a = sts[si];
+    St& s = S[si];
+    s.eq4.resize(L);
+    for (int l = 0; l < L; ++l) {
+      auto e = build_eq({pbit(a.z_row, l), pbit(point, l)});
+      s.eq4[l] = {e[0], e[1], e[2], e[3]};
+    }
+    size_t R = a.w.size();
+    s.sfx.assign(L + 1, std::vector<std::array<F128, 4>>(R));
+    for (size_t r = 0; r < R; ++r) { s.sfx[L][r] = {F128(), F128(), F128(), F128()}; s.sfx[L][r][BP_SUCCESS] = F128::one(); }
+    for (int l = L - 1; l >= 0; --l) {
+      F128 Mc[4][4][4];
+      for (int cd = 0; cd < 4; ++cd) bp_layer_matrix(s.eq4[l].data(), cd & 1, (cd >> 1) & 1, Mc[cd]);
+      for (size_t r = 0; r < R; ++r) {
+        int c = (int)((a.t[r].first >> l) & 1), d = (int)((a.t[r].second >> l) & 1);
+        auto& nx = s.sfx[l + 1][r];
+        std::array<F128, 4> out{};
+        for (int st = 0; st < 4; ++st) {
+          F128 acc;
+          for (int o = 0; o < 4; ++o) acc += Mc[c + 2 * d][st][o] * nx[o];
+          out[st] = acc;
+        }
+        s.sfx[l][r] = out;
+      }
+    }
+    s.part = a.w;
+    s.prefix = {F128(), F128(), F128(), F128()};
+    s.prefix[BP_INITIAL] = F128::one();
+  }
+  FrobeniusAssistProof pf;
+  F128 v;
+  for (size_t si = 0; si < sts.size(); ++si)
+    for (size_t r = 0; r < sts[si].w.size(); ++r) v += S[si].part[r] * S[si].sfx[0][r][BP_INITIAL];
+  pf.v = v;
+  T.observe_label("flock-frobenius-assist-v0");
+  T.observe_f128(v);
+  auto dot4 = [](const std::array<F128, 4>& a, const std::array<F128, 4>& b) {
+    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3];
+  };
+  auto add4 = [](const std::array<F128, 4>& a, const std::array<F128, 4>& b) {
+    return std::array<F128, 4>{a[0] + b[0], a[1] + b[1], a[2] + b[2], a[3] + b[3]};
+  };
+  auto comb4 = [](F128 x, const std::array<F128, 4>& a, F128 y, const std::array<F128, 4>& b) {
+    return std::array<F128, 4>{x * a[0] + y * b[0], x * a[1] + y * b[1], x * a[2] + y * b[2], x * a[3] + y * b[3]};
+  };
+  for (int l = 0; l < L; ++l) {
+    // per statement: u[cd] = prefix * M_l(c, d); bucket[cd] = sum over runs with bits (c,d) of part * S_{l+1}
+    std::vector<std::array<std::array<F128, 4>, 4>> U(S.size()), B(S.size());
+    for (size_t si = 0; si < S.size(); ++si) {
+      St& s = S[si];
+      for (int cd = 0; cd < 4; ++cd) {
+        F128 M[4][4];
+        bp_layer_matrix(s.eq4[l].data(), cd & 1, (cd >> 1) & 1, M);
+        for (int o = 0; o < 4; ++o) {
+          F128 acc;
+          for (int st = 0; st < 4; ++st) acc += s.prefix[st] * M[st][o];
+          U[si][cd][o] = acc;
+        }
+        B[si][cd] = {F128(), F128(), F128(), F128()};
+      }
+      const AssistStatement& a = sts[si];
+      for (size_t r = 0; r < a.w.size(); ++r) {
+        int c = (int)((a.t[r].first >> l) & 1), d = (int)((a.t[r].second >> l) & 1);
+        auto& nx = s.sfx[l + 1][r];
+        for (int o = 0; o < 4; ++o) B[si][c + 2 * d][o] += s.part[r] * nx[o];
+      }
+    }
+    F128 g1, gi;
+    for (size_t si = 0; si < S.size(); ++si) {
+      g1 += dot4(U[si][1], B[si][1]) + dot4(U[si][3], B[si][3]);
+      gi += dot4(add4(U[si][0], U[si][1]), add4(B[si][0], B[si][1])) + dot4(add4(U[si][2], U[si][3]), add4(B[si][2], B[si][3]));
+    }
+    T.observe_f128(g1); T.observe_f128(gi);
+    F128 rc;
+    if (round_bits) { auto pr = T.grind_pow_and_sample_f128(round_bits); pf.grinding_nonces.push_back(pr.first); rc = pr.second; }
+    else rc = T.sample_f128();
+    pf.rounds.push_back({g1, gi});
+    F128 rc1 = rc + F128::one();
+    g1 = F128(); gi = F128();
+    std::vector<std::pair<std::array<F128, 4>, std::array<F128, 4>>> folded(S.size());
+    for (size_t si = 0; si < S.size(); ++si) {
+      auto ud0 = comb4(rc1, U[si][0], rc, U[si][1]);
+      auto ud1 = comb4(rc1, U[si][2], rc, U[si][3]);
+      auto d0 = comb4(rc1, B[si][0], rc, B[si][1]);
+      auto d1 = comb4(rc1, B[si][2], rc, B[si][3]);
+      g1 += dot4(ud1, d1);
+      gi += dot4(add4(ud0, ud1), add4(d0, d1));
+      folded[si] = {ud0, ud1};
+    }
+    T.observe_f128(g1); T.observe_f128(gi);
+    F128 rd;
+    if (round_bits) { auto pr = T.grind_pow_and_sample_f128(round_bits); pf.grinding_nonces.push_back(pr.first); rd = pr.second; }
+    else rd = T.sample_f128();
+    pf.rounds.push_back({g1, gi});
+    F128 rd1 = rd + F128::one();
+    for (size_t si = 0; si < S.size(); ++si) {
+      S[si].prefix = comb4(rd1, folded[si].first, rd, folded[si].second);
+      // fold the run partials by the layer's (c, d) bits
+      const AssistStatement& a = sts[si];
+      for (size_t r = 0; r < a.w.size(); ++r) {
+        int c = (int)((a.t[r].first >> l) & 1), d = (int)((a.t[r].second >> l) & 1);
+        S[si].part[r] = S[si].part[r] * (c ? rc : rc1) * (d ? rd : rd1);
+      }
+    }
+  }
+  return pf;
+}
+
+// Runs of equal boundary pairs for the aligned layout and their column-weight sums.
+inline AssistStatement aligned_statement(const AlignedJagged& J, const std::vector<F128>& z_row,
+                                         const std::vector<F128>& z_col, F128 coeff) {
+  AssistStatement a;
+  a.z_row = z_row;
+  auto eqc = build_eq(z_col);
+  uint64_t H = uint64_t(1) << J.n;
+  for (uint64_t y = 0; y < J.used; ++y) { a.w.push_back(eqc[y] * coeff); a.t.push_back({y * H, (y + 1) * H}); }
+  uint64_t ncol = uint64_t(1) << J.k;
+  if (J.used < ncol) {
+    F128 s;
+    for (uint64_t y = J.used; y < ncol; ++y) s += eqc[y];
+    a.w.push_back(s * coeff);
+    a.t.push_back({J.area(), J.area()});
+  }
+  return a;
+}
+
+// ---------------------------------------------------------------- multipoint twisted assist
+struct RsClaimPoint {
+  std::vector<F128> z_row, z_col;   // (n, k)
+  std::vector<F128> coeffs;         // 128 linearised coefficients (gamma baked)
+};
+
+// x^(2^-j) for j = 0..127 of every coordinate (x^(2^128) = x).
+inline std::vector<std::vector<F128>> rho_inverse_powers(const std::vector<F128>& rho) {
+  std::vector<std::vector<F128>> sq(128, std::vector<F128>(rho.size()));
+  for (size_t i = 0; i < rho.size(); ++i) {
+    F128 x = rho[i];
+    sq[0][i] = x;
+    for (int e = 1; e < 128; ++e) { x = x * x; sq[e][i] = x; }
+  }
+  std::vector<std::vector<F128>> out(128);
+  for (int j = 0; j < 128; ++j) out[j] = sq[(128 - j) % 128];
+  return out;
+}
+
+// Prover of the multipoint twisted evaluation for ring-switched claims over the aligned
+// layout (jagged.rs:2884-3290): 128 dual values per claim, one m-round two-product
+// sumcheck of sum_d abar(d) g(d) with abar = sum_i gamma^(128 i) a_i and
+// g = sum_j gamma^j eq(rho^(2^-j), .), then the untwisted anchor at the endpoint.
+// Every message is evaluated in closed form over the tensor structure of a_i and g.
+inline MultipointTwistedProof prove_multipoint(Transcript& T, const AlignedJagged& J,
+                                               const std::vector<RsClaimPoint>& claims,
+                                               const std::vector<F128>& rho, uint32_t round_bits,
+                                               uint32_t anchor_round_bits) {
+  const uint32_t n = J.n, k = J.k, m = J.m;
+  const size_t R = claims.size();
+  auto rp = rho_inverse_powers(rho);  // rp[j][t]
+  MultipointTwistedProof pf;
+  // ---- dual values A_{i,j}
+  auto col_pps = [&](const std::vector<F128>& zc, const std::vector<F128>& rj, uint32_t off) {
+    std::vector<std::pair<F128, F128>> f(k);
+    for (uint32_t b = 0; b < k; ++b) {
+      auto ez = eq_pair(zc[b]), er = eq_pair(rj[off + b]);
+      f[b] = {ez.first * er.first, ez.second * er.second};
+    }
+    return prefix_product_sum(f, J.used);
+  };
+  pf.values.assign(R, std::vector<F128>(128));
+  for (size_t i = 0; i < R; ++i)
+    for (int j = 0; j < 128; ++j) {
+      F128 rowp = F128::one();
+      for (uint32_t t = 0; t < n; ++t) rowp = rowp * (F128::one() + claims[i].z_row[t] + rp[j][t]);
+      pf.values[i][j] = rowp * col_pps(claims[i].z_col, rp[j], n);
+    }
+  T.observe_label("flock-multipoint-twisted-v1");
+  for (auto& vs : pf.values) for (auto& v : vs) T.observe_f128(v);
+  uint32_t gamma_bits = std::max<uint32_t>(1, grinding_bits_for_degree(128 * R - 1));
+  auto gp = T.grind_pow_and_sample_f128(gamma_bits);
+  pf.gamma_grinding_nonce = gp.first;
+  F128 gamma = gp.second;
+  std::vector<F128> gpow(128 * R);
+  F128 p = F128::one();
+  for (auto& g : gpow) { g = p; p = p * gamma; }
+  // ---- closed-form two-product sumcheck
+  // coef_ij = gamma^(128 i + j); prefix products over bound bits; row suffix products.
+  std::vector<std::vector<F128>> P(R, std::vector<F128>(128)), rowsuf(R, std::vector<F128>(128 * (n + 1)));
+  for (size_t i = 0; i < R; ++i)
+    for (int j = 0; j < 128; ++j) {
+      P[i][j] = gpow[128 * i + j];
+      F128* sf = &rowsuf[i][j * (n + 1)];
+      sf[n] = F128::one();
+      for (int t = (int)n - 1; t >= 0; --t) sf[t] = sf[t + 1] * (F128::one() + claims[i].z_row[t] + rp[j][t]);
+    }
+  std::vector<std::vector<F128>> Ccol(R, std::vector<F128>(128));
+  for (size_t i = 0; i < R; ++i)
+    for (int j = 0; j < 128; ++j) Ccol[i][j] = col_pps(claims[i].z_col, rp[j], n);
+  std::vector<F128> s;  // bound challenges
+  auto message = [&](uint32_t t, F128& g1, F128& gi) {
+    g1 = F128(); gi = F128();
+    if (t < n) {
+      for (size_t i = 0; i < R; ++i)
+        for (int j = 0; j < 128; ++j) {
+          F128 c = P[i][j] * rowsuf[i][j * (n + 1) + t + 1] * Ccol[i][j];
+          g1 += c * claims[i].z_row[t] * rp[j][t];
+          gi += c;
+        }
+    } else {
+      uint32_t b = t - n;
+      for (size_t i = 0; i < R; ++i)
+        for (int j = 0; j < 128; ++j) {
+          // column weights: u < b bound to s, u = b the round variable, u > b summed against rho_j
+          std::vector<std::pair<F128, F128>> f0(k), f1(k);
+          for (uint32_t u = 0; u < k; ++u) {
+            auto ez = eq_pair(claims[i].z_col[u]);
+            std::pair<F128, F128> w;
+            if (u < b) w = eq_pair(s[n + u]);
+            else if (u > b) w = eq_pair(rp[j][n + u]);
+            if (u == b) { f0[u] = {ez.first, F128()}; f1[u] = {F128(), ez.second}; }
+            else { f0[u] = f1[u] = {ez.first * w.first, ez.second * w.second}; }
+          }
+          F128 l20 = prefix_product_sum(f0, J.used), l21 = prefix_product_sum(f1, J.used);
+          F128 c = P[i][j];  // row factors and bound column factors of g already folded in
+          g1 += c * rp[j][n + b] * l21;
+          gi += c * (l20 + l21);
+        }
+    }
+  };
+  F128 g1, gi;
+  message(0, g1, gi);
+  for (uint32_t t = 0; t < m; ++t) {
+    T.observe_f128(g1); T.observe_f128(gi);
+    F128 r;
+    if (round_bits) { auto pr = T.grind_pow_and_sample_f128(round_bits); pf.round_grinding_nonces.push_back(pr.first); r = pr.second; }
+    else r = T.sample_f128();
+    pf.rounds.push_back({g1, gi});
+    s.push_back(r);
+    if (t + 1 == m) break;
+    // absorb the bound variable into the prefix products
+    for (size_t i = 0; i < R; ++i)
+      for (int j = 0; j < 128; ++j) {
+        F128 f = F128::one() + rp[j][t] + r;  // eq(rho_j[t], r)
+        if (t < n) f = f * (F128::one() + claims[i].z_row[t] + r);
+        P[i][j] = P[i][j] * f;
+      }
+    message(t + 1, g1, gi);
+  }
+  // ---- anchor at the endpoint rho'' = s
+  F128 g_at;
+  for (int j = 0; j < 128; ++j) {
+    F128 prod = gpow[j];
+    for (uint32_t t = 0; t < m; ++t) prod = prod * (s[t] * rp[j][t] + (F128::one() + s[t]) * (F128::one() + rp[j][t]));
+    g_at += prod;
+  }
+  std::vector<AssistStatement> sts;
+  for (size_t i = 0; i < R; ++i) sts.push_back(aligned_statement(J, claims[i].z_row, claims[i].z_col, gpow[128 * i] * g_at));
+  pf.anchor = prove_anchor_assist(T, sts, s, m, anchor_round_bits);
+  return pf;
+}
+
+}  // namespace flock
