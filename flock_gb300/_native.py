@@ -1,0 +1,92 @@
+"""ctypes binding of libflock_gb300.so (the C ABI of include/flock_gb300.h).
+
+The library is built in-tree by ``__graft_entry__.build()`` into ``flock_gb300/_lib``.
+There is no fallback: if the library is missing or fails to load, every entry point
+raises ``NativeLibraryError``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+LIB_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib")
+LIB_PATH = os.path.join(LIB_DIR, "libflock_gb300.so")
+
+#: Exported symbols, in declaration order of include/flock_gb300.h.
+EXPORTS = (
+    "flock_gb300_input_record_bytes",
+    "flock_gb300_setup_new",
+    "flock_gb300_setup_free",
+    "flock_gb300_setup_info",
+    "flock_gb300_prove_fast",
+    "flock_gb300_last_phase_ms",
+    "flock_gb300_free",
+    "flock_gb300_device_count",
+    "flock_gb300_last_error",
+)
+
+BLAKE3, SHA256, KECCAK = 0, 1, 2
+OK, EINVAL, ECUDA, EINTERNAL = 0, 1, 2, 3
+
+
+class NativeLibraryError(RuntimeError):
+    """The CUDA library is not built or cannot be loaded."""
+
+
+class FlockError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load() -> ctypes.CDLL:
+    """Load (once) and return the library, declaring every signature."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise NativeLibraryError(
+                f"{LIB_PATH} is missing: build the CUDA extension with __graft_entry__.build()"
+            )
+        try:
+            lib = ctypes.CDLL(LIB_PATH)
+        except OSError as e:  # pragma: no cover - depends on the machine
+            raise NativeLibraryError(f"cannot load {LIB_PATH}: {e}") from e
+        c = ctypes
+        lib.flock_gb300_input_record_bytes.argtypes = [c.c_int]
+        lib.flock_gb300_input_record_bytes.restype = c.c_size_t
+        lib.flock_gb300_setup_new.argtypes = [c.c_int, c.c_uint64, c.POINTER(c.c_void_p)]
+        lib.flock_gb300_setup_new.restype = c.c_int
+        lib.flock_gb300_setup_free.argtypes = [c.c_void_p]
+        lib.flock_gb300_setup_free.restype = None
+        lib.flock_gb300_setup_info.argtypes = [c.c_void_p, c.POINTER(c.c_uint32), c.POINTER(c.c_uint32), c.c_char_p]
+        lib.flock_gb300_setup_info.restype = c.c_int
+        lib.flock_gb300_prove_fast.argtypes = [
+            c.c_void_p, c.c_void_p, c.c_size_t, c.c_char_p, c.c_size_t,
+            c.POINTER(c.POINTER(c.c_uint8)), c.POINTER(c.c_size_t),
+        ]
+        lib.flock_gb300_prove_fast.restype = c.c_int
+        lib.flock_gb300_last_phase_ms.argtypes = [c.c_void_p, c.POINTER(c.c_double)]
+        lib.flock_gb300_last_phase_ms.restype = c.c_int
+        lib.flock_gb300_free.argtypes = [c.POINTER(c.c_uint8)]
+        lib.flock_gb300_free.restype = None
+        lib.flock_gb300_device_count.argtypes = []
+        lib.flock_gb300_device_count.restype = c.c_int
+        lib.flock_gb300_last_error.argtypes = []
+        lib.flock_gb300_last_error.restype = c.c_char_p
+        _lib = lib
+        return lib
+
+
+def check(code: int) -> None:
+    if code != OK:
+        msg = load().flock_gb300_last_error().decode("utf-8", "replace")
+        raise FlockError(code, msg)

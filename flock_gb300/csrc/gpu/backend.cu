@@ -1,0 +1,582 @@
+// The device backend of prove_fast: owns every witness-sized buffer in HBM for the
+// life of a setup (z, a, b, the L0 codeword and tree, the zerocheck / merged-open fold
+// buffers, the Ligerito F256 state and level codewords) and runs each bulk step of the
+// protocol as sm_103a kernels on one stream. The host keeps only the transcript and the
+// O(m)-sized arithmetic between rounds; every round message comes back as a handful of
+// field elements.
+#include "backend.h"
+#include "../host/tables.h"
+
+namespace flock {
+namespace gpu {
+
+namespace {
+
+// GF(2^8) exp / log tables with generator 0x03.
+void gf8_exp_log(uint8_t gexp[512], uint8_t glog[256]) {
+  uint8_t x = 1;
+  for (int i = 0; i < 255; ++i) {
+    gexp[i] = x;
+    glog[x] = (uint8_t)i;
+    x = gf8_mul(x, 3);
+  }
+  for (int i = 255; i < 512; ++i) gexp[i] = gexp[i - 255];
+  glog[0] = 0;
+}
+
+std::once_flag g_consts_once;
+void upload_constants_once() {
+  std::call_once(g_consts_once, [] {
+    const SkipTables& st = skip_tables();
+    uint8_t gexp[512], glog[256];
+    gf8_exp_log(gexp, glog);
+    // eq factor of the three small zerocheck constants (bit j of K selects c_j or 1 + c_j)
+    const uint8_t c[3] = {0xF7, 0x53, 0xB5};
+    uint8_t mulk[8][256], e2[4];
+    for (int K = 0; K < 8; ++K) {
+      uint8_t e = 1;
+      for (int j = 0; j < 3; ++j) e = gf8_mul(e, ((K >> j) & 1) ? c[j] : (uint8_t)(c[j] ^ 1));
+      for (int v = 0; v < 256; ++v) mulk[K][v] = gf8_mul(e, (uint8_t)v);
+    }
+    for (int K2 = 0; K2 < 4; ++K2) {
+      uint8_t e = 1;
+      for (int j = 0; j < 2; ++j) e = gf8_mul(e, ((K2 >> j) & 1) ? c[j + 1] : (uint8_t)(c[j + 1] ^ 1));
+      e2[K2] = e;
+    }
+    upload_zc_consts(st.ext.data(), reinterpret_cast<const F128d*>(phi8_table().data()), gexp, glog, mulk, e2);
+  });
+}
+
+inline F128d dev(F128 v) { F128d r; r.lo = v.lo; r.hi = v.hi; return r; }
+inline F256d dev(F256 v) { F256d r; r.c0 = dev(v.c0); r.c1 = dev(v.c1); return r; }
+inline F128 host(F128d v) { return F128(v.lo, v.hi); }
+
+}  // namespace
+
+template <class T>
+static T* dmalloc(size_t n, std::vector<void*>& owned) {
+  void* p = nullptr;
+  if (n == 0) n = 1;
+  CUDA_OK(cudaMalloc(&p, n * sizeof(T)));
+  owned.push_back(p);
+  return static_cast<T*>(p);
+}
+
+GpuBackend::GpuBackend(const Statement& s) : S(s) {
+  CUDA_OK(cudaGetDevice(&device_));
+  CUDA_OK(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+  upload_constants_once();
+  W_ = uint64_t(1) << (S.m - 7);
+  K_ = 1u << S.k_log;
+  const uint64_t W = W_;
+  in_bytes_ = (size_t)S.n_blocks * input_record_bytes(S.hash);
+  d_in_ = dmalloc<uint8_t>(in_bytes_, owned_);
+  CUDA_OK(cudaMallocHost(&h_in_, in_bytes_));
+  z_ = dmalloc<F128d>(W, owned_);
+  a_ = dmalloc<F128d>(W, owned_);
+  b_ = dmalloc<F128d>(W, owned_);
+  // chunk columns the witness never writes stay zero for the life of the backend
+  CUDA_OK(cudaMemset(z_, 0, W * 16));
+  CUDA_OK(cudaMemset(a_, 0, W * 16));
+  CUDA_OK(cudaMemset(b_, 0, W * 16));
+  n_pos0_ = uint64_t(1) << S.k_code;
+  cw0_ = dmalloc<F128d>(n_pos0_ * S.lanes, owned_);
+  tree0_ = dmalloc<uint8_t>((2 * n_pos0_) * 32, owned_);
+  zc1a_ = dmalloc<F128d>(2 * W, owned_);
+  zc1b_ = dmalloc<F128d>(2 * W, owned_);
+  zc2a_ = dmalloc<F128d>(W, owned_);
+  zc2b_ = dmalloc<F128d>(W, owned_);
+  eqi_ = dmalloc<F128d>(K_, owned_);
+  ca_ = dmalloc<F128d>(K_, owned_);
+  cb_ = dmalloc<F128d>(K_, owned_);
+  comb_ = dmalloc<F128d>(K_, owned_);
+  zv_ = dmalloc<F128d>(K_, owned_);
+  zvcap_ = dmalloc<F128d>(K_, owned_);
+  if (S.hash != HASH_KECCAK) {
+    const Csc& A = *S.csc_a;
+    const Csc& B = *S.csc_b;
+    cola_ = dmalloc<uint32_t>(A.col_ptr.size(), owned_);
+    rowa_ = dmalloc<uint32_t>(A.rows_flat.size(), owned_);
+    colb_ = dmalloc<uint32_t>(B.col_ptr.size(), owned_);
+    rowb_ = dmalloc<uint32_t>(B.rows_flat.size(), owned_);
+    CUDA_OK(cudaMemcpy(cola_, A.col_ptr.data(), A.col_ptr.size() * 4, cudaMemcpyHostToDevice));
+    CUDA_OK(cudaMemcpy(rowa_, A.rows_flat.data(), A.rows_flat.size() * 4, cudaMemcpyHostToDevice));
+    CUDA_OK(cudaMemcpy(colb_, B.col_ptr.data(), B.col_ptr.size() * 4, cudaMemcpyHostToDevice));
+    CUDA_OK(cudaMemcpy(rowb_, B.rows_flat.data(), B.rows_flat.size() * 4, cudaMemcpyHostToDevice));
+  }
+  mw_ = dmalloc<F128d>(W, owned_);
+  moAq_ = dmalloc<F128d>(W / 2, owned_);
+  moAw_ = dmalloc<F128d>(W / 2, owned_);
+  moBq_ = dmalloc<F128d>(W / 4, owned_);
+  moBw_ = dmalloc<F128d>(W / 4, owned_);
+  lb128_ = dmalloc<F128d>(W, owned_);
+  for (int k = 0; k < 2; ++k) {
+    lf_[k] = dmalloc<F256d>(W / 2, owned_);
+    lb_[k] = dmalloc<F256d>(W / 2, owned_);
+  }
+  pend_ = dmalloc<F128d>(W / 2, owned_);
+  part_cap_ = 1u << 20;
+  part_ = dmalloc<F128d>(part_cap_, owned_);
+  red_ = dmalloc<F128d>(4096, owned_);
+  CUDA_OK(cudaMallocHost(&h_red_, 4096 * sizeof(F128d)));
+  scr_cap_ = size_t(96) << 20;
+  scr_ = dmalloc<uint8_t>(scr_cap_, owned_);
+  stage_cap_ = size_t(8) << 20;
+  d_stage_ = dmalloc<uint8_t>(stage_cap_, owned_);
+  CUDA_OK(cudaMallocHost(&h_stage_, stage_cap_));
+  // twiddles of the L0 transform
+  tw0_ = twiddles(S.k_code);
+  CUDA_OK(cudaDeviceSynchronize());
+}
+
+GpuBackend::~GpuBackend() {
+  cudaStreamSynchronize(st_);
+  for (void* p : owned_) cudaFree(p);
+  for (auto& kv : tw_) cudaFree(kv.second);
+  for (auto& L : levels_) { cudaFree(L.mat); cudaFree(L.tree); }
+  cudaFreeHost(h_in_);
+  cudaFreeHost(h_red_);
+  cudaFreeHost(h_stage_);
+  cudaStreamDestroy(st_);
+}
+
+const F128d* GpuBackend::twiddles(uint32_t log_d) {
+  auto it = tw_.find(log_d);
+  if (it != tw_.end()) return it->second;
+  auto tw = ntt_twiddles(log_d);
+  F128d* d = nullptr;
+  CUDA_OK(cudaMalloc(&d, std::max<size_t>(1, tw.size()) * sizeof(F128d)));
+  CUDA_OK(cudaMemcpy(d, tw.data(), tw.size() * sizeof(F128d), cudaMemcpyHostToDevice));
+  tw_[log_d] = d;
+  return d;
+}
+
+// ---- staging helpers
+void* GpuBackend::scratch(size_t bytes) {
+  size_t off = (scr_off_ + 255) & ~size_t(255);
+  if (off + bytes > scr_cap_) throw std::runtime_error("device scratch exhausted");
+  scr_off_ = off + bytes;
+  return scr_ + off;
+}
+const void* GpuBackend::upload(const void* src, size_t bytes) {
+  size_t off = (stage_off_ + 255) & ~size_t(255);
+  if (off + bytes > stage_cap_) {
+    sync();
+    off = 0;
+  }
+  memcpy(h_stage_ + off, src, bytes);
+  CUDA_OK(cudaMemcpyAsync(d_stage_ + off, h_stage_ + off, bytes, cudaMemcpyHostToDevice, st_));
+  stage_off_ = off + bytes;
+  return d_stage_ + off;
+}
+const F128d* GpuBackend::upload(const std::vector<F128>& v) {
+  return static_cast<const F128d*>(upload(v.data(), v.size() * sizeof(F128)));
+}
+void GpuBackend::sync() {
+  CUDA_OK(cudaStreamSynchronize(st_));
+  stage_off_ = 0;
+}
+std::vector<F128> GpuBackend::reduce(uint32_t n_blocks, uint32_t width) {
+  if ((uint64_t)n_blocks * width > part_cap_) throw std::runtime_error("partials buffer too small");
+  launch_reduce_parts(part_, n_blocks, width, red_, st_);
+  return fetch(red_, width);
+}
+std::vector<F128> GpuBackend::fetch(const F128d* d, size_t n) {
+  std::vector<F128> out(n);
+  F128d* h = h_red_;
+  bool big = n > 4096;
+  if (big) h = reinterpret_cast<F128d*>(out.data());
+  CUDA_OK(cudaMemcpyAsync(h, d, n * sizeof(F128d), cudaMemcpyDeviceToHost, st_));
+  sync();
+  if (!big) memcpy(out.data(), h, n * sizeof(F128d));
+  return out;
+}
+
+// eq(point) split as lo (first lo_bits coordinates) x hi (rest, times scale).
+GpuBackend::EqSplit GpuBackend::eq_split(const std::vector<F128>& point, F128 scale, uint32_t max_lo) {
+  EqSplit e;
+  uint32_t n = (uint32_t)point.size();
+  e.lo_bits = std::min(n, max_lo);
+  uint32_t hi_bits = n - e.lo_bits;
+  const F128d* dp = upload(point);
+  F128d* lo = static_cast<F128d*>(scratch((size_t(16)) << e.lo_bits));
+  F128d* hi = static_cast<F128d*>(scratch((size_t(16)) << hi_bits));
+  launch_eq_table(dp, e.lo_bits, dev(F128::one()), lo, st_);
+  launch_eq_table(dp + e.lo_bits, hi_bits, dev(scale), hi, st_);
+  e.lo = lo;
+  e.hi = hi;
+  return e;
+}
+
+// ------------------------------------------------------------------ witness + commit
+void GpuBackend::witness(const uint8_t* inputs) {
+  scr_off_ = 0;
+  memcpy(h_in_, inputs, in_bytes_);
+  CUDA_OK(cudaMemcpyAsync(d_in_, h_in_, in_bytes_, cudaMemcpyHostToDevice, st_));
+  launch_witness((int)S.hash, d_in_, S.n_blocks, S.nu, z_, a_, b_, (uint32_t)S.geo.used_cols, st_);
+}
+
+void GpuBackend::commit_l0(uint32_t cap_depth, std::vector<Hash>& cap) {
+  launch_fill_lane_major(z_, cw0_, S.lanes, S.log_dim, S.k_code, st_);
+  launch_ntt(cw0_, S.lanes, S.k_code, 1, tw0_, st_);
+  launch_merkle(cw0_, S.lanes, n_pos0_, tree0_, st_);
+  cap = read_cap(tree0_, n_pos0_, cap_depth);
+}
+
+std::vector<Hash> GpuBackend::read_cap(const uint8_t* tree, uint64_t n_leaves, uint32_t cap_depth) {
+  uint64_t l = uint64_t(1) << cap_depth;
+  std::vector<Hash> cap(l);
+  CUDA_OK(cudaMemcpyAsync(cap.data(), tree + (2 * n_leaves - 2 * l) * 32, l * 32, cudaMemcpyDeviceToHost, st_));
+  sync();
+  return cap;
+}
+
+// ------------------------------------------------------------------ zerocheck
+void GpuBackend::zc_round1(const std::vector<F128>& r, std::vector<F128>& ab, std::vector<F128>& c,
+                           std::vector<F128>& svc) {
+  scr_off_ = 0;
+  const uint32_t m = S.m;
+  auto fixed = zc_fixed_challenges();
+  for (int i = 0; i < 7; ++i)
+    if (r[6 + i] != fixed[i]) throw std::runtime_error("zerocheck round 1 expects the fixed challenges at r[6..13)");
+  std::vector<F128> outer(r.begin() + 13, r.end());
+  EqSplit e = eq_split(outer, F128::one(), 10);
+  uint32_t nb = launch_zc_round1(a_, b_, z_, m, e.lo, e.lo_bits, e.hi, part_, st_);
+  auto v = reduce(nb, 256);
+  F128 D = F128::one();
+  for (int i = 0; i < 4; ++i) D = D * inv(F128::one() + fixed[3 + i]);
+  ab.assign(64, F128());
+  c.assign(64, F128());
+  svc.assign(128, F128());
+  for (int i = 0; i < 64; ++i) { ab[i] = D * v[i]; c[i] = D * v[64 + i]; }
+  for (int i = 0; i < 128; ++i) svc[i] = D * v[128 + i];
+}
+
+void GpuBackend::zc_fold_skip(const std::vector<F128>& w, const std::vector<F128>& eq_point, F128& g1, F128& gi) {
+  scr_off_ = 0;
+  const F128d* dw = upload(w);
+  EqSplit e = eq_split(eq_point, F128::one(), 10);
+  if (e.lo_bits != 10) throw std::runtime_error("zerocheck skip fold needs m >= 17");
+  uint32_t nb = launch_zc_fold_skip(a_, b_, dw, W_, e.lo, e.lo_bits, e.hi, zc1a_, zc1b_, part_, st_);
+  auto v = reduce(nb, 2);
+  g1 = v[0];
+  gi = v[1];
+  zc_cur_a_ = zc1a_;
+  zc_cur_b_ = zc1b_;
+  zc_len_ = 2 * W_;
+}
+
+void GpuBackend::zc_fold(F128 rho, const std::vector<F128>& eq_point, F128& g1, F128& gi) {
+  scr_off_ = 0;
+  uint64_t n_pairs = zc_len_ / 4;
+  if ((uint64_t(1) << eq_point.size()) != n_pairs) throw std::runtime_error("zerocheck fold: eq size mismatch");
+  EqSplit e = eq_split(eq_point, F128::one(), 10);
+  F128d* oa = (zc_cur_a_ == zc1a_) ? zc2a_ : zc1a_;
+  F128d* ob = (zc_cur_a_ == zc1a_) ? zc2b_ : zc1b_;
+  uint32_t nb = launch_pair_fold(zc_cur_a_, zc_cur_b_, n_pairs, dev(rho), e.lo, e.lo_bits, e.hi, oa, ob, part_, true, st_);
+  auto v = reduce(nb, 2);
+  g1 = v[0];
+  gi = v[1];
+  zc_cur_a_ = oa;
+  zc_cur_b_ = ob;
+  zc_len_ /= 2;
+}
+
+void GpuBackend::zc_final(F128 rho, F128& ae, F128& be) {
+  if (zc_len_ != 2) throw std::runtime_error("zerocheck final fold expects two values");
+  auto av = fetch(zc_cur_a_, 2);
+  auto bv = fetch(zc_cur_b_, 2);
+  ae = av[0] + rho * (av[1] + av[0]);
+  be = bv[0] + rho * (bv[1] + bv[0]);
+}
+
+// ------------------------------------------------------------------ lincheck
+void GpuBackend::lc_comb(const std::vector<F128>& skip_w, const std::vector<F128>& xir) {
+  scr_off_ = 0;
+  const F128d* dw = upload(skip_w);
+  const F128d* der = upload(build_eq(xir));
+  launch_lc_eq_inner(dw, der, K_, eqi_, st_);
+  if (S.hash == HASH_KECCAK) {
+    // walker fold (additions only) on the host over the downloaded eq vector
+    auto eqi = fetch(eqi_, K_);
+    std::vector<F128> ha, hb;
+    kr1cs::fold_split(eqi.data(), ha, hb);
+    CUDA_OK(cudaMemcpyAsync(ca_, ha.data(), K_ * 16, cudaMemcpyHostToDevice, st_));
+    CUDA_OK(cudaMemcpyAsync(cb_, hb.data(), K_ * 16, cudaMemcpyHostToDevice, st_));
+    sync();
+    return;
+  }
+  launch_csc_fold(cola_, rowa_, K_, eqi_, ca_, st_);
+  launch_csc_fold(colb_, rowb_, K_, eqi_, cb_, st_);
+}
+
+void GpuBackend::lc_zvec(const std::vector<F128>& x_outer) {
+  scr_off_ = 0;
+  const uint32_t nu = S.nu;
+  const F128d* dp = upload(x_outer);
+  F128d* eq = static_cast<F128d*>(scratch(size_t(16) << nu));
+  launch_eq_table(dp, nu, dev(F128::one()), eq, st_);
+  uint32_t used = (uint32_t)S.geo.used_cols;
+  if ((uint64_t)used * 128 < K_) CUDA_OK(cudaMemsetAsync(zv_ + used * 128, 0, (K_ - used * 128) * 16, st_));
+  launch_lc_zvec(z_, nu, used, eq, part_, zv_, st_);
+  CUDA_OK(cudaMemcpyAsync(zvcap_, zv_, K_ * 16, cudaMemcpyDeviceToDevice, st_));
+  lc_len_ = K_;
+}
+
+void GpuBackend::lc_start(F128 alpha, F128 beta, uint32_t pin, F128& e1, F128& ei) {
+  uint32_t nb = launch_lc_start(ca_, cb_, dev(alpha), dev(beta), pin, K_, comb_, zv_, part_, st_);
+  auto v = reduce(nb, 2);
+  e1 = v[0];
+  ei = v[1];
+}
+
+void GpuBackend::lc_round(F128 r, bool last, F128& e1, F128& ei) {
+  uint32_t nb = launch_lc_round(comb_, zv_, lc_len_, dev(r), !last, part_, st_);
+  lc_len_ /= 2;
+  if (!last) {
+    auto v = reduce(nb, 2);
+    e1 = v[0];
+    ei = v[1];
+  }
+}
+
+void GpuBackend::lc_partial(std::vector<F128>& zp) {
+  if (lc_len_ != 64) throw std::runtime_error("lincheck partial expects 64 values");
+  zp = fetch(zv_, 64);
+}
+
+void GpuBackend::lc_matrix_evals(const std::vector<F128>& rest, const std::vector<F128>& zp, F128& ea, F128& eb) {
+  scr_off_ = 0;
+  const F128d* der = upload(build_eq(rest));
+  const F128d* dzp = upload(zp);
+  uint32_t nb = launch_lc_matrix_evals(ca_, cb_, der, dzp, K_, part_, st_);
+  auto v = reduce(nb, 2);
+  ea = v[0];
+  eb = v[1];
+}
+
+void GpuBackend::lc_s_hat_v(const std::vector<F128>& tail, std::vector<F128>& out) {
+  auto et = build_eq(tail);
+  const F128d* det = upload(et);
+  launch_lc_s_hat_v(zvcap_, det, (uint32_t)et.size(), red_, st_);
+  out = fetch(red_, 128);
+}
+
+// ------------------------------------------------------------------ merged open
+void GpuBackend::mo_build_w(const std::vector<WeightClaim>& cl, uint32_t nu, uint64_t area, F128& u0, F128& u2) {
+  scr_off_ = 0;
+  if (cl.size() != 2) throw std::runtime_error("merged open expects the AB and C claims");
+  F128d* er[2];
+  F128d* ec[2];
+  for (int i = 0; i < 2; ++i) {
+    const F128d* pr = upload(cl[i].z_row);
+    er[i] = static_cast<F128d*>(scratch(size_t(16) << cl[i].z_row.size()));
+    launch_eq_table(pr, (uint32_t)cl[i].z_row.size(), dev(F128::one()), er[i], st_);
+    const F128d* pc = upload(cl[i].z_col);
+    ec[i] = static_cast<F128d*>(scratch(size_t(16) << cl[i].z_col.size()));
+    launch_eq_table(pc, (uint32_t)cl[i].z_col.size(), dev(F128::one()), ec[i], st_);
+  }
+  std::vector<F128> tabs(cl[0].table);
+  tabs.insert(tabs.end(), cl[1].table.begin(), cl[1].table.end());
+  const F128d* dt = upload(tabs);
+  uint32_t nb = launch_mo_build_w(z_, er[0], ec[0], er[1], ec[1], dt, nu, area, W_, mw_, part_, st_);
+  auto v = reduce(nb, 2);
+  u0 = v[0];
+  u2 = v[1];
+  mo_q_ = z_;
+  mo_w_ = mw_;
+  mo_len_ = W_;
+}
+
+void GpuBackend::mo_round(F128 r, bool last, F128& g1, F128& gi) {
+  if (mo_len_ == 2) {
+    auto q = fetch(mo_q_, 2);
+    mo_final_ = q[0] + r * (q[1] + q[0]);
+    mo_len_ = 1;
+    return;
+  }
+  F128d* oq = (mo_q_ == moAq_) ? moBq_ : moAq_;
+  F128d* ow = (mo_q_ == moAq_) ? moBw_ : moAw_;
+  uint64_t n_pairs = mo_len_ / 4;
+  uint32_t chunk_bits = std::min<uint32_t>(10, ceil_log2(n_pairs));  // chunking only sets the work split
+  uint32_t nb = launch_pair_fold(mo_q_, mo_w_, n_pairs, dev(r), nullptr, chunk_bits, nullptr, oq, ow, part_, !last, st_);
+  mo_q_ = oq;
+  mo_w_ = ow;
+  mo_len_ /= 2;
+  if (!last) {
+    auto v = reduce(nb, 2);
+    g1 = v[0];
+    gi = v[1];
+  }
+}
+
+F128 GpuBackend::mo_q_eval() {
+  if (mo_len_ == 1) return mo_final_;
+  return fetch(mo_q_, 1)[0];
+}
+
+// ------------------------------------------------------------------ Ligerito
+void GpuBackend::lg_basis_eq(F128 gamma, const std::vector<F128>& rho) {
+  scr_off_ = 0;
+  if ((uint64_t(1) << rho.size()) != W_) throw std::runtime_error("Ligerito basis size mismatch");
+  EqSplit e = eq_split(rho, gamma, 10);
+  launch_lg_eq_fill(e.lo, e.lo_bits, e.hi, W_, lb128_, false, st_);
+  lg_base_ = true;
+  lg_n_ = W_;
+  lg_cur_ = 0;
+}
+
+F128 GpuBackend::lg_eval_eq(const std::vector<F128>& zp) {
+  scr_off_ = 0;
+  if (!lg_base_) throw std::runtime_error("OOD evaluation expects the committed base vector");
+  EqSplit e = eq_split(zp, F128::one(), 10);
+  uint32_t nb = launch_lg_dot_eq(z_, 1, e.lo, e.lo_bits, e.hi, W_, part_, st_);
+  return reduce(nb, 1)[0];
+}
+
+void GpuBackend::lg_add_eq(F128 beta, const std::vector<F128>& zp) {
+  scr_off_ = 0;
+  if (!lg_base_) throw std::runtime_error("basis update expects the base stage");
+  EqSplit e = eq_split(zp, beta, 10);
+  launch_lg_eq_fill(e.lo, e.lo_bits, e.hi, W_, lb128_, true, st_);
+}
+
+Msg256 GpuBackend::lg_message(size_t d) {
+  uint64_t n = lg_n_;
+  if (d == 1 || n == d) d = 1;
+  Msg256 m;
+  if (lg_base_) {
+    uint32_t nb = launch_lg_message128(z_, lb128_, n, d, part_, st_);
+    auto v = reduce(nb, 2);
+    m.u0 = F256(v[0]);
+    m.u2 = F256(v[1]);
+  } else {
+    uint32_t nb = launch_lg_message256(lf_[lg_cur_], lb_[lg_cur_], n, d, part_, st_);
+    auto v = reduce(nb, 4);
+    m.u0 = F256(v[0], v[1]);
+    m.u2 = F256(v[2], v[3]);
+  }
+  return m;
+}
+
+void GpuBackend::lg_fold(F256 r, size_t d) {
+  uint64_t n_out = lg_n_ / 2;
+  if (lg_base_) {
+    launch_lg_fold128(z_, lb128_, n_out, dev(r), d, lf_[0], lb_[0], st_);
+    lg_cur_ = 0;
+    lg_base_ = false;
+  } else {
+    int nx = lg_cur_ ^ 1;
+    launch_lg_fold256(lf_[lg_cur_], lb_[lg_cur_], n_out, dev(r), d, lf_[nx], lb_[nx], st_);
+    lg_cur_ = nx;
+  }
+  lg_n_ = n_out;
+}
+
+void GpuBackend::lg_code_switch() {
+  if (lg_base_) throw std::runtime_error("code switch before the first fold");
+  if (2 * lg_n_ > W_ / 2) throw std::runtime_error("code switch exceeds the Ligerito buffers");
+  int nx = lg_cur_ ^ 1;
+  launch_lg_code_switch(lf_[lg_cur_], lb_[lg_cur_], lg_n_, lf_[nx], lb_[nx], st_);
+  lg_cur_ = nx;
+  lg_n_ *= 2;
+}
+
+void GpuBackend::lg_commit(uint32_t level, uint32_t log_cols, uint32_t log_lanes, uint32_t log_rate,
+                           uint32_t cap_depth, std::vector<Hash>& cap) {
+  if (lg_n_ != (uint64_t(1) << (log_cols + log_lanes))) throw std::runtime_error("Ligerito commit size mismatch");
+  if (levels_.size() < level + 1) levels_.resize(level + 1);
+  Level& L = levels_[level];
+  uint64_t block_len = uint64_t(1) << (log_cols + log_rate);
+  uint32_t lanes = 1u << log_lanes;
+  if (L.block_len != block_len || L.lanes != lanes) {
+    if (L.mat) { cudaFree(L.mat); cudaFree(L.tree); }
+    CUDA_OK(cudaMalloc(&L.mat, block_len * lanes * sizeof(F128d)));
+    CUDA_OK(cudaMalloc(&L.tree, 2 * block_len * 32));
+    L.block_len = block_len;
+    L.lanes = lanes;
+  }
+  launch_lg_replicate(lf_[lg_cur_], lg_n_, block_len * lanes, L.mat, st_);
+  launch_ntt(L.mat, lanes, log_cols + log_rate, log_rate, twiddles(log_cols + log_rate), st_);
+  launch_merkle(L.mat, lanes, block_len, L.tree, st_);
+  cap = read_cap(L.tree, block_len, cap_depth);
+}
+
+Msg256 GpuBackend::lg_introduce_eq(const std::vector<F128>& zp, F128& answer) {
+  scr_off_ = 0;
+  if ((uint64_t(1) << zp.size()) != lg_n_) throw std::runtime_error("OOD point size mismatch");
+  EqSplit e = eq_split(zp, F128::one(), 10);
+  uint32_t nb = launch_lg_intro_eq(lf_[lg_cur_], e.lo, e.lo_bits, e.hi, lg_n_, pend_, part_, st_);
+  auto v = reduce(nb, 3);
+  answer = v[0];
+  pend_induced_ = false;
+  pend_n_ = lg_n_;
+  Msg256 m;
+  m.u0 = F256(v[1]);
+  m.u2 = F256(v[2]);
+  return m;
+}
+
+Msg256 GpuBackend::lg_introduce_induced(uint32_t ln, const std::vector<F128>& w,
+                                        const std::vector<std::vector<F128>>& what) {
+  scr_off_ = 0;
+  if ((uint64_t(2) << ln) != lg_n_) throw std::runtime_error("induced basis size mismatch");
+  uint32_t nq = (uint32_t)w.size();
+  std::vector<F128> flat;
+  flat.reserve((size_t)nq * ln);
+  for (auto& q : what) flat.insert(flat.end(), q.begin(), q.end());
+  const F128d* dwhat = upload(flat);
+  const F128d* dw = upload(w);
+  uint32_t lo_bits = ln / 2;
+  F128d* lo_tab = static_cast<F128d*>(scratch((size_t)nq * (size_t(16) << lo_bits)));
+  F128d* hi_tab = static_cast<F128d*>(scratch((size_t)nq * (size_t(16) << (ln - lo_bits))));
+  uint32_t nb = launch_lg_induced(dwhat, dw, nq, ln, lf_[lg_cur_], lo_tab, hi_tab, pend_, part_, st_);
+  auto v = reduce(nb, 2);
+  pend_induced_ = true;
+  pend_n_ = uint64_t(1) << ln;
+  Msg256 m;
+  m.u0 = F256(v[0]);
+  m.u2 = F256(v[1], v[1]);
+  return m;
+}
+
+void GpuBackend::lg_glue(F128 beta) { launch_lg_glue(lb_[lg_cur_], pend_, dev(beta), pend_n_, pend_induced_, st_); }
+
+void GpuBackend::lg_open(uint32_t level, const std::vector<uint64_t>& pos, uint32_t cap_depth,
+                         std::vector<std::vector<F128>>& rows, std::vector<Hash>& paths) {
+  scr_off_ = 0;
+  const F128d* mat;
+  const uint8_t* tree;
+  uint32_t lanes;
+  uint64_t n_leaves;
+  if (level == 0) { mat = cw0_; tree = tree0_; lanes = S.lanes; n_leaves = n_pos0_; }
+  else { mat = levels_.at(level).mat; tree = levels_.at(level).tree; lanes = levels_[level].lanes; n_leaves = levels_[level].block_len; }
+  uint32_t n = (uint32_t)pos.size();
+  for (uint64_t p : pos)
+    if (p >= n_leaves) throw std::runtime_error("opening position out of range");
+  uint32_t depth = 0;
+  while ((uint64_t(1) << depth) < n_leaves) ++depth;
+  uint32_t plen = depth - cap_depth;
+  const uint64_t* dpos = static_cast<const uint64_t*>(upload(pos.data(), n * 8));
+  F128d* drows = static_cast<F128d*>(scratch((size_t)n * lanes * 16));
+  uint8_t* dpaths = static_cast<uint8_t*>(scratch((size_t)n * plen * 32 + 32));
+  launch_gather_rows(mat, lanes, dpos, n, drows, st_);
+  launch_gather_paths(tree, n_leaves, dpos, n, cap_depth, dpaths, st_);
+  std::vector<F128> hr((size_t)n * lanes);
+  std::vector<Hash> hp((size_t)n * plen);
+  CUDA_OK(cudaMemcpyAsync(hr.data(), drows, hr.size() * 16, cudaMemcpyDeviceToHost, st_));
+  if (plen) CUDA_OK(cudaMemcpyAsync(hp.data(), dpaths, hp.size() * 32, cudaMemcpyDeviceToHost, st_));
+  sync();
+  for (uint32_t q = 0; q < n; ++q) rows.emplace_back(hr.begin() + (size_t)q * lanes, hr.begin() + (size_t)(q + 1) * lanes);
+  paths.insert(paths.end(), hp.begin(), hp.end());
+}
+
+std::vector<F256> GpuBackend::lg_residual() {
+  std::vector<F256> out(lg_n_);
+  CUDA_OK(cudaMemcpyAsync(out.data(), lf_[lg_cur_], lg_n_ * sizeof(F256d), cudaMemcpyDeviceToHost, st_));
+  sync();
+  return out;
+}
+
+}  // namespace gpu
+}  // namespace flock

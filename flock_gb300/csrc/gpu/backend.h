@@ -1,0 +1,137 @@
+// Device backend of prove_fast (one setup = one statement shape, one stream, buffers
+// allocated once and reused by every prove of that shape).
+#pragma once
+#include "kernels.h"
+#include "../host/prover.h"
+#include <map>
+#include <mutex>
+
+namespace flock {
+namespace gpu {
+
+class GpuBackend : public ProverBackend {
+ public:
+  explicit GpuBackend(const Statement& s);
+  ~GpuBackend() override;
+  GpuBackend(const GpuBackend&) = delete;
+  GpuBackend& operator=(const GpuBackend&) = delete;
+
+  void witness(const uint8_t* inputs) override;
+  void commit_l0(uint32_t cap_depth, std::vector<Hash>& cap) override;
+  void zc_round1(const std::vector<F128>& r, std::vector<F128>& ab, std::vector<F128>& c,
+                 std::vector<F128>& s_hat_v_c) override;
+  void zc_fold_skip(const std::vector<F128>& w, const std::vector<F128>& eq_point, F128& g1, F128& ginf) override;
+  void zc_fold(F128 rho, const std::vector<F128>& eq_point, F128& g1, F128& ginf) override;
+  void zc_final(F128 rho, F128& a_eval, F128& b_eval) override;
+  void lc_comb(const std::vector<F128>& skip_w, const std::vector<F128>& x_inner_rest) override;
+  void lc_zvec(const std::vector<F128>& x_outer) override;
+  void lc_start(F128 alpha, F128 beta, uint32_t pin, F128& e1, F128& einf) override;
+  void lc_round(F128 r, bool last, F128& e1, F128& einf) override;
+  void lc_partial(std::vector<F128>& z_partial64) override;
+  void lc_matrix_evals(const std::vector<F128>& rest_point, const std::vector<F128>& zp, F128& ea, F128& eb) override;
+  void lc_s_hat_v(const std::vector<F128>& tail, std::vector<F128>& out128) override;
+  void mo_build_w(const std::vector<WeightClaim>& claims, uint32_t nu, uint64_t area, F128& u0, F128& u2) override;
+  void mo_round(F128 r, bool last, F128& g1, F128& ginf) override;
+  F128 mo_q_eval() override;
+  void lg_basis_eq(F128 gamma, const std::vector<F128>& rho) override;
+  F128 lg_eval_eq(const std::vector<F128>& z) override;
+  void lg_add_eq(F128 beta, const std::vector<F128>& z) override;
+  Msg256 lg_message(size_t d) override;
+  void lg_fold(F256 r, size_t d) override;
+  void lg_code_switch() override;
+  void lg_commit(uint32_t level, uint32_t log_cols, uint32_t log_lanes, uint32_t log_rate, uint32_t cap_depth,
+                 std::vector<Hash>& cap) override;
+  Msg256 lg_introduce_eq(const std::vector<F128>& z, F128& answer) override;
+  Msg256 lg_introduce_induced(uint32_t log_msg_cols, const std::vector<F128>& w,
+                              const std::vector<std::vector<F128>>& what) override;
+  void lg_glue(F128 beta) override;
+  void lg_open(uint32_t level, const std::vector<uint64_t>& positions, uint32_t cap_depth,
+               std::vector<std::vector<F128>>& rows, std::vector<Hash>& paths) override;
+  std::vector<F256> lg_residual() override;
+
+  cudaStream_t stream() const { return st_; }
+  int device() const { return device_; }
+  // Device views for tests of single stages.
+  const F128d* z() const { return z_; }
+  const F128d* codeword0() const { return cw0_; }
+  const uint8_t* tree0() const { return tree0_; }
+  uint64_t words() const { return W_; }
+
+ private:
+  struct EqSplit {
+    const F128d* lo = nullptr;
+    const F128d* hi = nullptr;
+    uint32_t lo_bits = 0;
+  };
+  struct Level {
+    F128d* mat = nullptr;
+    uint8_t* tree = nullptr;
+    uint64_t block_len = 0;
+    uint32_t lanes = 0;
+  };
+
+  void* scratch(size_t bytes);
+  const void* upload(const void* src, size_t bytes);
+  const F128d* upload(const std::vector<F128>& v);
+  void sync();
+  std::vector<F128> reduce(uint32_t n_blocks, uint32_t width);
+  std::vector<F128> fetch(const F128d* d, size_t n);
+  EqSplit eq_split(const std::vector<F128>& point, F128 scale, uint32_t max_lo);
+  const F128d* twiddles(uint32_t log_d);
+  std::vector<Hash> read_cap(const uint8_t* tree, uint64_t n_leaves, uint32_t cap_depth);
+
+  const Statement& S;
+  int device_ = 0;
+  cudaStream_t st_ = nullptr;
+  uint64_t W_ = 0;
+  uint32_t K_ = 0;
+  std::vector<void*> owned_;
+  std::map<uint32_t, F128d*> tw_;
+
+  size_t in_bytes_ = 0;
+  uint8_t* d_in_ = nullptr;
+  uint8_t* h_in_ = nullptr;
+  F128d *z_ = nullptr, *a_ = nullptr, *b_ = nullptr;
+  uint64_t n_pos0_ = 0;
+  F128d* cw0_ = nullptr;
+  uint8_t* tree0_ = nullptr;
+  const F128d* tw0_ = nullptr;
+
+  F128d *zc1a_ = nullptr, *zc1b_ = nullptr, *zc2a_ = nullptr, *zc2b_ = nullptr;
+  F128d *zc_cur_a_ = nullptr, *zc_cur_b_ = nullptr;
+  uint64_t zc_len_ = 0;
+
+  F128d *eqi_ = nullptr, *ca_ = nullptr, *cb_ = nullptr, *comb_ = nullptr, *zv_ = nullptr, *zvcap_ = nullptr;
+  uint32_t *cola_ = nullptr, *rowa_ = nullptr, *colb_ = nullptr, *rowb_ = nullptr;
+  uint32_t lc_len_ = 0;
+
+  F128d *mw_ = nullptr, *moAq_ = nullptr, *moAw_ = nullptr, *moBq_ = nullptr, *moBw_ = nullptr;
+  const F128d* mo_q_ = nullptr;
+  const F128d* mo_w_ = nullptr;
+  uint64_t mo_len_ = 0;
+  F128 mo_final_;
+
+  F128d* lb128_ = nullptr;
+  F256d* lf_[2] = {nullptr, nullptr};
+  F256d* lb_[2] = {nullptr, nullptr};
+  int lg_cur_ = 0;
+  bool lg_base_ = true;
+  uint64_t lg_n_ = 0;
+  F128d* pend_ = nullptr;
+  bool pend_induced_ = false;
+  uint64_t pend_n_ = 0;
+  std::vector<Level> levels_;
+
+  F128d* part_ = nullptr;
+  uint32_t part_cap_ = 0;
+  F128d* red_ = nullptr;
+  F128d* h_red_ = nullptr;
+  uint8_t* scr_ = nullptr;
+  size_t scr_cap_ = 0, scr_off_ = 0;
+  uint8_t* d_stage_ = nullptr;
+  uint8_t* h_stage_ = nullptr;
+  size_t stage_cap_ = 0, stage_off_ = 0;
+};
+
+}  // namespace gpu
+}  // namespace flock

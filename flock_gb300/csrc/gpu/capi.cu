@@ -1,0 +1,141 @@
+// extern "C" entry points declared in include/flock_gb300.h.
+#include "../../../include/flock_gb300.h"
+#include "backend.h"
+#include <cstdlib>
+#include <memory>
+
+using namespace flock;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+// Statements are shared by every setup of the same (kind, n_blocks): building the
+// matrices and the registry digest is the expensive part of Setup::new.
+std::shared_ptr<Statement> statement_for(HashKind h, uint32_t n) {
+  static std::mutex mu;
+  static std::map<std::pair<int, uint32_t>, std::shared_ptr<Statement>> cache;
+  std::lock_guard<std::mutex> g(mu);
+  auto key = std::make_pair((int)h, n);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  auto s = std::make_shared<Statement>(make_statement(h, n));
+  compute_registry_digest(*s);
+  cache[key] = s;
+  return s;
+}
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    return f();
+  } catch (const std::invalid_argument& e) {
+    return fail(FLOCK_GB300_EINVAL, e.what());
+  } catch (const std::runtime_error& e) {
+    std::string w = e.what();
+    return fail(w.rfind("CUDA error", 0) == 0 ? FLOCK_GB300_ECUDA : FLOCK_GB300_EINTERNAL, w);
+  } catch (const std::exception& e) {
+    return fail(FLOCK_GB300_EINTERNAL, e.what());
+  } catch (...) {
+    return fail(FLOCK_GB300_EINTERNAL, "unknown error");
+  }
+}
+
+}  // namespace
+
+struct flock_gb300_setup {
+  std::shared_ptr<Statement> stmt;
+  std::unique_ptr<gpu::GpuBackend> backend;
+  std::mutex mu;
+  ProveTimings last;
+};
+
+extern "C" {
+
+size_t flock_gb300_input_record_bytes(int hash_kind) {
+  if (hash_kind < 0 || hash_kind > 2) return 0;
+  return input_record_bytes((HashKind)hash_kind);
+}
+
+int flock_gb300_setup_new(int hash_kind, uint64_t n_blocks, flock_gb300_setup** out) {
+  g_last_error.clear();
+  if (!out) return fail(FLOCK_GB300_EINVAL, "null output pointer");
+  *out = nullptr;
+  if (hash_kind < 0 || hash_kind > 2) return fail(FLOCK_GB300_EINVAL, "unknown hash kind");
+  if (n_blocks < 8 || (n_blocks & (n_blocks - 1)) || n_blocks > (uint64_t(1) << 24))
+    return fail(FLOCK_GB300_EINVAL, "n_blocks must be a power of two in [8, 2^24]");
+  return guarded([&] {
+    auto s = std::make_unique<flock_gb300_setup>();
+    s->stmt = statement_for((HashKind)hash_kind, (uint32_t)n_blocks);
+    s->backend = std::make_unique<gpu::GpuBackend>(*s->stmt);
+    *out = s.release();
+    return FLOCK_GB300_OK;
+  });
+}
+
+void flock_gb300_setup_free(flock_gb300_setup* setup) { delete setup; }
+
+int flock_gb300_setup_info(const flock_gb300_setup* setup, uint32_t* m, uint32_t* lanes, uint8_t digest[32]) {
+  if (!setup) return fail(FLOCK_GB300_EINVAL, "null setup");
+  if (m) *m = setup->stmt->m;
+  if (lanes) *lanes = setup->stmt->lanes;
+  if (digest) memcpy(digest, setup->stmt->registry_digest.data(), 32);
+  return FLOCK_GB300_OK;
+}
+
+int flock_gb300_prove_fast(flock_gb300_setup* setup, const void* inputs, size_t n_inputs, const uint8_t* domain,
+                           size_t domain_len, uint8_t** out, size_t* out_len) {
+  g_last_error.clear();
+  if (!setup || !inputs || !out || !out_len || (!domain && domain_len))
+    return fail(FLOCK_GB300_EINVAL, "null argument");
+  *out = nullptr;
+  *out_len = 0;
+  if (n_inputs != setup->stmt->n_blocks)
+    return fail(FLOCK_GB300_EINVAL, "input count " + std::to_string(n_inputs) + " != setup n_blocks " +
+                                        std::to_string(setup->stmt->n_blocks));
+  return guarded([&] {
+    std::lock_guard<std::mutex> g(setup->mu);
+    CUDA_OK(cudaSetDevice(setup->backend->device()));
+    ProveResult R = prove_fast(*setup->stmt, *setup->backend, static_cast<const uint8_t*>(inputs), domain, domain_len);
+    setup->last = R.t;
+    std::vector<uint8_t> pb = proof_bytes(R.proof);
+    size_t len = 8 + pb.size() + 8 + 32 * R.cap.size() + 32;
+    uint8_t* buf = static_cast<uint8_t*>(malloc(len));
+    if (!buf) return fail(FLOCK_GB300_EINTERNAL, "out of host memory");
+    size_t o = 0;
+    auto u64 = [&](uint64_t v) { for (int i = 0; i < 8; ++i) buf[o++] = (uint8_t)(v >> (8 * i)); };
+    u64(pb.size());
+    memcpy(buf + o, pb.data(), pb.size());
+    o += pb.size();
+    u64(R.cap.size());
+    for (auto& h : R.cap) { memcpy(buf + o, h.data(), 32); o += 32; }
+    for (F128 v : {R.claims.ab_value, R.claims.c_value}) { u64(v.lo); u64(v.hi); }
+    *out = buf;
+    *out_len = len;
+    return FLOCK_GB300_OK;
+  });
+}
+
+int flock_gb300_last_phase_ms(const flock_gb300_setup* setup, double out[6]) {
+  if (!setup || !out) return fail(FLOCK_GB300_EINVAL, "null argument");
+  const ProveTimings& t = setup->last;
+  out[0] = t.witness; out[1] = t.commit; out[2] = t.zerocheck; out[3] = t.lincheck; out[4] = t.open; out[5] = t.total;
+  return FLOCK_GB300_OK;
+}
+
+void flock_gb300_free(uint8_t* p) { free(p); }
+
+int flock_gb300_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+  return n;
+}
+
+const char* flock_gb300_last_error(void) { return g_last_error.c_str(); }
+
+}  // extern "C"

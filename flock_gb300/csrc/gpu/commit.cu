@@ -1,0 +1,218 @@
+// Commitment kernels: the lane-major codeword fill, the additive NTT over GF(2^128)
+// (LCH novel basis, neighbours-last: at layer l pairs are 2^(log_d - l - 1) apart and
+// share the twiddle of their block; crates/flock-core/src/ntt/additive_ntt_f128.rs:
+// 627-648), Merkle trees over codeword rows (crates/flock-core/src/merkle.rs:593-620)
+// and the row / capped-path gathers of Ligerito openings
+// (crates/flock-core/src/pcs/ligerito.rs:4582-4610, merkle.rs:663-690).
+//
+// Layout: codewords are position-major SoA, data[pos * lanes + lane]; a Merkle leaf is
+// one position's `lanes` words. Trees are flat: leaves [0, N), then each level, root last.
+#include "kernels.h"
+#include "sha256.cuh"
+
+namespace flock {
+namespace gpu {
+
+// cw[(rep * D + p) * lanes + l] = q[l * D + p]: 2^(log_pos - log_dim) replicas of the
+// transposed lane-major stack (the state after the first log_inv_rate NTT layers).
+// Tiled through shared memory: a 32-position x 32-lane tile per block.
+__global__ void fill_lane_major_kernel(const F128d* __restrict__ q, F128d* __restrict__ cw, uint32_t lanes,
+                                       uint32_t log_dim, uint64_t n_pos) {
+  __shared__ F128d tile[32][33];
+  uint64_t p0 = (uint64_t)blockIdx.x * 32;
+  uint32_t l0 = blockIdx.y * 32;
+  uint64_t D = 1ull << log_dim;
+  // read: lane-major, consecutive threads -> consecutive positions
+  for (int ly = threadIdx.y; ly < 32; ly += blockDim.y) {
+    uint32_t l = l0 + ly;
+    uint64_t p = p0 + threadIdx.x;
+    if (l < lanes && p < n_pos) tile[ly][threadIdx.x] = q[(uint64_t)l * D + (p & (D - 1))];
+  }
+  __syncthreads();
+  // write: position-major, consecutive threads -> consecutive lanes
+  for (int py = threadIdx.y; py < 32; py += blockDim.y) {
+    uint64_t p = p0 + py;
+    uint32_t l = l0 + threadIdx.x;
+    if (l < lanes && p < n_pos) cw[p * lanes + l] = tile[threadIdx.x][py];
+  }
+}
+
+void launch_fill_lane_major(const F128d* q, F128d* cw, uint32_t lanes, uint32_t log_dim, uint32_t log_pos,
+                            cudaStream_t s) {
+  uint64_t n_pos = 1ull << log_pos;
+  dim3 grid((unsigned)((n_pos + 31) / 32), (lanes + 31) / 32), block(32, 8);
+  fill_lane_major_kernel<<<grid, block, 0, s>>>(q, cw, lanes, log_dim, n_pos);
+  CUDA_OK(cudaGetLastError());
+}
+
+// One butterfly layer: thread per (pair, lane). tw[(1 << layer) - 1 + block].
+__global__ void ntt_layer_kernel(F128d* __restrict__ data, uint32_t lanes, uint32_t log_d, uint32_t layer,
+                                 const F128d* __restrict__ tw) {
+  uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t n_pairs = 1ull << (log_d - 1);
+  if (gid >= n_pairs * lanes) return;
+  uint64_t pair = gid / lanes;
+  uint32_t l = (uint32_t)(gid - pair * lanes);
+  uint32_t sh = log_d - layer - 1;
+  uint64_t block = pair >> sh, within = pair & ((1ull << sh) - 1);
+  uint64_t i0 = (block << (sh + 1)) + within, i1 = i0 + (1ull << sh);
+  F128d t = tw[(1ull << layer) - 1 + block];
+  F128d u = data[i0 * lanes + l], v = data[i1 * lanes + l];
+  F128d nu = u + v * t;
+  data[i0 * lanes + l] = nu;
+  data[i1 * lanes + l] = v + nu;
+}
+
+// Several consecutive layers [layer, layer + nl) fused through shared memory. A block
+// owns 2^nl positions spaced 2^(log_d - layer - nl) apart (one residue class inside a
+// block of the first fused layer) for a slice of lanes; each fused layer pairs positions
+// within that set.
+template <int NL>
+__global__ void ntt_fused_kernel(F128d* __restrict__ data, uint32_t lanes, uint32_t log_d, uint32_t layer,
+                                 const F128d* __restrict__ tw, uint32_t lane_tile) {
+  extern __shared__ F128d sm[];  // [2^NL][lane_tile]
+  const uint32_t P = 1u << NL;
+  uint32_t stride_log = log_d - layer - NL;  // spacing of the positions in this group
+  uint64_t n_groups = 1ull << (log_d - NL);
+  uint64_t lane_tiles = (lanes + lane_tile - 1) / lane_tile;
+  uint64_t gidx = blockIdx.x / lane_tiles;
+  uint32_t lt = (uint32_t)(blockIdx.x % lane_tiles);
+  if (gidx >= n_groups) return;
+  // group -> (outer block of the first fused layer, residue within stride)
+  uint64_t outer = gidx >> stride_log, resid = gidx & ((1ull << stride_log) - 1);
+  uint64_t base = (outer << (stride_log + NL)) + resid;
+  uint32_t l0 = lt * lane_tile;
+  uint32_t nl_here = min(lane_tile, lanes - l0);
+  for (uint32_t i = threadIdx.x; i < P * nl_here; i += blockDim.x) {
+    uint32_t pos = i / nl_here, l = i - pos * nl_here;
+    sm[pos * lane_tile + l] = data[(base + ((uint64_t)pos << stride_log)) * lanes + l0 + l];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NL; ++k) {
+    uint32_t L = layer + k;
+    uint32_t half = P >> (k + 1);  // pairing distance inside the group (in group positions)
+    for (uint32_t i = threadIdx.x; i < (P / 2) * nl_here; i += blockDim.x) {
+      uint32_t pr = i / nl_here, l = i - pr * nl_here;
+      uint32_t blk = pr / half, w = pr - blk * half;
+      uint32_t i0 = blk * 2 * half + w, i1 = i0 + half;
+      // global block index at layer L of position i0
+      uint64_t gpos = base + ((uint64_t)i0 << stride_log);
+      uint64_t gblock = gpos >> (log_d - L);
+      F128d t = tw[(1ull << L) - 1 + gblock];
+      F128d u = sm[i0 * lane_tile + l], v = sm[i1 * lane_tile + l];
+      F128d nu = u + v * t;
+      sm[i0 * lane_tile + l] = nu;
+      sm[i1 * lane_tile + l] = v + nu;
+    }
+    __syncthreads();
+  }
+  for (uint32_t i = threadIdx.x; i < P * nl_here; i += blockDim.x) {
+    uint32_t pos = i / nl_here, l = i - pos * nl_here;
+    data[(base + ((uint64_t)pos << stride_log)) * lanes + l0 + l] = sm[pos * lane_tile + l];
+  }
+}
+
+void launch_ntt(F128d* data, uint32_t lanes, uint32_t log_d, uint32_t start_layer, const F128d* tw, cudaStream_t s) {
+  const int NL = 6;  // layers fused per pass
+  uint32_t layer = start_layer;
+  uint32_t lane_tile = lanes < 64 ? lanes : 64;
+  while (layer < log_d) {
+    uint32_t remaining = log_d - layer;
+    if (remaining >= (uint32_t)NL) {
+      uint64_t n_groups = 1ull << (log_d - NL);
+      uint64_t lane_tiles = (lanes + lane_tile - 1) / lane_tile;
+      size_t smem = (size_t)(1u << NL) * lane_tile * sizeof(F128d);
+      static bool attr = false;
+      if (!attr) {
+        CUDA_OK(cudaFuncSetAttribute(ntt_fused_kernel<NL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)((1u << NL) * 64 * sizeof(F128d))));
+        attr = true;
+      }
+      ntt_fused_kernel<NL><<<(unsigned)(n_groups * lane_tiles), 256, smem, s>>>(data, lanes, log_d, layer, tw,
+                                                                                 lane_tile);
+      CUDA_OK(cudaGetLastError());
+      layer += NL;
+    } else {
+      uint64_t work = (1ull << (log_d - 1)) * lanes;
+      ntt_layer_kernel<<<(unsigned)((work + 255) / 256), 256, 0, s>>>(data, lanes, log_d, layer, tw);
+      CUDA_OK(cudaGetLastError());
+      layer += 1;
+    }
+  }
+}
+
+// ---- Merkle
+__global__ void merkle_leaves_kernel(const F128d* __restrict__ rows, uint32_t lanes, uint64_t n_leaves,
+                                     uint32_t* __restrict__ tree) {
+  uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n_leaves) return;
+  const uint32_t* w = (const uint32_t*)(rows + p * lanes);
+  uint32_t out[8];
+  sha256_words([&](uint32_t i) { return __ldg(w + i); }, lanes * 4, out);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) tree[p * 8 + i] = out[i];
+}
+__global__ void merkle_level_kernel(uint32_t* __restrict__ tree, uint64_t in_off, uint64_t n_out) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_out) return;
+  const uint32_t* l = tree + (in_off + 2 * i) * 8;
+  uint32_t out[8];
+  sha256_words([&](uint32_t k) { return l[k]; }, 16, out);
+  uint64_t o = in_off + 2 * n_out + i;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) tree[o * 8 + k] = out[k];
+}
+void launch_merkle(const F128d* rows, uint32_t lanes, uint64_t n_leaves, uint8_t* tree, cudaStream_t s) {
+  merkle_leaves_kernel<<<(unsigned)((n_leaves + 127) / 128), 128, 0, s>>>(rows, lanes, n_leaves, (uint32_t*)tree);
+  CUDA_OK(cudaGetLastError());
+  uint64_t off = 0, len = n_leaves;
+  while (len > 1) {
+    uint64_t nout = len / 2;
+    merkle_level_kernel<<<(unsigned)((nout + 127) / 128), 128, 0, s>>>((uint32_t*)tree, off, nout);
+    CUDA_OK(cudaGetLastError());
+    off += len;
+    len = nout;
+  }
+}
+
+// ---- openings
+__global__ void gather_rows_kernel(const F128d* __restrict__ mat, uint32_t lanes, const uint64_t* __restrict__ pos,
+                                   uint32_t n, F128d* __restrict__ out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * lanes) return;
+  uint32_t q = i / lanes, l = i - q * lanes;
+  out[i] = mat[pos[q] * lanes + l];
+}
+void launch_gather_rows(const F128d* mat, uint32_t lanes, const uint64_t* d_pos, uint32_t n, F128d* out,
+                        cudaStream_t s) {
+  uint32_t work = n * lanes;
+  gather_rows_kernel<<<(work + 255) / 256, 256, 0, s>>>(mat, lanes, d_pos, n, out);
+  CUDA_OK(cudaGetLastError());
+}
+__global__ void gather_paths_kernel(const uint8_t* __restrict__ tree, uint64_t n_leaves,
+                                    const uint64_t* __restrict__ pos, uint32_t n, uint32_t cap_depth,
+                                    uint8_t* __restrict__ out) {
+  uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  uint32_t depth = 0;
+  while ((1ull << depth) < n_leaves) ++depth;
+  uint32_t plen = depth - cap_depth;
+  uint64_t start = 0, len = n_leaves, idx = pos[q];
+  for (uint32_t k = 0; k < plen; ++k) {
+    const uint8_t* src = tree + (start + (idx ^ 1)) * 32;
+    uint8_t* dst = out + ((uint64_t)q * plen + k) * 32;
+    for (int b = 0; b < 32; ++b) dst[b] = src[b];
+    start += len;
+    len >>= 1;
+    idx >>= 1;
+  }
+}
+void launch_gather_paths(const uint8_t* tree, uint64_t n_leaves, const uint64_t* d_pos, uint32_t n,
+                         uint32_t cap_depth, uint8_t* out, cudaStream_t s) {
+  gather_paths_kernel<<<(n + 127) / 128, 128, 0, s>>>(tree, n_leaves, d_pos, n, cap_depth, out);
+  CUDA_OK(cudaGetLastError());
+}
+
+}  // namespace gpu
+}  // namespace flock

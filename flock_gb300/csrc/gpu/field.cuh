@@ -1,0 +1,105 @@
+// Device arithmetic in GF(2^128) (x^128 + x^7 + x^2 + x + 1, lo = x^0..x^63) and
+// GF(2^256) = F128[u]/(u^2 + u + x^-1), the fields of the prove_fast path
+// (crates/flock-core/src/field/gf2_128.rs, gf2_256.rs).
+//
+// sm_103a has no carry-less multiply instruction. A 32x32 -> 64 carry-less product is
+// formed from sixteen 32x32 -> 64 integer multiplies of operands thinned to every
+// fourth bit ("holes"): within one residue class mod 4 each product column receives at
+// most 8 partial products, so no carry reaches the next bit of the same class and the
+// class bits of the integer product are the GF(2) sums. The four classes are masked and
+// merged. Two Karatsuba levels build the 128 x 128 product from nine such products,
+// followed by the shift-and-fold reduction.
+#pragma once
+#include <cstdint>
+
+namespace flock {
+namespace gpu {
+
+struct __align__(16) F128d {
+  uint64_t lo, hi;
+};
+struct __align__(16) F256d {
+  F128d c0, c1;
+};
+
+__device__ __forceinline__ F128d f128(uint64_t lo, uint64_t hi) { F128d r; r.lo = lo; r.hi = hi; return r; }
+__device__ __forceinline__ F128d f128_zero() { return f128(0, 0); }
+__device__ __forceinline__ F128d f128_one() { return f128(1, 0); }
+__device__ __forceinline__ F128d operator+(F128d a, F128d b) { return f128(a.lo ^ b.lo, a.hi ^ b.hi); }
+__device__ __forceinline__ F128d& operator+=(F128d& a, F128d b) { a.lo ^= b.lo; a.hi ^= b.hi; return a; }
+__device__ __forceinline__ bool is_zero(F128d a) { return (a.lo | a.hi) == 0; }
+
+__device__ __forceinline__ uint64_t mulw(uint32_t a, uint32_t b) { return (uint64_t)a * (uint64_t)b; }
+
+// 32 x 32 -> 64 carry-less product.
+__device__ __forceinline__ uint64_t clmul32(uint32_t x, uint32_t y) {
+  const uint32_t m0 = 0x11111111u, m1 = 0x22222222u, m2 = 0x44444444u, m3 = 0x88888888u;
+  uint32_t x0 = x & m0, x1 = x & m1, x2 = x & m2, x3 = x & m3;
+  uint32_t y0 = y & m0, y1 = y & m1, y2 = y & m2, y3 = y & m3;
+  uint64_t z0 = mulw(x0, y0) ^ mulw(x1, y3) ^ mulw(x2, y2) ^ mulw(x3, y1);
+  uint64_t z1 = mulw(x0, y1) ^ mulw(x1, y0) ^ mulw(x2, y3) ^ mulw(x3, y2);
+  uint64_t z2 = mulw(x0, y2) ^ mulw(x1, y1) ^ mulw(x2, y0) ^ mulw(x3, y3);
+  uint64_t z3 = mulw(x0, y3) ^ mulw(x1, y2) ^ mulw(x2, y1) ^ mulw(x3, y0);
+  const uint64_t M0 = 0x1111111111111111ull, M1 = 0x2222222222222222ull, M2 = 0x4444444444444444ull,
+                 M3 = 0x8888888888888888ull;
+  return (z0 & M0) | (z1 & M1) | (z2 & M2) | (z3 & M3);
+}
+
+// 64 x 64 -> 128 carry-less product (Karatsuba over 32-bit halves).
+__device__ __forceinline__ void clmul64(uint64_t a, uint64_t b, uint64_t& lo, uint64_t& hi) {
+  uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32), b0 = (uint32_t)b, b1 = (uint32_t)(b >> 32);
+  uint64_t l = clmul32(a0, b0), h = clmul32(a1, b1), m = clmul32(a0 ^ a1, b0 ^ b1) ^ l ^ h;
+  lo = l ^ (m << 32);
+  hi = h ^ (m >> 32);
+}
+
+__device__ __forceinline__ F128d ghash_reduce(uint64_t r0, uint64_t r1, uint64_t r2, uint64_t r3) {
+  uint64_t t_lo = r2 ^ (r2 << 1) ^ (r2 << 2) ^ (r2 << 7);
+  uint64_t t_hi = r3 ^ ((r3 << 1) | (r2 >> 63)) ^ ((r3 << 2) | (r2 >> 62)) ^ ((r3 << 7) | (r2 >> 57));
+  uint64_t ov = (r3 >> 63) ^ (r3 >> 62) ^ (r3 >> 57);
+  uint64_t corr = ov ^ (ov << 1) ^ (ov << 2) ^ (ov << 7);
+  return f128(r0 ^ t_lo ^ corr, r1 ^ t_hi);
+}
+
+__device__ __forceinline__ F128d mul(F128d a, F128d b) {
+  uint64_t l0, l1, h0, h1, m0, m1;
+  clmul64(a.lo, b.lo, l0, l1);
+  clmul64(a.hi, b.hi, h0, h1);
+  clmul64(a.lo ^ a.hi, b.lo ^ b.hi, m0, m1);
+  m0 ^= l0 ^ h0;
+  m1 ^= l1 ^ h1;
+  return ghash_reduce(l0, l1 ^ m0, h0 ^ m1, h1);
+}
+__device__ __forceinline__ F128d operator*(F128d a, F128d b) { return mul(a, b); }
+
+__device__ __forceinline__ F128d mul_by_x(F128d z) {
+  uint64_t mask = 0ull - (z.hi >> 63);
+  return f128((z.lo << 1) ^ (0x87ull & mask), (z.hi << 1) | (z.lo >> 63));
+}
+__device__ __forceinline__ F128d mul_by_x_inv(F128d z) {
+  uint64_t mask = 0ull - (z.lo & 1);
+  return f128(((z.lo >> 1) | (z.hi << 63)) ^ (0x43ull & mask), (z.hi >> 1) ^ ((1ull << 63) & mask));
+}
+
+// ---- F256
+__device__ __forceinline__ F256d f256(F128d a, F128d b) { F256d r; r.c0 = a; r.c1 = b; return r; }
+__device__ __forceinline__ F256d f256_base(F128d a) { return f256(a, f128_zero()); }
+__device__ __forceinline__ F256d operator+(F256d a, F256d b) { return f256(a.c0 + b.c0, a.c1 + b.c1); }
+__device__ __forceinline__ F256d& operator+=(F256d& a, F256d b) { a.c0 += b.c0; a.c1 += b.c1; return a; }
+__device__ __forceinline__ F256d operator*(F256d a, F256d b) {
+  F128d p0 = a.c0 * b.c0, p1 = a.c1 * b.c1, p2 = (a.c0 + a.c1) * (b.c0 + b.c1);
+  return f256(p0 + mul_by_x_inv(p1), p2 + p0);
+}
+__device__ __forceinline__ F256d operator*(F256d a, F128d b) { return f256(a.c0 * b, a.c1 * b); }
+
+// ---- warp / block XOR reductions
+__device__ __forceinline__ F128d warp_xor(F128d v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    v.lo ^= __shfl_xor_sync(0xffffffffu, v.lo, o);
+    v.hi ^= __shfl_xor_sync(0xffffffffu, v.hi, o);
+  }
+  return v;
+}
+
+}  // namespace gpu
+}  // namespace flock

@@ -1,0 +1,91 @@
+// Launchers of the sm_103a kernels behind the prove_fast backend. Every launcher runs
+// on the caller's stream; none allocates device memory (the one-time constant uploads
+// excepted: upload_zc_consts and the witness constants live in module memory).
+#pragma once
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include "field.cuh"
+
+#define CUDA_OK(x)                                                                          \
+  do {                                                                                      \
+    cudaError_t e__ = (x);                                                                  \
+    if (e__ != cudaSuccess)                                                                 \
+      throw std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(e__) + " at " + \
+                               __FILE__ + ":" + std::to_string(__LINE__));                  \
+  } while (0)
+
+namespace flock {
+namespace gpu {
+
+int sm_count();
+
+// witness.cu — writes chunk columns [0, used_chunks) of z, a, b
+void launch_witness(int hash, const void* d_inputs, uint32_t n_inst, uint32_t nu, F128d* z, F128d* a, F128d* b,
+                    uint32_t used_chunks, cudaStream_t s);
+
+// commit.cu
+void launch_fill_lane_major(const F128d* q, F128d* cw, uint32_t lanes, uint32_t log_dim, uint32_t log_pos,
+                            cudaStream_t s);
+void launch_ntt(F128d* data, uint32_t lanes, uint32_t log_d, uint32_t start_layer, const F128d* tw, cudaStream_t s);
+void launch_merkle(const F128d* rows, uint32_t lanes, uint64_t n_leaves, uint8_t* tree, cudaStream_t s);
+void launch_gather_rows(const F128d* mat, uint32_t lanes, const uint64_t* d_pos, uint32_t n, F128d* out,
+                        cudaStream_t s);
+void launch_gather_paths(const uint8_t* tree, uint64_t n_leaves, const uint64_t* d_pos, uint32_t n,
+                         uint32_t cap_depth, uint8_t* out, cudaStream_t s);
+
+// sumcheck.cu. Kernels returning a block count wrote per-block partials of the stated
+// width into `part`; launch_reduce_parts XORs them.
+void launch_eq_table(const F128d* d_point, uint32_t n, F128d scale, F128d* out, cudaStream_t s);
+void launch_reduce_parts(const F128d* part, uint32_t n_blocks, uint32_t width, F128d* out, cudaStream_t s);
+
+void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t* gexp, const uint8_t* glog,
+                      const uint8_t mulk[8][256], const uint8_t e2[4]);
+uint32_t launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32_t m, const F128d* eq_lo,
+                          uint32_t lo_bits, const F128d* eq_hi, F128d* part, cudaStream_t s);          // width 256
+uint32_t launch_zc_fold_skip(const F128d* a, const F128d* b, const F128d* w64, uint64_t n_words, const F128d* eq_lo,
+                             uint32_t lo_bits, const F128d* eq_hi, F128d* amlv, F128d* bmlv, F128d* part,
+                             cudaStream_t s);                                                          // width 2
+uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, F128d r, const F128d* eq_lo,
+                          uint32_t lo_bits, const F128d* eq_hi, F128d* aout, F128d* bout, F128d* part, bool msg,
+                          cudaStream_t s);                                                             // width 2
+
+void launch_lc_eq_inner(const F128d* w64, const F128d* er, uint32_t K, F128d* eqi, cudaStream_t s);
+void launch_csc_fold(const uint32_t* col_ptr, const uint32_t* rows, uint32_t K, const F128d* eqi, F128d* out,
+                     cudaStream_t s);
+void launch_lc_zvec(const F128d* z, uint32_t nu, uint32_t used_chunks, const F128d* eq, F128d* part, F128d* zv,
+                    cudaStream_t s);
+uint32_t launch_lc_start(const F128d* ca, const F128d* cb, F128d alpha, F128d beta, uint32_t pin, uint32_t K,
+                         F128d* comb, const F128d* zv, F128d* part, cudaStream_t s);                   // width 2
+uint32_t launch_lc_round(F128d* comb, F128d* zv, uint32_t len, F128d r, bool msg, F128d* part, cudaStream_t s);
+uint32_t launch_lc_matrix_evals(const F128d* ca, const F128d* cb, const F128d* er, const F128d* zp, uint32_t K,
+                                F128d* part, cudaStream_t s);                                          // width 2
+void launch_lc_s_hat_v(const F128d* zv, const F128d* et, uint32_t n_tail, F128d* out, cudaStream_t s);
+
+uint32_t launch_mo_build_w(const F128d* q, const F128d* er0, const F128d* ec0, const F128d* er1, const F128d* ec1,
+                           const F128d* tables, uint32_t nu, uint64_t area, uint64_t n, F128d* w, F128d* part,
+                           cudaStream_t s);                                                            // width 2
+
+void launch_lg_eq_fill(const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, uint64_t n, F128d* out, bool add,
+                       cudaStream_t s);
+uint32_t launch_lg_dot_eq(const F128d* f, uint32_t stride, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi,
+                          uint64_t n, F128d* part, cudaStream_t s);                                    // width 1
+uint32_t launch_lg_message128(const F128d* f, const F128d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s);
+uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s);
+void launch_lg_fold128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, uint64_t d, F256d* fo, F256d* bo,
+                       cudaStream_t s);
+void launch_lg_fold256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, uint64_t d, F256d* fo, F256d* bo,
+                       cudaStream_t s);
+void launch_lg_code_switch(const F256d* f, const F256d* b, uint64_t n, F256d* fo, F256d* bo, cudaStream_t s);
+void launch_lg_replicate(const F256d* f, uint64_t msg, uint64_t total, F128d* mat, cudaStream_t s);
+uint32_t launch_lg_intro_eq(const F256d* f, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, uint64_t n,
+                            F128d* pend, F128d* part, cudaStream_t s);                                 // width 3
+uint32_t launch_lg_induced(const F128d* what, const F128d* w, uint32_t n_q, uint32_t ln, const F256d* f,
+                           F128d* lo_tab, F128d* hi_tab, F128d* basis, F128d* part, cudaStream_t s);   // width 2
+void launch_lg_glue(F256d* b, const F128d* p, F128d beta, uint64_t n, bool induced, cudaStream_t s);
+
+}  // namespace gpu
+}  // namespace flock

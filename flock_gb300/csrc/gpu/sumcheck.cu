@@ -1,0 +1,832 @@
+// Sumcheck-side kernels of prove_fast: the zerocheck round 1 on the skip domain and
+// its folds, the lincheck column folds / row fold / product sumcheck, the merged-open
+// weight build and folds, and the Ligerito F256 ladder (basis tables, folds, messages,
+// code switch, induced basis).
+//
+// Reductions: every message kernel writes per-block XOR partials to `part`
+// (part[block * width + j]); reduce_parts XORs them into `width` values.
+// Eq tables over many variables are never materialised: eq(i) = lo[i & (2^lo_bits - 1)]
+// * hi[i >> lo_bits], and kernels that sum eq-weighted terms walk chunks of 2^lo_bits
+// consecutive indices, summing lo-weighted terms and multiplying by hi once per chunk.
+#include "kernels.h"
+
+namespace flock {
+namespace gpu {
+
+__device__ __forceinline__ F128d block_xor(F128d v, F128d* sh) {
+  v = warp_xor(v);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  F128d r = f128_zero();
+  if (w == 0) {
+    r = l < nw ? sh[l] : f128_zero();
+    r = warp_xor(r);
+  }
+  return r;  // valid in thread 0
+}
+
+__device__ __forceinline__ F128d eq_at(const F128d* lo, uint32_t lo_bits, const F128d* hi, uint64_t i) {
+  F128d l = lo[i & ((1ull << lo_bits) - 1)];
+  return hi ? l * hi[i >> lo_bits] : l;
+}
+
+// ------------------------------------------------------------------ generic pieces
+__global__ void eq_table_kernel(const F128d* __restrict__ p, uint32_t n, F128d scale, F128d* __restrict__ out) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (1ull << n)) return;
+  F128d v = scale;
+  for (uint32_t j = 0; j < n; ++j) {
+    F128d r = p[j];
+    if (!((i >> j) & 1)) r.lo ^= 1;
+    v = v * r;
+  }
+  out[i] = v;
+}
+void launch_eq_table(const F128d* d_point, uint32_t n, F128d scale, F128d* out, cudaStream_t s) {
+  uint64_t len = 1ull << n;
+  eq_table_kernel<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(d_point, n, scale, out);
+  CUDA_OK(cudaGetLastError());
+}
+
+__global__ void reduce_parts_kernel(const F128d* __restrict__ part, uint32_t n_blocks, uint32_t width,
+                                    F128d* __restrict__ out) {
+  __shared__ F128d sh[32];
+  uint32_t col = blockIdx.x;
+  F128d acc = f128_zero();
+  for (uint32_t b = threadIdx.x; b < n_blocks; b += blockDim.x) acc += part[(uint64_t)b * width + col];
+  acc = block_xor(acc, sh);
+  if (threadIdx.x == 0) out[col] = acc;
+}
+void launch_reduce_parts(const F128d* part, uint32_t n_blocks, uint32_t width, F128d* out, cudaStream_t s) {
+  reduce_parts_kernel<<<width, 256, 0, s>>>(part, n_blocks, width, out);
+  CUDA_OK(cudaGetLastError());
+}
+
+static int g_sm_count = 0;
+int sm_count() {
+  if (!g_sm_count) {
+    int dev = 0;
+    CUDA_OK(cudaGetDevice(&dev));
+    CUDA_OK(cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev));
+  }
+  return g_sm_count;
+}
+
+// ------------------------------------------------------------------ zerocheck round 1
+// With the fixed challenges r[6..13) the row eq factorises. For a row x (m - 6 bits)
+// = (K: 3 bits, M: 4 bits, xo):
+//   eq(r[6..m], x) = phi8(e_K) * D * x^M * eq(r[13..m], xo),
+// e_K = prod_j (K_j ? c_j : 1 + c_j) over the three GF(2^8) constants c_j (phi8 is a
+// ring embedding), and D = prod_i (1 + g_i)^-1 over the medium constants g_i = x^(2^i)
+// (the bit-1 factor g/(1+g) and the bit-0 factor 1/(1+g)). Hence per output i
+//   P(i) = D * sum_xo eq_o(xo) * sum_M x^M * phi8( sum_K e_K * p_x(i) )
+// with p_x(i) the GF(2^8) value of the row at Lambda point i. The inner sums are
+// GF(2^8) byte arithmetic; each xo costs one F128 multiply per output. D is applied
+// by the host.
+//   ab[i]  : p = ext(a_x)[i] * ext(b_x)[i]    c[i] : p = ext(z_x)[i]
+//   svc[t] : per word w = (K2: 2 bits, M, xo), p = bit t of z_w with e2 over r[7], r[8].
+struct ZcConsts {
+  uint8_t ext[8 * 256 * 64];
+  F128d phi8[256];
+  uint8_t gexp[512], glog[256];
+  uint8_t mulk[8][256];
+  uint8_t e2[4];
+};
+
+constexpr int ZC_XPB = 4;  // xo groups in flight per block (256 threads each)
+struct ZcStage {
+  F128d wa[64], wb[64], wz[64];
+  uint32_t gab[16][16], gc[16][16];
+  F128d eqo;
+};
+constexpr size_t ZC_CONST_BYTES = (sizeof(ZcConsts) + 15) & ~size_t(15);
+
+__global__ void __launch_bounds__(256 * ZC_XPB, 1)
+zc_round1_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, const F128d* __restrict__ z,
+                 uint64_t n_xo, const ZcConsts* __restrict__ gconst, const F128d* __restrict__ eq_lo,
+                 uint32_t lo_bits, const F128d* __restrict__ eq_hi, F128d* __restrict__ part) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  ZcConsts& C = *reinterpret_cast<ZcConsts*>(smem);
+  ZcStage* stages = reinterpret_cast<ZcStage*>(smem + ZC_CONST_BYTES);
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(gconst);
+    uint4* dst = reinterpret_cast<uint4*>(smem);
+    for (uint32_t i = threadIdx.x; i < sizeof(ZcConsts) / 16; i += blockDim.x) dst[i] = src[i];
+    // tail bytes (struct size need not be a multiple of 16)
+    for (uint32_t i = (sizeof(ZcConsts) / 16) * 16 + threadIdx.x; i < sizeof(ZcConsts); i += blockDim.x)
+      smem[i] = reinterpret_cast<const uint8_t*>(gconst)[i];
+  }
+  const uint32_t sub = threadIdx.x >> 8, t = threadIdx.x & 255;
+  ZcStage& S = stages[sub];
+  const uint32_t* ext32 = reinterpret_cast<const uint32_t*>(C.ext);
+  F128d acc = f128_zero();
+  __syncthreads();
+  const uint64_t n_groups = (n_xo + ZC_XPB - 1) / ZC_XPB;
+  for (uint64_t g = blockIdx.x; g < n_groups; g += gridDim.x) {
+    uint64_t xo = g * ZC_XPB + sub;
+    bool live = xo < n_xo;
+    if (live) {
+      if (t < 64) S.wa[t] = a[xo * 64 + t];
+      else if (t < 128) S.wb[t - 64] = b[xo * 64 + t - 64];
+      else if (t < 192) S.wz[t - 128] = z[xo * 64 + t - 128];
+      else if (t == 192) S.eqo = eq_at(eq_lo, lo_bits, eq_hi, xo);
+    }
+    __syncthreads();
+    if (live) {
+      const uint32_t M = t >> 4, lane = t & 15;
+      uint32_t gab = 0, gc = 0;
+#pragma unroll 1
+      for (uint32_t K = 0; K < 8; ++K) {
+        uint32_t xl = 8 * M + K, w = xl >> 1;
+        uint64_t ab = (xl & 1) ? S.wa[w].hi : S.wa[w].lo;
+        uint64_t bb = (xl & 1) ? S.wb[w].hi : S.wb[w].lo;
+        uint64_t zb = (xl & 1) ? S.wz[w].hi : S.wz[w].lo;
+        uint32_t ea = 0, eb = 0, ec = 0;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          ea ^= ext32[((c << 8) + ((ab >> (8 * c)) & 255)) * 16 + lane];
+          eb ^= ext32[((c << 8) + ((bb >> (8 * c)) & 255)) * 16 + lane];
+          ec ^= ext32[((c << 8) + ((zb >> (8 * c)) & 255)) * 16 + lane];
+        }
+        uint32_t p = 0, q = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          uint32_t x = (ea >> (8 * k)) & 255, y = (eb >> (8 * k)) & 255;
+          uint32_t pr = (x && y) ? C.gexp[C.glog[x] + C.glog[y]] : 0;
+          p |= (uint32_t)C.mulk[K][pr] << (8 * k);
+          q |= (uint32_t)C.mulk[K][(ec >> (8 * k)) & 255] << (8 * k);
+        }
+        gab ^= p;
+        gc ^= q;
+      }
+      S.gab[M][lane] = gab;
+      S.gc[M][lane] = gc;
+    }
+    __syncthreads();
+    if (live) {
+      F128d F = f128_zero();
+      if (t < 128) {
+        const uint8_t* G = reinterpret_cast<const uint8_t*>(t < 64 ? &S.gab[0][0] : &S.gc[0][0]);
+        uint32_t i = t & 63;
+#pragma unroll
+        for (int M = 15; M >= 0; --M) F = mul_by_x(F) + C.phi8[G[M * 64 + i]];
+      } else {
+        uint32_t tb = t - 128, limb = tb >> 6, sh = tb & 63;
+#pragma unroll
+        for (int M = 15; M >= 0; --M) {
+          uint32_t gv = 0;
+#pragma unroll
+          for (int K2 = 0; K2 < 4; ++K2) {
+            const F128d& wv = S.wz[4 * M + K2];
+            uint64_t bits = limb ? wv.hi : wv.lo;
+            if ((bits >> sh) & 1) gv ^= C.e2[K2];
+          }
+          F = mul_by_x(F) + C.phi8[gv];
+        }
+      }
+      acc += S.eqo * F;
+    }
+    __syncthreads();
+  }
+  part[((uint64_t)blockIdx.x * ZC_XPB + sub) * 256 + t] = acc;
+}
+
+static ZcConsts* g_zc_consts = nullptr;
+void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t* gexp, const uint8_t* glog,
+                      const uint8_t mulk[8][256], const uint8_t e2[4]) {
+  if (g_zc_consts) return;
+  ZcConsts* h = new ZcConsts();
+  memcpy(h->ext, ext, sizeof(h->ext));
+  memcpy(h->phi8, phi8, sizeof(h->phi8));
+  memcpy(h->gexp, gexp, 512);
+  memcpy(h->glog, glog, 256);
+  memcpy(h->mulk, mulk, sizeof(h->mulk));
+  memcpy(h->e2, e2, 4);
+  ZcConsts* d = nullptr;
+  CUDA_OK(cudaMalloc(&d, sizeof(ZcConsts)));
+  CUDA_OK(cudaMemcpy(d, h, sizeof(ZcConsts), cudaMemcpyHostToDevice));
+  delete h;
+  g_zc_consts = d;
+}
+
+uint32_t launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32_t m, const F128d* eq_lo,
+                          uint32_t lo_bits, const F128d* eq_hi, F128d* part, cudaStream_t s) {
+  if (!g_zc_consts) throw std::runtime_error("zerocheck constants not uploaded");
+  uint64_t n_xo = 1ull << (m - 13);
+  size_t smem = ZC_CONST_BYTES + ZC_XPB * sizeof(ZcStage);
+  static bool attr = false;
+  if (!attr) {
+    CUDA_OK(cudaFuncSetAttribute(zc_round1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  uint64_t groups = (n_xo + ZC_XPB - 1) / ZC_XPB;
+  uint32_t blocks = (uint32_t)std::min<uint64_t>(groups, (uint64_t)sm_count());
+  zc_round1_kernel<<<blocks, 256 * ZC_XPB, smem, s>>>(a, b, z, n_xo, g_zc_consts, eq_lo, lo_bits, eq_hi, part);
+  CUDA_OK(cudaGetLastError());
+  return blocks * ZC_XPB;  // partial rows of width 256
+}
+
+// ------------------------------------------------------------------ zerocheck skip fold
+// a_mlv[x] = sum_{s in bits(a_x)} w[s] via 8 byte tables of the 64 Lagrange weights;
+// word w holds rows 2w (lo) and 2w+1 (hi), which is exactly the first multilinear pair.
+// Message: g1 = sum_w eq(w) a1 b1, ginf = sum_w eq(w) (a0 + a1)(b0 + b1).
+__global__ void __launch_bounds__(256)
+zc_fold_skip_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, const F128d* __restrict__ w64,
+                    uint64_t n_words, const F128d* __restrict__ eq_lo, uint32_t lo_bits,
+                    const F128d* __restrict__ eq_hi, F128d* __restrict__ amlv, F128d* __restrict__ bmlv,
+                    F128d* __restrict__ part) {
+  __shared__ F128d T[8][256];
+  __shared__ F128d sh[32];
+  for (uint32_t e = threadIdx.x; e < 2048; e += blockDim.x) {
+    uint32_t c = e >> 8, v = e & 255;
+    F128d acc = f128_zero();
+    for (int k = 0; k < 8; ++k)
+      if ((v >> k) & 1) acc += w64[8 * c + k];
+    T[c][v] = acc;
+  }
+  __syncthreads();
+  const uint64_t chunk = 1ull << lo_bits;
+  const uint64_t n_chunks = (n_words + chunk - 1) / chunk;
+  F128d G1 = f128_zero(), GI = f128_zero();
+  for (uint64_t ch = blockIdx.x; ch < n_chunks; ch += gridDim.x) {
+    F128d g1 = f128_zero(), gi = f128_zero();
+    uint64_t end = min(n_words, (ch + 1) * chunk);
+    for (uint64_t wi = ch * chunk + threadIdx.x; wi < end; wi += blockDim.x) {
+      F128d av = a[wi], bv = b[wi];
+      F128d a0 = f128_zero(), a1 = f128_zero(), b0 = f128_zero(), b1 = f128_zero();
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        a0 += T[c][(av.lo >> (8 * c)) & 255];
+        a1 += T[c][(av.hi >> (8 * c)) & 255];
+        b0 += T[c][(bv.lo >> (8 * c)) & 255];
+        b1 += T[c][(bv.hi >> (8 * c)) & 255];
+      }
+      amlv[2 * wi] = a0; amlv[2 * wi + 1] = a1;
+      bmlv[2 * wi] = b0; bmlv[2 * wi + 1] = b1;
+      F128d e = eq_lo[wi & (chunk - 1)];
+      g1 += e * (a1 * b1);
+      gi += e * ((a0 + a1) * (b0 + b1));
+    }
+    g1 = block_xor(g1, sh);
+    gi = block_xor(gi, sh);
+    if (threadIdx.x == 0) {
+      F128d h = eq_hi ? eq_hi[ch] : f128_one();
+      G1 += h * g1;
+      GI += h * gi;
+    }
+  }
+  if (threadIdx.x == 0) { part[blockIdx.x * 2] = G1; part[blockIdx.x * 2 + 1] = GI; }
+}
+uint32_t launch_zc_fold_skip(const F128d* a, const F128d* b, const F128d* w64, uint64_t n_words, const F128d* eq_lo,
+                             uint32_t lo_bits, const F128d* eq_hi, F128d* amlv, F128d* bmlv, F128d* part,
+                             cudaStream_t s) {
+  uint64_t n_chunks = (n_words + (1ull << lo_bits) - 1) >> lo_bits;
+  uint32_t blocks = (uint32_t)std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 8);
+  zc_fold_skip_kernel<<<blocks, 256, 0, s>>>(a, b, w64, n_words, eq_lo, lo_bits, eq_hi, amlv, bmlv, part);
+  CUDA_OK(cudaGetLastError());
+  return blocks;
+}
+
+// ------------------------------------------------------------------ pair fold + message
+// Fold the low variable of two vectors at r (out[i] = in[2i] + r (in[2i+1] + in[2i]))
+// and, unless `msg` is false, emit the pair message over the folded vectors:
+//   g1 = sum_j eq(j) A1 B1, ginf = sum_j eq(j) (A0 + A1)(B0 + B1), (A0, A1) = out[2j..2j+2).
+// eq_lo == nullptr means eq = 1. n_pairs = output length / 2 (>= 1).
+__global__ void __launch_bounds__(256)
+pair_fold_kernel(const F128d* __restrict__ ain, const F128d* __restrict__ bin, uint64_t n_pairs, F128d r,
+                 const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F128d* __restrict__ eq_hi,
+                 F128d* __restrict__ aout, F128d* __restrict__ bout, F128d* __restrict__ part, int msg) {
+  __shared__ F128d sh[32];
+  const uint64_t chunk = 1ull << lo_bits;
+  const uint64_t n_chunks = (n_pairs + chunk - 1) / chunk;
+  F128d G1 = f128_zero(), GI = f128_zero();
+  for (uint64_t ch = blockIdx.x; ch < n_chunks; ch += gridDim.x) {
+    F128d g1 = f128_zero(), gi = f128_zero();
+    uint64_t end = min(n_pairs, (ch + 1) * chunk);
+    for (uint64_t j = ch * chunk + threadIdx.x; j < end; j += blockDim.x) {
+      F128d x0 = ain[4 * j], x1 = ain[4 * j + 1], x2 = ain[4 * j + 2], x3 = ain[4 * j + 3];
+      F128d y0 = bin[4 * j], y1 = bin[4 * j + 1], y2 = bin[4 * j + 2], y3 = bin[4 * j + 3];
+      F128d A0 = x0 + r * (x1 + x0), A1 = x2 + r * (x3 + x2);
+      F128d B0 = y0 + r * (y1 + y0), B1 = y2 + r * (y3 + y2);
+      aout[2 * j] = A0; aout[2 * j + 1] = A1;
+      bout[2 * j] = B0; bout[2 * j + 1] = B1;
+      if (msg) {
+        F128d t1 = A1 * B1, ti = (A0 + A1) * (B0 + B1);
+        if (eq_lo) {
+          F128d e = eq_lo[j & (chunk - 1)];
+          t1 = e * t1;
+          ti = e * ti;
+        }
+        g1 += t1;
+        gi += ti;
+      }
+    }
+    if (msg) {
+      g1 = block_xor(g1, sh);
+      gi = block_xor(gi, sh);
+      if (threadIdx.x == 0) {
+        F128d h = (eq_lo && eq_hi) ? eq_hi[ch] : f128_one();
+        G1 += h * g1;
+        GI += h * gi;
+      }
+    }
+  }
+  if (msg && threadIdx.x == 0) { part[blockIdx.x * 2] = G1; part[blockIdx.x * 2 + 1] = GI; }
+}
+uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, F128d r, const F128d* eq_lo,
+                          uint32_t lo_bits, const F128d* eq_hi, F128d* aout, F128d* bout, F128d* part, bool msg,
+                          cudaStream_t s) {
+  uint64_t n_chunks = (n_pairs + (1ull << lo_bits) - 1) >> lo_bits;
+  uint32_t blocks = (uint32_t)std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 8);
+  pair_fold_kernel<<<blocks, 256, 0, s>>>(ain, bin, n_pairs, r, eq_lo, lo_bits, eq_hi, aout, bout, part, msg ? 1 : 0);
+  CUDA_OK(cudaGetLastError());
+  return blocks;
+}
+
+// ------------------------------------------------------------------ lincheck
+__global__ void lc_eq_inner_kernel(const F128d* __restrict__ w64, const F128d* __restrict__ er, uint32_t K,
+                                   F128d* __restrict__ eqi) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < K) eqi[i] = w64[i & 63] * er[i >> 6];
+}
+void launch_lc_eq_inner(const F128d* w64, const F128d* er, uint32_t K, F128d* eqi, cudaStream_t s) {
+  lc_eq_inner_kernel<<<(K + 255) / 256, 256, 0, s>>>(w64, er, K, eqi);
+  CUDA_OK(cudaGetLastError());
+}
+__global__ void csc_fold_kernel(const uint32_t* __restrict__ col_ptr, const uint32_t* __restrict__ rows,
+                                uint32_t K, const F128d* __restrict__ eqi, F128d* __restrict__ out) {
+  uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= K) return;
+  F128d acc = f128_zero();
+  for (uint32_t p = col_ptr[c]; p < col_ptr[c + 1]; ++p) acc += eqi[rows[p]];
+  out[c] = acc;
+}
+void launch_csc_fold(const uint32_t* col_ptr, const uint32_t* rows, uint32_t K, const F128d* eqi, F128d* out,
+                     cudaStream_t s) {
+  csc_fold_kernel<<<(K + 255) / 256, 256, 0, s>>>(col_ptr, rows, K, eqi, out);
+  CUDA_OK(cudaGetLastError());
+}
+
+// z_vec[128 cc + t] = sum_row eq(row) * bit_t(z[(cc << nu) + row]). Block = (cc, row split),
+// thread = bit t; rows staged through shared memory.
+constexpr uint32_t ZV_TILE = 256;
+__global__ void __launch_bounds__(128)
+lc_zvec_kernel(const F128d* __restrict__ z, uint32_t nu, uint32_t n_split, const F128d* __restrict__ eq,
+               F128d* __restrict__ part) {
+  __shared__ F128d wz[ZV_TILE];
+  __shared__ F128d we[ZV_TILE];
+  uint32_t cc = blockIdx.x / n_split, sp = blockIdx.x % n_split;
+  uint64_t rows = 1ull << nu, per = rows / n_split;
+  uint64_t r0 = sp * per;
+  uint32_t t = threadIdx.x, limb = t >> 5, sh = t & 31;
+  F128d acc = f128_zero();
+  for (uint64_t base = r0; base < r0 + per; base += ZV_TILE) {
+    uint32_t n = (uint32_t)(ZV_TILE < r0 + per - base ? (uint64_t)ZV_TILE : r0 + per - base);
+    __syncthreads();
+    for (uint32_t i = t; i < n; i += blockDim.x) {
+      wz[i] = z[((uint64_t)cc << nu) + base + i];
+      we[i] = eq[base + i];
+    }
+    __syncthreads();
+    for (uint32_t i = 0; i < n; ++i) {
+      const uint32_t* wl = reinterpret_cast<const uint32_t*>(&wz[i]);
+      uint64_t m = 0ull - (uint64_t)((wl[limb] >> sh) & 1);
+      acc.lo ^= we[i].lo & m;
+      acc.hi ^= we[i].hi & m;
+    }
+  }
+  part[(uint64_t)blockIdx.x * 128 + t] = acc;
+}
+__global__ void lc_zvec_reduce_kernel(const F128d* __restrict__ part, uint32_t n_split, uint32_t n_out,
+                                      F128d* __restrict__ zv) {
+  uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;  // o = 128 cc + t
+  if (o >= n_out) return;
+  uint32_t cc = o >> 7, t = o & 127;
+  F128d acc = f128_zero();
+  for (uint32_t sp = 0; sp < n_split; ++sp) acc += part[((uint64_t)cc * n_split + sp) * 128 + t];
+  zv[o] = acc;
+}
+void launch_lc_zvec(const F128d* z, uint32_t nu, uint32_t used_chunks, const F128d* eq, F128d* part, F128d* zv,
+                    cudaStream_t s) {
+  uint32_t n_split = 1;
+  while ((uint64_t)used_chunks * n_split < (uint64_t)sm_count() * 8 && (n_split << 1) <= (1u << nu) / 64)
+    n_split <<= 1;
+  lc_zvec_kernel<<<used_chunks * n_split, 128, 0, s>>>(z, nu, n_split, eq, part);
+  CUDA_OK(cudaGetLastError());
+  uint32_t n_out = used_chunks * 128;
+  lc_zvec_reduce_kernel<<<(n_out + 127) / 128, 128, 0, s>>>(part, n_split, n_out, zv);
+  CUDA_OK(cudaGetLastError());
+}
+
+// comb = alpha comb_a + comb_b (+ beta at pin); message over the top variable:
+//   e1 = sum_i comb[h+i] zv[h+i], einf = sum_i (comb[h+i] + comb[i]) (zv[h+i] + zv[i]).
+__global__ void lc_start_kernel(const F128d* __restrict__ ca, const F128d* __restrict__ cb, F128d alpha, F128d beta,
+                                uint32_t pin, uint32_t K, F128d* __restrict__ comb, const F128d* __restrict__ zv,
+                                F128d* __restrict__ part) {
+  __shared__ F128d sh[32];
+  uint32_t h = K / 2;
+  F128d e1 = f128_zero(), ei = f128_zero();
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < h; i += gridDim.x * blockDim.x) {
+    F128d c0 = alpha * ca[i] + cb[i], c1 = alpha * ca[i + h] + cb[i + h];
+    if (i == pin) c0 += beta;
+    if (i + h == pin) c1 += beta;
+    comb[i] = c0; comb[i + h] = c1;
+    F128d z0 = zv[i], z1 = zv[i + h];
+    e1 += c1 * z1;
+    ei += (c0 + c1) * (z0 + z1);
+  }
+  e1 = block_xor(e1, sh);
+  ei = block_xor(ei, sh);
+  if (threadIdx.x == 0) { part[blockIdx.x * 2] = e1; part[blockIdx.x * 2 + 1] = ei; }
+}
+uint32_t launch_lc_start(const F128d* ca, const F128d* cb, F128d alpha, F128d beta, uint32_t pin, uint32_t K,
+                         F128d* comb, const F128d* zv, F128d* part, cudaStream_t s) {
+  uint32_t blocks = std::max(1u, std::min((K / 2 + 255) / 256, 256u));
+  lc_start_kernel<<<blocks, 256, 0, s>>>(ca, cb, alpha, beta, pin, K, comb, zv, part);
+  CUDA_OK(cudaGetLastError());
+  return blocks;
+}
+// Bind the top variable of comb and zv (length len -> len/2) in place and emit the next
+// top-variable message over the bound vectors (pairs (i, i + len/4)).
+__global__ void lc_round_kernel(F128d* __restrict__ comb, F128d* __restrict__ zv, uint32_t len, F128d r, int msg,
+                                F128d* __restrict__ part) {
+  __shared__ F128d sh[32];
+  uint32_t h = len / 2, q = h / 2;
+  F128d e1 = f128_zero(), ei = f128_zero();
+  if (q == 0) {
+    // len == 2: single bind, no message
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      comb[0] = comb[0] + r * (comb[1] + comb[0]);
+      zv[0] = zv[0] + r * (zv[1] + zv[0]);
+    }
+  } else {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < q; i += gridDim.x * blockDim.x) {
+      F128d c0 = comb[i] + r * (comb[i + h] + comb[i]);
+      F128d c1 = comb[i + q] + r * (comb[i + q + h] + comb[i + q]);
+      F128d z0 = zv[i] + r * (zv[i + h] + zv[i]);
+      F128d z1 = zv[i + q] + r * (zv[i + q + h] + zv[i + q]);
+      comb[i] = c0; comb[i + q] = c1;
+      zv[i] = z0; zv[i + q] = z1;
+      if (msg) {
+        e1 += c1 * z1;
+        ei += (c0 + c1) * (z0 + z1);
+      }
+    }
+  }
+  e1 = block_xor(e1, sh);
+  ei = block_xor(ei, sh);
+  if (threadIdx.x == 0) { part[blockIdx.x * 2] = e1; part[blockIdx.x * 2 + 1] = ei; }
+}
+uint32_t launch_lc_round(F128d* comb, F128d* zv, uint32_t len, F128d r, bool msg, F128d* part, cudaStream_t s) {
+  uint32_t q = len / 4;
+  uint32_t blocks = std::max(1u, std::min((q + 255) / 256, 256u));
+  lc_round_kernel<<<blocks, 256, 0, s>>>(comb, zv, len, r, msg ? 1 : 0, part);
+  CUDA_OK(cudaGetLastError());
+  return blocks;
+}
+// (<w, comb_a>, <w, comb_b>), w[c] = er[c >> 6] * zp[c & 63].
+__global__ void lc_matrix_evals_kernel(const F128d* __restrict__ ca, const F128d* __restrict__ cb,
+                                       const F128d* __restrict__ er, const F128d* __restrict__ zp, uint32_t K,
+                                       F128d* __restrict__ part) {
+  __shared__ F128d sh[32];
+  F128d ea = f128_zero(), eb = f128_zero();
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < K; c += gridDim.x * blockDim.x) {
+    F128d w = er[c >> 6] * zp[c & 63];
+    ea += w * ca[c];
+    eb += w * cb[c];
+  }
+  ea = block_xor(ea, sh);
+  eb = block_xor(eb, sh);
+  if (threadIdx.x == 0) { part[blockIdx.x * 2] = ea; part[blockIdx.x * 2 + 1] = eb; }
+}
+uint32_t launch_lc_matrix_evals(const F128d* ca, const F128d* cb, const F128d* er, const F128d* zp, uint32_t K,
+                                F128d* part, cudaStream_t s) {
+  uint32_t blocks = std::max(1u, std::min((K + 255) / 256, 256u));
+  lc_matrix_evals_kernel<<<blocks, 256, 0, s>>>(ca, cb, er, zp, K, part);
+  CUDA_OK(cudaGetLastError());
+  return blocks;
+}
+// out[b] = sum_k et[k] * zv[b + 128 k]; one block per b.
+__global__ void lc_s_hat_v_kernel(const F128d* __restrict__ zv, const F128d* __restrict__ et, uint32_t n_tail,
+                                  F128d* __restrict__ out) {
+  __shared__ F128d sh[32];
+  uint32_t bb = blockIdx.x;
+  F128d acc = f128_zero();
+  for (uint32_t k = threadIdx.x; k < n_tail; k += blockDim.x) acc += et[k] * zv[bb + 128 * k];
+  acc = block_xor(acc, sh);
+  if (threadIdx.x == 0) out[bb] = acc;
+}
+void launch_lc_s_hat_v(const F128d* zv, const F128d* et, uint32_t n_tail, F128d* out, cudaStream_t s) {
+  lc_s_hat_v_kernel<<<128, 128, 0, s>>>(zv, et, n_tail, out);
+  CUDA_OK(cudaGetLastError());
+}
+
+// ------------------------------------------------------------------ merged open
+// W[d] = sum_c fold_one_slot(er_c[row] * ec_c[col], table_c) for d < area (row = d mod 2^nu,
+// col = d >> nu), else 0; round-0 prime over (q, W): u0 = sum q[2i] W[2i],
+// u2 = sum (q[2i] + q[2i+1]) (W[2i] + W[2i+1]).
+__device__ __forceinline__ F128d fold_slot(F128d x, const F128d* tab) {
+  F128d acc = f128_zero();
+#pragma unroll
+  for (int k = 0; k < 8; ++k) acc += tab[k * 256 + ((x.lo >> (8 * k)) & 255)];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) acc += tab[(8 + k) * 256 + ((x.hi >> (8 * k)) & 255)];
+  return acc;
+}
+__global__ void __launch_bounds__(512, 1)
+mo_build_w_kernel(const F128d* __restrict__ q, const F128d* __restrict__ er0, const F128d* __restrict__ ec0,
+                  const F128d* __restrict__ er1, const F128d* __restrict__ ec1, const F128d* __restrict__ tables,
+                  uint32_t nu, uint64_t area, uint64_t n, F128d* __restrict__ w, F128d* __restrict__ part) {
+  extern __shared__ __align__(16) F128d tab[];  // 2 x 16 x 256
+  __shared__ F128d sh[32];
+  for (uint32_t i = threadIdx.x; i < 2 * 16 * 256; i += blockDim.x) tab[i] = tables[i];
+  __syncthreads();
+  const uint64_t rmask = (1ull << nu) - 1;
+  F128d u0 = f128_zero(), u2 = f128_zero();
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n / 2; i += (uint64_t)gridDim.x * blockDim.x) {
+    F128d W[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      uint64_t d = 2 * i + k;
+      F128d acc = f128_zero();
+      if (d < area) {
+        uint64_t row = d & rmask, col = d >> nu;
+        acc = fold_slot(er0[row] * ec0[col], tab) + fold_slot(er1[row] * ec1[col], tab + 16 * 256);
+      }
+      W[k] = acc;
+      w[d] = acc;
+    }
+    F128d q0 = q[2 * i], q1 = q[2 * i + 1];
+    u0 += q0 * W[0];
+    u2 += (q0 + q1) * (W[0] + W[1]);
+  }
+  u0 = block_xor(u0, sh);
+  u2 = block_xor(u2, sh);
+  if (threadIdx.x == 0) { part[blockIdx.x * 2] = u0; part[blockIdx.x * 2 + 1] = u2; }
+}
+uint32_t launch_mo_build_w(const F128d* q, const F128d* er0, const F128d* ec0, const F128d* er1, const F128d* ec1,
+                           const F128d* tables, uint32_t nu, uint64_t area, uint64_t n, F128d* w, F128d* part,
+                           cudaStream_t s) {
+  size_t smem = 2 * 16 * 256 * sizeof(F128d);
+  static bool attr = false;
+  if (!attr) {
+    CUDA_OK(cudaFuncSetAttribute(mo_build_w_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  uint32_t blocks = (uint32_t)std::min<uint64_t>((n / 2 + 511) / 512, (uint64_t)sm_count());
+  mo_build_w_kernel<<<blocks, 512, smem, s>>>(q, er0, ec0, er1, ec1, tables, nu, area, n, w, part);
+  CUDA_OK(cudaGetLastError());
+  return blocks;
+}
+
+// ------------------------------------------------------------------ Ligerito
+// b[i] = eq(i) (the hi table carries the scale).
+__global__ void lg_eq_fill_kernel(const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F128d* __restrict__ eq_hi,
+                                  uint64_t n, F128d* __restrict__ out, int add) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  F128d e = eq_at(eq_lo, lo_bits, eq_hi, i);
+  if (add) out[i] += e;
+  else out[i] = e;
+}
+void launch_lg_eq_fill(const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, uint64_t n, F128d* out, bool add,
+                       cudaStream_t s) {
+  lg_eq_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(eq_lo, lo_bits, eq_hi, n, out, add ? 1 : 0);
+  CUDA_OK(cudaGetLastError());
+}
+// sum_i f[i * stride] (F128 words) * eq(i), chunked.
+__global__ void lg_dot_eq_kernel(const F128d* __restrict__ f, uint32_t stride, const F128d* __restrict__ eq_lo,
+                                 uint32_t lo_bits, const F128d* __restrict__ eq_hi, uint64_t n,
+                                 F128d* __restrict__ part) {
+  __shared__ F128d sh[32];
+  const uint64_t chunk = 1ull << lo_bits;
+  const uint64_t n_chunks = (n + chunk - 1) / chunk;
+  F128d G = f128_zero();
+  for (uint64_t ch = blockIdx.x; ch < n_chunks; ch += gridDim.x) {
+    F128d g = f128_zero();
+    uint64_t end = min(n, (ch + 1) * chunk);
+    for (uint64_t i = ch * chunk + threadIdx.x; i < end; i += blockDim.x) g += f[i * stride] * eq_lo[i & (chunk - 1)];
+    g = block_xor(g, sh);
+    if (threadIdx.x == 0) G += (eq_hi ? eq_hi[ch] : f128_one()) * g;
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = G;
+}
+uint32_t launch_lg_dot_eq(const F128d* f, uint32_t stride, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi,
+                          uint64_t n, F128d* part, cudaStream_t s) {
+  uint64_t n_chunks = (n + (1ull << lo_bits) - 1) >> lo_bits;
+  uint32_t blocks = (uint32_t)std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 8);
+  lg_dot_eq_kernel<<<blocks, 256, 0, s>>>(f, stride, eq_lo, lo_bits, eq_hi, n, part);
+  CUDA_OK(cudaGetLastError());
+  return blocks;
+}
+
+// Round message with block pairing d: pairs (lo, lo + d), lo = 2 d blk + k.
+//   u0 = sum f[lo] b[lo], u2 = sum (f[lo] + f[hi]) (b[lo] + b[hi]).
+// F128 (base) variant: outputs 2 words per block; F256 variant: 4 words (u0.c0, u0.c1, u2.c0, u2.c1).
+__global__ void lg_message128_kernel(const F128d* __restrict__ f, const F128d* __restrict__ b, uint64_t n, uint64_t d,
+                                     F128d* __restrict__ part) {
+  __shared__ F128d sh[32];
+  F128d u0 = f128_zero(), u2 = f128_zero();
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n / 2; p += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t blk = p / d, k = p - blk * d, lo = 2 * blk * d + k, hi = lo + d;
+    F128d f0 = f[lo], f1 = f[hi], b0 = b[lo], b1 = b[hi];
+    u0 += f0 * b0;
+    u2 += (f0 + f1) * (b0 + b1);
+  }
+  u0 = block_xor(u0, sh);
+  u2 = block_xor(u2, sh);
+  if (threadIdx.x == 0) { part[blockIdx.x * 2] = u0; part[blockIdx.x * 2 + 1] = u2; }
+}
+uint32_t launch_lg_message128(const F128d* f, const F128d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s) {
+  uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n / 2 + 255) / 256, (uint64_t)sm_count() * 8));
+  lg_message128_kernel<<<blocks, 256, 0, s>>>(f, b, n, d, part);
+  CUDA_OK(cudaGetLastError());
+  return blocks;
+}
+__global__ void lg_message256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n, uint64_t d,
+                                     F128d* __restrict__ part) {
+  __shared__ F128d sh[32];
+  F256d u0 = f256(f128_zero(), f128_zero()), u2 = u0;
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n / 2; p += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t blk = p / d, k = p - blk * d, lo = 2 * blk * d + k, hi = lo + d;
+    F256d f0 = f[lo], f1 = f[hi], b0 = b[lo], b1 = b[hi];
+    u0 += f0 * b0;
+    u2 += (f0 + f1) * (b0 + b1);
+  }
+  F128d r0 = block_xor(u0.c0, sh), r1 = block_xor(u0.c1, sh), r2 = block_xor(u2.c0, sh), r3 = block_xor(u2.c1, sh);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x * 4] = r0; part[blockIdx.x * 4 + 1] = r1;
+    part[blockIdx.x * 4 + 2] = r2; part[blockIdx.x * 4 + 3] = r3;
+  }
+}
+uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s) {
+  uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n / 2 + 255) / 256, (uint64_t)sm_count() * 8));
+  lg_message256_kernel<<<blocks, 256, 0, s>>>(f, b, n, d, part);
+  CUDA_OK(cudaGetLastError());
+  return blocks;
+}
+// o[i] = v[lo] + r (v[hi] + v[lo]), i = blk d + k, lo = 2 d blk + k.
+__global__ void lg_fold128_kernel(const F128d* __restrict__ f, const F128d* __restrict__ b, uint64_t n_out, F256d r,
+                                  uint64_t d, F256d* __restrict__ fo, F256d* __restrict__ bo) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_out) return;
+  uint64_t blk = i / d, k = i - blk * d, lo = 2 * blk * d + k, hi = lo + d;
+  F128d f0 = f[lo], df = f[hi] + f0, b0 = b[lo], db = b[hi] + b0;
+  fo[i] = f256(f0 + r.c0 * df, r.c1 * df);
+  bo[i] = f256(b0 + r.c0 * db, r.c1 * db);
+}
+void launch_lg_fold128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, uint64_t d, F256d* fo, F256d* bo,
+                       cudaStream_t s) {
+  lg_fold128_kernel<<<(unsigned)((n_out + 255) / 256), 256, 0, s>>>(f, b, n_out, r, d, fo, bo);
+  CUDA_OK(cudaGetLastError());
+}
+__global__ void lg_fold256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n_out, F256d r,
+                                  uint64_t d, F256d* __restrict__ fo, F256d* __restrict__ bo) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_out) return;
+  uint64_t blk = i / d, k = i - blk * d, lo = 2 * blk * d + k, hi = lo + d;
+  F256d f0 = f[lo], b0 = b[lo];
+  fo[i] = f0 + r * (f[hi] + f0);
+  bo[i] = b0 + r * (b[hi] + b0);
+}
+void launch_lg_fold256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, uint64_t d, F256d* fo, F256d* bo,
+                       cudaStream_t s) {
+  lg_fold256_kernel<<<(unsigned)((n_out + 255) / 256), 256, 0, s>>>(f, b, n_out, r, d, fo, bo);
+  CUDA_OK(cudaGetLastError());
+}
+// f' = (f.c0, f.c1) interleaved as base values; b' = (b, u b).
+__global__ void lg_code_switch_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n,
+                                      F256d* __restrict__ fo, F256d* __restrict__ bo) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  F256d fv = f[i], bv = b[i];
+  fo[2 * i] = f256_base(fv.c0);
+  fo[2 * i + 1] = f256_base(fv.c1);
+  bo[2 * i] = bv;
+  bo[2 * i + 1] = f256(mul_by_x_inv(bv.c1), bv.c0 + bv.c1);
+}
+void launch_lg_code_switch(const F256d* f, const F256d* b, uint64_t n, F256d* fo, F256d* bo, cudaStream_t s) {
+  lg_code_switch_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(f, b, n, fo, bo);
+  CUDA_OK(cudaGetLastError());
+}
+// mat[i] = f[i mod msg].c0
+__global__ void lg_replicate_kernel(const F256d* __restrict__ f, uint64_t msg, uint64_t total, F128d* __restrict__ mat) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < total) mat[i] = f[i & (msg - 1)].c0;
+}
+void launch_lg_replicate(const F256d* f, uint64_t msg, uint64_t total, F128d* mat, cudaStream_t s) {
+  lg_replicate_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(f, msg, total, mat);
+  CUDA_OK(cudaGetLastError());
+}
+// Pending eq basis e = eq(z) over the (base-valued) f of length n: stores e, returns per
+// block (answer = sum f e, u0 = sum f[2j] e[2j], u2 = sum (f0 + f1)(e0 + e1)).
+__global__ void lg_intro_eq_kernel(const F256d* __restrict__ f, const F128d* __restrict__ eq_lo, uint32_t lo_bits,
+                                   const F128d* __restrict__ eq_hi, uint64_t n, F128d* __restrict__ pend,
+                                   F128d* __restrict__ part) {
+  __shared__ F128d sh[32];
+  F128d ans = f128_zero(), u0 = f128_zero(), u2 = f128_zero();
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n / 2; j += (uint64_t)gridDim.x * blockDim.x) {
+    F128d e0 = eq_at(eq_lo, lo_bits, eq_hi, 2 * j), e1 = eq_at(eq_lo, lo_bits, eq_hi, 2 * j + 1);
+    pend[2 * j] = e0;
+    pend[2 * j + 1] = e1;
+    F128d f0 = f[2 * j].c0, f1 = f[2 * j + 1].c0;
+    F128d p0 = f0 * e0;
+    ans += p0 + f1 * e1;
+    u0 += p0;
+    u2 += (f0 + f1) * (e0 + e1);
+  }
+  ans = block_xor(ans, sh);
+  u0 = block_xor(u0, sh);
+  u2 = block_xor(u2, sh);
+  if (threadIdx.x == 0) { part[blockIdx.x * 3] = ans; part[blockIdx.x * 3 + 1] = u0; part[blockIdx.x * 3 + 2] = u2; }
+}
+uint32_t launch_lg_intro_eq(const F256d* f, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, uint64_t n,
+                            F128d* pend, F128d* part, cudaStream_t s) {
+  uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n / 2 + 255) / 256, (uint64_t)sm_count() * 8));
+  lg_intro_eq_kernel<<<blocks, 256, 0, s>>>(f, eq_lo, lo_bits, eq_hi, n, pend, part);
+  CUDA_OK(cudaGetLastError());
+  return blocks;
+}
+// Per-query tensor tables of the induced basis: lo_tab[q][l] = prod_{k < lo_bits, bit k of l}
+// what[q][k]; hi_tab[q][h] = w[q] * prod_{k >= lo_bits, bit (k - lo_bits) of h} what[q][k].
+__global__ void lg_induced_tables_kernel(const F128d* __restrict__ what, const F128d* __restrict__ w, uint32_t n_q,
+                                         uint32_t ln, uint32_t lo_bits, F128d* __restrict__ lo_tab,
+                                         F128d* __restrict__ hi_tab) {
+  uint32_t lo_n = 1u << lo_bits, hi_bits = ln - lo_bits, hi_n = 1u << hi_bits;
+  uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t per = lo_n + hi_n;
+  if (e >= (uint64_t)n_q * per) return;
+  uint32_t q = (uint32_t)(e / per), i = (uint32_t)(e % per);
+  const F128d* wh = what + (uint64_t)q * ln;
+  if (i < lo_n) {
+    F128d v = f128_one();
+    for (uint32_t k = 0; k < lo_bits; ++k)
+      if ((i >> k) & 1) v = v * wh[k];
+    lo_tab[(uint64_t)q * lo_n + i] = v;
+  } else {
+    uint32_t h = i - lo_n;
+    F128d v = w[q];
+    for (uint32_t k = 0; k < hi_bits; ++k)
+      if ((h >> k) & 1) v = v * wh[lo_bits + k];
+    hi_tab[(uint64_t)q * hi_n + h] = v;
+  }
+}
+// basis[i] = sum_q lo_tab[q][i & lo_mask] * hi_tab[q][i >> lo_bits]; with the split
+// f (length 2n): a = sum f[2i] basis[i], s = sum (f[2i] + f[2i+1]) basis[i].
+__global__ void lg_induced_basis_kernel(const F128d* __restrict__ lo_tab, const F128d* __restrict__ hi_tab,
+                                        uint32_t n_q, uint32_t ln, uint32_t lo_bits, const F256d* __restrict__ f,
+                                        F128d* __restrict__ basis, F128d* __restrict__ part) {
+  __shared__ F128d sh[32];
+  uint32_t lo_n = 1u << lo_bits, hi_n = 1u << (ln - lo_bits);
+  uint64_t n = 1ull << ln;
+  F128d A = f128_zero(), Sm = f128_zero();
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t l = (uint32_t)(i & (lo_n - 1)), h = (uint32_t)(i >> lo_bits);
+    F128d acc = f128_zero();
+    for (uint32_t q = 0; q < n_q; ++q) acc += lo_tab[(uint64_t)q * lo_n + l] * hi_tab[(uint64_t)q * hi_n + h];
+    basis[i] = acc;
+    F128d f0 = f[2 * i].c0, f1 = f[2 * i + 1].c0;
+    A += f0 * acc;
+    Sm += (f0 + f1) * acc;
+  }
+  A = block_xor(A, sh);
+  Sm = block_xor(Sm, sh);
+  if (threadIdx.x == 0) { part[blockIdx.x * 2] = A; part[blockIdx.x * 2 + 1] = Sm; }
+}
+uint32_t launch_lg_induced(const F128d* what, const F128d* w, uint32_t n_q, uint32_t ln, const F256d* f,
+                           F128d* lo_tab, F128d* hi_tab, F128d* basis, F128d* part, cudaStream_t s) {
+  uint32_t lo_bits = ln / 2;
+  uint64_t per = (1ull << lo_bits) + (1ull << (ln - lo_bits));
+  uint64_t total = per * n_q;
+  lg_induced_tables_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(what, w, n_q, ln, lo_bits, lo_tab, hi_tab);
+  CUDA_OK(cudaGetLastError());
+  uint64_t n = 1ull << ln;
+  uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, (uint64_t)sm_count() * 8));
+  lg_induced_basis_kernel<<<blocks, 256, 0, s>>>(lo_tab, hi_tab, n_q, ln, lo_bits, f, basis, part);
+  CUDA_OK(cudaGetLastError());
+  return blocks;
+}
+// Glue a pending basis into b with weight beta.
+//   eq mode      : b[i].c0 += beta * p[i]
+//   induced mode : b[2i].c0 += beta * p[i], b[2i+1].c1 += beta * p[i]  (u * base = (0, base))
+__global__ void lg_glue_kernel(F256d* __restrict__ b, const F128d* __restrict__ p, F128d beta, uint64_t n,
+                               int induced) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  F128d v = beta * p[i];
+  if (induced) {
+    b[2 * i].c0 += v;
+    b[2 * i + 1].c1 += v;
+  } else {
+    b[i].c0 += v;
+  }
+}
+void launch_lg_glue(F256d* b, const F128d* p, F128d beta, uint64_t n, bool induced, cudaStream_t s) {
+  lg_glue_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, p, beta, n, induced ? 1 : 0);
+  CUDA_OK(cudaGetLastError());
+}
+
+}  // namespace gpu
+}  // namespace flock

@@ -1,0 +1,122 @@
+"""Host mirror of the reference's prove_fast interface.
+
+    Blake3Setup(n).prove_fast(inputs, domain)       blake3.rs:1589-1652, 1669-1685
+    Sha256HybridSetup(n).prove_fast(inputs, domain) sha2.rs:1185-1268, 1289-1306
+    KeccakSetup(n).prove_fast(inputs, domain)       keccak.rs:847-909, 922-938
+
+(crates/flock-prover/src/r1cs_hashes/). The reference passes a challenger built as
+``FsChallenger::new(domain)``; here the domain bytes are passed and the transcript is
+built inside the library. Inputs are numpy structured arrays (see ``*_DTYPE``) or raw
+bytes of ``n`` packed records. Like the reference's ``assert_eq!(blocks.len(),
+self.n_blocks)``, a wrong count is an error (``FlockError`` with code EINVAL).
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Union
+
+import numpy as np
+
+from . import _native
+from .bundle import ProofBundle
+
+#: Compression {cv[8], m[16], counter, block_len, flags} (blake3.rs:1232)
+BLAKE3_DTYPE = np.dtype([("cv", "<u4", 8), ("m", "<u4", 16), ("counter", "<u8"),
+                         ("block_len", "<u4"), ("flags", "<u4")])
+#: {h[8], w[16]} (sha2.rs:1332)
+SHA256_DTYPE = np.dtype([("h", "<u4", 8), ("w", "<u4", 16)])
+#: 25 lanes, bit j of lane i = state bit 64 i + j
+KECCAK_DTYPE = np.dtype([("lanes", "<u8", 25)])
+
+Inputs = Union[bytes, bytearray, memoryview, np.ndarray]
+
+
+class _Setup:
+    KIND = -1
+    DTYPE: np.dtype = None
+
+    def __init__(self, n_blocks: int):
+        lib = _native.load()
+        h = ctypes.c_void_p()
+        _native.check(lib.flock_gb300_setup_new(self.KIND, int(n_blocks), ctypes.byref(h)))
+        self._h = h
+        self._lib = lib
+        self.n_blocks = int(n_blocks)
+        m, lanes = ctypes.c_uint32(), ctypes.c_uint32()
+        dig = ctypes.create_string_buffer(32)
+        _native.check(lib.flock_gb300_setup_info(h, ctypes.byref(m), ctypes.byref(lanes), dig))
+        self.m = m.value
+        self.lanes = lanes.value
+        self.registry_digest = dig.raw
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.flock_gb300_setup_free(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _buffer(self, inputs: Inputs):
+        if isinstance(inputs, np.ndarray):
+            if inputs.dtype != self.DTYPE:
+                raise TypeError(f"inputs must have dtype {self.DTYPE}")
+            arr = np.ascontiguousarray(inputs)
+            n = arr.shape[0]
+            return arr, arr.ctypes.data, n
+        b = bytes(inputs)
+        rec = self.DTYPE.itemsize
+        if len(b) % rec:
+            raise ValueError(f"input bytes are not a whole number of {rec}-byte records")
+        buf = ctypes.create_string_buffer(b, len(b))
+        return buf, ctypes.addressof(buf), len(b) // rec
+
+    def prove_fast_bytes(self, inputs: Inputs, domain: bytes) -> bytes:
+        """prove_fast; returns the raw proof bundle."""
+        if self._h is None:
+            raise RuntimeError("setup is closed")
+        keep, ptr, n = self._buffer(inputs)
+        out = ctypes.POINTER(ctypes.c_uint8)()
+        out_len = ctypes.c_size_t()
+        _native.check(self._lib.flock_gb300_prove_fast(self._h, ptr, n, domain, len(domain),
+                                                       ctypes.byref(out), ctypes.byref(out_len)))
+        try:
+            return ctypes.string_at(out, out_len.value)
+        finally:
+            self._lib.flock_gb300_free(out)
+        del keep
+
+    def prove_fast(self, inputs: Inputs, domain: bytes) -> ProofBundle:
+        return ProofBundle.parse(self.prove_fast_bytes(inputs, domain))
+
+    def last_phase_ms(self) -> dict:
+        v = (ctypes.c_double * 6)()
+        _native.check(self._lib.flock_gb300_last_phase_ms(self._h, v))
+        return dict(zip(("witness", "commit", "zerocheck", "lincheck", "open", "total"), list(v)))
+
+
+class Blake3Setup(_Setup):
+    KIND = _native.BLAKE3
+    DTYPE = BLAKE3_DTYPE
+
+
+class Sha256HybridSetup(_Setup):
+    KIND = _native.SHA256
+    DTYPE = SHA256_DTYPE
+
+
+class KeccakSetup(_Setup):
+    KIND = _native.KECCAK
+    DTYPE = KECCAK_DTYPE
+
+
+SETUPS = {_native.BLAKE3: Blake3Setup, _native.SHA256: Sha256HybridSetup, _native.KECCAK: KeccakSetup}

@@ -1,0 +1,91 @@
+/* flock_gb300 — C ABI of the GB300 prove_fast path.
+ *
+ * Drop-in boundary for the reference's prove_fast entry points
+ *   Blake3Setup::new / prove_fast        crates/flock-prover/src/r1cs_hashes/blake3.rs:1589-1652, 1669-1685
+ *   Sha256HybridSetup::new / prove_fast  crates/flock-prover/src/r1cs_hashes/sha2.rs:1185-1268, 1289-1306
+ *   KeccakSetup::new / prove_fast        crates/flock-prover/src/r1cs_hashes/keccak.rs:847-909, 922-938
+ * and for the reference's own C ABI of its CUDA prover
+ *   flock_cuda_prove_blake3 / flock_cuda_free / flock_cuda_device_count
+ *                                        cuda-ghash/prove_ffi.cu:366-420
+ *
+ * Conventions (those of prove_ffi.cu): plain pointers and sizes, int status codes (0 = ok),
+ * no exceptions across the boundary, output bytes malloc'd by the library and released
+ * with flock_gb300_free. Unlike prove_ffi.cu, statement constants (R1CS matrices, GF(2^8)
+ * tables, Ligerito configurations) are derived inside the library, and there is no
+ * process-global lock: each setup owns its device buffers and stream, and calls on one
+ * setup are serialised by that setup's own lock.
+ */
+#ifndef FLOCK_GB300_H
+#define FLOCK_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Hash kinds (the three single-type registries of prove_fast). */
+#define FLOCK_GB300_BLAKE3 0
+#define FLOCK_GB300_SHA256 1
+#define FLOCK_GB300_KECCAK 2
+
+/* Status codes. */
+#define FLOCK_GB300_OK 0
+#define FLOCK_GB300_EINVAL 1   /* bad argument: kind, count, sizes, null pointers */
+#define FLOCK_GB300_ECUDA 2    /* a CUDA call failed (message in flock_gb300_last_error) */
+#define FLOCK_GB300_EINTERNAL 3
+
+typedef struct flock_gb300_setup flock_gb300_setup;
+
+/* Input record layouts (little-endian, packed):
+ *   BLAKE3  : { u32 cv[8]; u32 m[16]; u64 counter; u32 block_len; u32 flags; }  112 bytes
+ *             (Compression, blake3.rs:1232)
+ *   SHA-256 : { u32 h[8]; u32 w[16]; }                                           96 bytes
+ *             (sha2.rs:1332)
+ *   Keccak  : { u64 lanes[25]; }  bit j of lane i = state bit 64 i + j           200 bytes
+ *             (keccak.rs:922) */
+size_t flock_gb300_input_record_bytes(int hash_kind);
+
+/* Setup::new(n_blocks): builds the statement (matrices, registry digest, Ligerito
+ * parameters) and allocates the device buffers of one prove of this shape on the
+ * current CUDA device. n_blocks must be a power of two >= 8 (full utilisation).
+ * Replaces Blake3Setup::new / Sha256HybridSetup::new / KeccakSetup::new. */
+int flock_gb300_setup_new(int hash_kind, uint64_t n_blocks, flock_gb300_setup** out);
+void flock_gb300_setup_free(flock_gb300_setup* setup);
+
+/* Committed dimension m, lanes t and the 32-byte registry digest of a setup. */
+int flock_gb300_setup_info(const flock_gb300_setup* setup, uint32_t* m, uint32_t* lanes, uint8_t digest[32]);
+
+/* prove_fast(inputs, &mut FsChallenger::new(domain)) on the GPU. n_inputs must equal the
+ * setup's n_blocks (the reference asserts the same). On success *out receives a malloc'd
+ * proof bundle of *out_len bytes:
+ *   u64 proof_len | proof_len bytes : bincode(R1csProofMergedLigerito)   (proof.rs:43-48)
+ *   u64 cap_len   | cap_len x 32    : Commitment cap (the L0 Merkle cap)
+ *   16 bytes ab_value | 16 bytes c_value : R1csClaim values (F128 lo, hi little-endian)
+ * SHA-256 over the bundle without its two length words is the digest of
+ * crates/flock-prover/tests/union_m6_fixtures.rs:166-180.
+ * Replaces Blake3Setup::prove_fast (blake3.rs:1669), Sha256HybridSetup::prove_fast
+ * (sha2.rs:1289), KeccakSetup::prove_fast (keccak.rs:922) and flock_cuda_prove_blake3
+ * (cuda-ghash/prove_ffi.cu:420). */
+int flock_gb300_prove_fast(flock_gb300_setup* setup, const void* inputs, size_t n_inputs, const uint8_t* domain,
+                           size_t domain_len, uint8_t** out, size_t* out_len);
+
+/* Host wall-clock milliseconds of the last prove on this setup:
+ * [witness, commit, zerocheck, lincheck, open, total]. */
+int flock_gb300_last_phase_ms(const flock_gb300_setup* setup, double out[6]);
+
+/* Releases a bundle returned by flock_gb300_prove_fast (cuda-ghash/prove_ffi.cu:417 flock_cuda_free). */
+void flock_gb300_free(uint8_t* p);
+
+/* Number of visible CUDA devices (cuda-ghash/prove_ffi.cu:410 flock_cuda_device_count). */
+int flock_gb300_device_count(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* flock_gb300_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLOCK_GB300_H */
