@@ -243,8 +243,9 @@ void GpuBackend::zc_round1(const std::vector<F128>& r, std::vector<F128>& ab, st
   EqSplit e = eq_split(outer, F128::one(), 10);
   uint32_t nb = launch_zc_round1(a_, b_, z_, m, e.lo, e.lo_bits, e.hi, part_, st_);
   auto v = reduce(nb, 256);
+  // D = prod (1 + g_i)^-1 over the medium constants' g_i = x^1, x^2, x^4, x^8
   F128 D = F128::one();
-  for (int i = 0; i < 4; ++i) D = D * inv(F128::one() + fixed[3 + i]);
+  for (int e : {1, 2, 4, 8}) D = D * inv(F128::one() + F128(1ull << e, 0));
   ab.assign(64, F128());
   c.assign(64, F128());
   svc.assign(128, F128());

@@ -58,11 +58,14 @@ struct ChunkWriter {
       uint32_t o = off - 64;
       z1 |= zz << o; a1 |= aa << o; b1 |= bb << o;
       if (o > 32) {
-        // spills into the next chunk
+        // Bits past the chunk go to the next one. A field narrower than 32 bits may
+        // leave nothing to spill; the chunk then stays open for the fields after it.
         uint32_t sh = 64 - o;
         uint64_t sz = zz >> sh, sa = aa >> sh, sb = bb >> sh;
-        advance_to(chunk + 1);
-        z0 |= sz; a0 |= sa; b0 |= sb;
+        if (sz | sa | sb) {
+          advance_to(chunk + 1);
+          z0 |= sz; a0 |= sa; b0 |= sb;
+        }
       }
     }
   }
