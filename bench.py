@@ -1,0 +1,391 @@
+"""Benchmark: proved hashes per second of prove_fast on one GB300.
+
+Default workload: prove_fast of a SHA-256 batch of 2^16 compressions (m = 31, 50 commit
+lanes), seeded synthetic inputs (h[8], w[16] uniform u32). One step = one full prove
+(witness generation through proof bytes) of one batch.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload sha256|blake3|keccak]
+    python bench.py --impl reference ...   # the CPU restatement, timed on the host cores
+
+value : inputs already resident in HBM (flock_gb300_prove_fast_device), CUDA events on
+        the library's stream around K proves, k hashes/s over all ranks.
+e2e   : the public host-buffer call (Setup.prove_fast: host->device copy of the inputs
+        and the proof bytes back inside the timed region).
+roofline : the stage with the most device time in the timed region, its algorithmic
+        bytes per launch over its CUDA-event duration, against the measured HBM copy
+        bandwidth.
+Multi-GPU: replicas only (each rank proves its own batch; no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "k hashes/s proved per GB300 vs host CPU prove_fast; p50/p99 served proof latency"
+UNIT = "k hashes/s"
+WORKLOADS = {
+    # name: (kind, batch, description)
+    "blake3": (0, 1 << 12, "prove_fast BLAKE3 batch 2^12 (counter=index, block_len 64, flags 0)"),
+    "sha256": (1, 1 << 16, "prove_fast SHA-256 batch 2^16"),
+    "keccak": (2, 1 << 18, "prove_fast Keccak-f[1600] batch 2^18"),
+}
+# CPU-baseline sample per workload (oracle proves of a smaller batch of the same hash)
+CPU_SAMPLE = {"blake3": 1 << 10, "sha256": 1 << 10, "keccak": 1 << 8}
+DOMAIN = b"flock-gb300-bench"
+SEED = 0x5EED
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def algorithmic_bytes(stage: str, m: int, lanes: int, k_code: int, n: int, kind: int) -> float | None:
+    """Algorithmic bytes of one prove's `stage` (summed over its launches): the data the
+    stage must read and write at least once."""
+    W = 1 << (m - 7)           # F128 words of z, a, b
+    code_words = lanes << k_code
+    rec = (112, 96, 200)[kind]
+    table = {
+        "witness": n * rec + 3 * 16 * W,
+        "l0_fill": 16 * lanes * (1 << (k_code - 1)) + 16 * code_words,
+        "l0_ntt": 2 * 16 * code_words,
+        "l0_merkle": 16 * code_words + 32 * (2 * (1 << k_code) - 1),
+        "zc_round1": 3 * 16 * W,
+        "zc_fold_skip": 2 * 16 * W + 2 * 32 * W,
+        "mo_build_w": 16 * W + 16 * W,
+    }
+    return table.get(stage)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                    rows.append(parts)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows]
+        mx = max(float(r[2]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows),
+                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit()) if rows else None}
+
+
+# ------------------------------------------------------------------ CPU baseline (oracle)
+def cpu_sample_rate(workload: str, rounds: int = 1, threads: int | None = None) -> dict:
+    """Independent oracle proves of the sample batch on all host cores; k hashes/s."""
+    import oracle
+    from flock_gb300 import inputs
+
+    kind = WORKLOADS[workload][0]
+    n = CPU_SAMPLE[workload]
+    threads = threads or min(os.cpu_count() or 1, 32)
+    oracle.registry_digest(kind, n)  # statement set-up outside the timed region
+    batches = [inputs.batch(kind, n, SEED + 1000 + i) for i in range(threads)]
+    best = None
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        for _ in range(rounds):
+            t0 = time.perf_counter()
+            list(ex.map(lambda b: oracle.prove_fast_bytes(kind, b, DOMAIN), batches))
+            dt = time.perf_counter() - t0
+            rate = threads * n / dt / 1e3
+            best = rate if best is None else max(best, rate)
+    return {"value": best, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{threads} concurrent single-threaded oracle prove_fast runs, each of a {workload} batch of {n} "
+                      f"compressions (one per host thread), best of {rounds}"}
+
+
+# ------------------------------------------------------------------ distributed helpers
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allmax(world, v: float) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ arms
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    wl = args.workload
+    W, K = args.warmup, args.steps
+    n = CPU_SAMPLE[wl]
+    import oracle
+    from flock_gb300 import inputs
+
+    kind = WORKLOADS[wl][0]
+    threads = min(os.cpu_count() or 1, 32)
+    oracle.registry_digest(kind, n)
+    batches = [inputs.batch(kind, n, SEED + 1000 + i) for i in range(threads)]
+    times = []
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        for step in range(W + K):
+            t0 = time.perf_counter()
+            list(ex.map(lambda b: oracle.prove_fast_bytes(kind, b, DOMAIN), batches))
+            if step >= W:
+                times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = K * threads * n / total / 1e3
+    sample = (f"each step: {threads} concurrent single-threaded oracle prove_fast runs of a "
+              f"{n}-compression batch (one per host thread) of the {wl} workload")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": K, "warmup": W,
+        "ms_per_step": 1e3 * total / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "gf2_128", "data": "synthetic (seeded SplitMix64 inputs)",
+        "config": {"workload": WORKLOADS[wl][2] + " (CPU sample, see cpu_baseline.sample)", "hash": wl,
+                   "batch": n, "threads": threads},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    import flock_gb300
+    from flock_gb300 import inputs
+
+    wl = args.workload
+    kind, n, desc = WORKLOADS[wl]
+    if args.batch:
+        n = args.batch
+    torch.cuda.set_device(local)
+    setup = flock_gb300.SETUPS[kind](n)
+    host = inputs.batch(kind, n, SEED + rank)
+    dev = torch.from_numpy(np.frombuffer(host.tobytes(), dtype=np.uint8).copy()).to(f"cuda:{local}")
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(setup.stream_handle(), device=f"cuda:{local}")
+    lib = flock_gb300.load()
+
+    def prove_dev():
+        return setup.prove_fast_device_bytes(dev.data_ptr(), n, DOMAIN)
+
+    # warm-up (also a parity check of the two entry points)
+    for _ in range(args.warmup):
+        a = prove_dev()
+    b = setup.prove_fast_bytes(host, DOMAIN)
+    if a != b:
+        raise SystemExit("device-input and host-input proves differ")
+    bundle_len = len(b)
+
+    # ---- value: inputs resident in HBM
+    setup.set_stage_timing(True)
+    stage_tot = {}
+    step_ms = []
+    barrier(world)
+    torch.cuda.synchronize()
+    launches0 = lib.flock_gb300_launch_count()
+    with ClockSampler(local) as clk:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            s0 = torch.cuda.Event(enable_timing=True)
+            s1 = torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            prove_dev()
+            s1.record(stream)
+            for k, (ms, ln) in setup.last_stage_ms().items():
+                t = stage_tot.setdefault(k, [0.0, 0])
+                t[0] += ms
+                t[1] += ln
+            step_ms.append((s0, s1))
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = lib.flock_gb300_launch_count() - launches0
+    phases = setup.last_phase_ms()
+    barrier(world)
+    ms = allmax(world, ev0.elapsed_time(ev1))
+    per_step = [a.elapsed_time(b) for a, b in step_ms]
+    setup.set_stage_timing(False)
+    value = world * n * args.steps / (ms / 1e3) / 1e3
+
+    # ---- e2e: host buffers through the public call
+    barrier(world)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        setup.prove_fast_bytes(host, DOMAIN)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    h2d, d2h = setup.last_transfer_bytes()
+    barrier(world)
+    e2e_ms = allmax(world, e0.elapsed_time(e1))
+    e2e = world * n * args.steps / (e2e_ms / 1e3) / 1e3
+
+    # ---- roofline of the stage with the most device time
+    peak, peak_src = peaks()
+    m, lanes = setup.m, setup.lanes
+    ranked = sorted(stage_tot.items(), key=lambda kv: -kv[1][0])
+    roof = None
+    for stage, (tot_ms, tot_launch) in ranked:
+        alg = algorithmic_bytes(stage, m, lanes, setup.log_code_len, n, kind)
+        if alg is None or tot_launch == 0:
+            continue
+        per_prove_ms = tot_ms / args.steps
+        achieved = alg / (per_prove_ms / 1e3) / 1e9
+        traffic = None
+        tf = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tf):
+            try:
+                traffic = json.load(open(tf)).get(wl, {}).get(stage)
+            except Exception:
+                traffic = None
+        roof = {"bound": "hbm", "kernel": stage, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": alg,
+                "launches_per_prove": tot_launch / args.steps, "device_ms_per_prove": per_prove_ms,
+                "peak_source": f"{peak_src} hbm_gbs", "share_of_step": per_prove_ms / (ms / args.steps)}
+        break
+    if rank != 0:
+        return 0
+
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_sample_rate(wl, rounds=1)
+    per_step.sort()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "gf2_128", "data": "synthetic (seeded SplitMix64 inputs)",
+        "config": {"workload": desc, "hash": wl, "batch": n, "m": m, "lanes": lanes,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "no flush: every step streams z, a, b and the codeword, each larger than L2",
+                   "seed": SEED},
+        "latency_ms": {"p50": per_step[len(per_step) // 2], "p99": per_step[min(len(per_step) - 1,
+                                                                             int(0.99 * len(per_step)))]},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "bundle_bytes": bundle_len},
+        "roofline": roof,
+        "stages_ms_per_prove": {k: round(v[0] / args.steps, 4) for k, v in ranked},
+        "host_phase_ms": {k: round(v, 3) for k, v in phases.items()},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    setup.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="sha256")
+    ap.add_argument("--batch", type=int, default=0, help="override the batch size (parity-test sizes)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        rc = run_reference(args, world, rank)
+    else:
+        import __graft_entry__
+
+        if rank == 0:
+            __graft_entry__.build()
+        barrier(world)
+        if rank != 0:
+            __graft_entry__.build()
+        rc = run_gpu(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

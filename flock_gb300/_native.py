@@ -20,6 +20,13 @@ EXPORTS = (
     "flock_gb300_setup_free",
     "flock_gb300_setup_info",
     "flock_gb300_prove_fast",
+    "flock_gb300_prove_fast_device",
+    "flock_gb300_setup_stream",
+    "flock_gb300_set_stage_timing",
+    "flock_gb300_last_stage_ms",
+    "flock_gb300_stage_name",
+    "flock_gb300_last_transfer_bytes",
+    "flock_gb300_launch_count",
     "flock_gb300_last_phase_ms",
     "flock_gb300_free",
     "flock_gb300_device_count",
@@ -67,13 +74,28 @@ def load() -> ctypes.CDLL:
         lib.flock_gb300_setup_new.restype = c.c_int
         lib.flock_gb300_setup_free.argtypes = [c.c_void_p]
         lib.flock_gb300_setup_free.restype = None
-        lib.flock_gb300_setup_info.argtypes = [c.c_void_p, c.POINTER(c.c_uint32), c.POINTER(c.c_uint32), c.c_char_p]
+        lib.flock_gb300_setup_info.argtypes = [c.c_void_p, c.POINTER(c.c_uint32), c.POINTER(c.c_uint32),
+                                               c.POINTER(c.c_uint32), c.c_char_p]
         lib.flock_gb300_setup_info.restype = c.c_int
         lib.flock_gb300_prove_fast.argtypes = [
             c.c_void_p, c.c_void_p, c.c_size_t, c.c_char_p, c.c_size_t,
             c.POINTER(c.POINTER(c.c_uint8)), c.POINTER(c.c_size_t),
         ]
         lib.flock_gb300_prove_fast.restype = c.c_int
+        lib.flock_gb300_prove_fast_device.argtypes = lib.flock_gb300_prove_fast.argtypes
+        lib.flock_gb300_prove_fast_device.restype = c.c_int
+        lib.flock_gb300_setup_stream.argtypes = [c.c_void_p, c.POINTER(c.c_void_p)]
+        lib.flock_gb300_setup_stream.restype = c.c_int
+        lib.flock_gb300_set_stage_timing.argtypes = [c.c_void_p, c.c_int]
+        lib.flock_gb300_set_stage_timing.restype = c.c_int
+        lib.flock_gb300_last_stage_ms.argtypes = [c.c_void_p, c.POINTER(c.c_double), c.POINTER(c.c_uint32), c.c_int]
+        lib.flock_gb300_last_stage_ms.restype = c.c_int
+        lib.flock_gb300_stage_name.argtypes = [c.c_int]
+        lib.flock_gb300_stage_name.restype = c.c_char_p
+        lib.flock_gb300_last_transfer_bytes.argtypes = [c.c_void_p, c.POINTER(c.c_uint64), c.POINTER(c.c_uint64)]
+        lib.flock_gb300_last_transfer_bytes.restype = c.c_int
+        lib.flock_gb300_launch_count.argtypes = []
+        lib.flock_gb300_launch_count.restype = c.c_uint64
         lib.flock_gb300_last_phase_ms.argtypes = [c.c_void_p, c.POINTER(c.c_double)]
         lib.flock_gb300_last_phase_ms.restype = c.c_int
         lib.flock_gb300_free.argtypes = [c.POINTER(c.c_uint8)]

@@ -134,6 +134,7 @@ GpuBackend::~GpuBackend() {
   for (void* p : owned_) cudaFree(p);
   for (auto& kv : tw_) cudaFree(kv.second);
   for (auto& L : levels_) { cudaFree(L.mat); cudaFree(L.tree); }
+  for (cudaEvent_t e : ev_pool_) cudaEventDestroy(e);
   cudaFreeHost(h_in_);
   cudaFreeHost(h_red_);
   cudaFreeHost(h_stage_);
@@ -151,6 +152,55 @@ const F128d* GpuBackend::twiddles(uint32_t log_d) {
   return d;
 }
 
+// ---- stage timing
+const char* GpuBackend::stage_name(int s) {
+  static const char* names[ST_COUNT] = {"witness", "l0_fill", "l0_ntt", "l0_merkle", "zc_round1", "zc_fold_skip",
+                                        "zc_folds", "lincheck", "mo_build_w", "mo_rounds", "ligerito", "lg_ntt",
+                                        "lg_merkle"};
+  return (s >= 0 && s < ST_COUNT) ? names[s] : "?";
+}
+cudaEvent_t GpuBackend::event() {
+  if (ev_used_ == ev_pool_.size()) {
+    cudaEvent_t e;
+    CUDA_OK(cudaEventCreate(&e));
+    ev_pool_.push_back(e);
+  }
+  return ev_pool_[ev_used_++];
+}
+GpuBackend::Mark::Mark(GpuBackend* be, int stage) : b(be), st(stage), l0(launch_count()) {
+  if (b->timing_) {
+    cudaEvent_t a = b->event();
+    CUDA_OK(cudaEventRecord(a, b->st_));
+    b->spans_.push_back({st, a, nullptr, 0});
+  }
+}
+GpuBackend::Mark::~Mark() {
+  if (b->timing_ && !b->spans_.empty()) {
+    cudaEvent_t e = b->event();
+    if (cudaEventRecord(e, b->st_) == cudaSuccess) {
+      b->spans_.back().b = e;
+      b->spans_.back().launches = launch_count() - l0;
+    }
+  }
+}
+void GpuBackend::begin_prove(const void* d_inputs) {
+  d_user_inputs_ = d_inputs;
+  h2d_ = d2h_ = 0;
+  spans_.clear();
+  ev_used_ = 0;
+}
+void GpuBackend::stage_ms(double out[ST_COUNT], uint32_t launches[ST_COUNT]) {
+  for (int i = 0; i < ST_COUNT; ++i) { out[i] = 0; launches[i] = 0; }
+  CUDA_OK(cudaStreamSynchronize(st_));
+  for (auto& sp : spans_) {
+    if (!sp.b) continue;
+    float ms = 0;
+    CUDA_OK(cudaEventElapsedTime(&ms, sp.a, sp.b));
+    out[sp.st] += ms;
+    launches[sp.st] += (uint32_t)sp.launches;
+  }
+}
+
 // ---- staging helpers
 void* GpuBackend::scratch(size_t bytes) {
   size_t off = (scr_off_ + 255) & ~size_t(255);
@@ -166,6 +216,7 @@ const void* GpuBackend::upload(const void* src, size_t bytes) {
   }
   memcpy(h_stage_ + off, src, bytes);
   CUDA_OK(cudaMemcpyAsync(d_stage_ + off, h_stage_ + off, bytes, cudaMemcpyHostToDevice, st_));
+  h2d_ += bytes;
   stage_off_ = off + bytes;
   return d_stage_ + off;
 }
@@ -187,6 +238,7 @@ std::vector<F128> GpuBackend::fetch(const F128d* d, size_t n) {
   bool big = n > 4096;
   if (big) h = reinterpret_cast<F128d*>(out.data());
   CUDA_OK(cudaMemcpyAsync(h, d, n * sizeof(F128d), cudaMemcpyDeviceToHost, st_));
+  d2h_ += n * sizeof(F128d);
   sync();
   if (!big) memcpy(out.data(), h, n * sizeof(F128d));
   return out;
@@ -211,15 +263,21 @@ GpuBackend::EqSplit GpuBackend::eq_split(const std::vector<F128>& point, F128 sc
 // ------------------------------------------------------------------ witness + commit
 void GpuBackend::witness(const uint8_t* inputs) {
   scr_off_ = 0;
-  memcpy(h_in_, inputs, in_bytes_);
-  CUDA_OK(cudaMemcpyAsync(d_in_, h_in_, in_bytes_, cudaMemcpyHostToDevice, st_));
-  launch_witness((int)S.hash, d_in_, S.n_blocks, S.nu, z_, a_, b_, (uint32_t)S.geo.used_cols, st_);
+  const void* src = d_user_inputs_;
+  if (!src) {
+    memcpy(h_in_, inputs, in_bytes_);
+    CUDA_OK(cudaMemcpyAsync(d_in_, h_in_, in_bytes_, cudaMemcpyHostToDevice, st_));
+    h2d_ += in_bytes_;
+    src = d_in_;
+  }
+  Mark mk(this, ST_WITNESS);
+  launch_witness((int)S.hash, src, S.n_blocks, S.nu, z_, a_, b_, (uint32_t)S.geo.used_cols, st_);
 }
 
 void GpuBackend::commit_l0(uint32_t cap_depth, std::vector<Hash>& cap) {
-  launch_fill_lane_major(z_, cw0_, S.lanes, S.log_dim, S.k_code, st_);
-  launch_ntt(cw0_, S.lanes, S.k_code, 1, tw0_, st_);
-  launch_merkle(cw0_, S.lanes, n_pos0_, tree0_, st_);
+  { Mark mk(this, ST_L0_FILL); launch_fill_lane_major(z_, cw0_, S.lanes, S.log_dim, S.k_code, st_); }
+  { Mark mk(this, ST_L0_NTT); launch_ntt(cw0_, S.lanes, S.k_code, 1, tw0_, st_); }
+  { Mark mk(this, ST_L0_MERKLE); launch_merkle(cw0_, S.lanes, n_pos0_, tree0_, st_); }
   cap = read_cap(tree0_, n_pos0_, cap_depth);
 }
 
@@ -227,6 +285,7 @@ std::vector<Hash> GpuBackend::read_cap(const uint8_t* tree, uint64_t n_leaves, u
   uint64_t l = uint64_t(1) << cap_depth;
   std::vector<Hash> cap(l);
   CUDA_OK(cudaMemcpyAsync(cap.data(), tree + (2 * n_leaves - 2 * l) * 32, l * 32, cudaMemcpyDeviceToHost, st_));
+  d2h_ += l * 32;
   sync();
   return cap;
 }
@@ -241,7 +300,11 @@ void GpuBackend::zc_round1(const std::vector<F128>& r, std::vector<F128>& ab, st
     if (r[6 + i] != fixed[i]) throw std::runtime_error("zerocheck round 1 expects the fixed challenges at r[6..13)");
   std::vector<F128> outer(r.begin() + 13, r.end());
   EqSplit e = eq_split(outer, F128::one(), 10);
-  uint32_t nb = launch_zc_round1(a_, b_, z_, m, e.lo, e.lo_bits, e.hi, part_, st_);
+  uint32_t nb;
+  {
+    Mark mk(this, ST_ZC_ROUND1);
+    nb = launch_zc_round1(a_, b_, z_, m, e.lo, e.lo_bits, e.hi, part_, st_);
+  }
   auto v = reduce(nb, 256);
   // D = prod (1 + g_i)^-1 over the medium constants' g_i = x^1, x^2, x^4, x^8
   F128 D = F128::one();
@@ -258,7 +321,11 @@ void GpuBackend::zc_fold_skip(const std::vector<F128>& w, const std::vector<F128
   const F128d* dw = upload(w);
   EqSplit e = eq_split(eq_point, F128::one(), 10);
   if (e.lo_bits != 10) throw std::runtime_error("zerocheck skip fold needs m >= 17");
-  uint32_t nb = launch_zc_fold_skip(a_, b_, dw, W_, e.lo, e.lo_bits, e.hi, zc1a_, zc1b_, part_, st_);
+  uint32_t nb;
+  {
+    Mark mk(this, ST_ZC_FOLD_SKIP);
+    nb = launch_zc_fold_skip(a_, b_, dw, W_, e.lo, e.lo_bits, e.hi, zc1a_, zc1b_, part_, st_);
+  }
   auto v = reduce(nb, 2);
   g1 = v[0];
   gi = v[1];
@@ -274,7 +341,11 @@ void GpuBackend::zc_fold(F128 rho, const std::vector<F128>& eq_point, F128& g1, 
   EqSplit e = eq_split(eq_point, F128::one(), 10);
   F128d* oa = (zc_cur_a_ == zc1a_) ? zc2a_ : zc1a_;
   F128d* ob = (zc_cur_a_ == zc1a_) ? zc2b_ : zc1b_;
-  uint32_t nb = launch_pair_fold(zc_cur_a_, zc_cur_b_, n_pairs, dev(rho), e.lo, e.lo_bits, e.hi, oa, ob, part_, true, st_);
+  uint32_t nb;
+  {
+    Mark mk(this, ST_ZC_FOLDS);
+    nb = launch_pair_fold(zc_cur_a_, zc_cur_b_, n_pairs, dev(rho), e.lo, e.lo_bits, e.hi, oa, ob, part_, true, st_);
+  }
   auto v = reduce(nb, 2);
   g1 = v[0];
   gi = v[1];
@@ -296,6 +367,7 @@ void GpuBackend::lc_comb(const std::vector<F128>& skip_w, const std::vector<F128
   scr_off_ = 0;
   const F128d* dw = upload(skip_w);
   const F128d* der = upload(build_eq(xir));
+  Mark mk(this, ST_LINCHECK);
   launch_lc_eq_inner(dw, der, K_, eqi_, st_);
   if (S.hash == HASH_KECCAK) {
     // walker fold (additions only) on the host over the downloaded eq vector
@@ -304,6 +376,7 @@ void GpuBackend::lc_comb(const std::vector<F128>& skip_w, const std::vector<F128
     kr1cs::fold_split(eqi.data(), ha, hb);
     CUDA_OK(cudaMemcpyAsync(ca_, ha.data(), K_ * 16, cudaMemcpyHostToDevice, st_));
     CUDA_OK(cudaMemcpyAsync(cb_, hb.data(), K_ * 16, cudaMemcpyHostToDevice, st_));
+    h2d_ += 2 * K_ * 16;
     sync();
     return;
   }
@@ -316,6 +389,7 @@ void GpuBackend::lc_zvec(const std::vector<F128>& x_outer) {
   const uint32_t nu = S.nu;
   const F128d* dp = upload(x_outer);
   F128d* eq = static_cast<F128d*>(scratch(size_t(16) << nu));
+  Mark mk(this, ST_LINCHECK);
   launch_eq_table(dp, nu, dev(F128::one()), eq, st_);
   uint32_t used = (uint32_t)S.geo.used_cols;
   if ((uint64_t)used * 128 < K_) CUDA_OK(cudaMemsetAsync(zv_ + used * 128, 0, (K_ - used * 128) * 16, st_));
@@ -325,14 +399,16 @@ void GpuBackend::lc_zvec(const std::vector<F128>& x_outer) {
 }
 
 void GpuBackend::lc_start(F128 alpha, F128 beta, uint32_t pin, F128& e1, F128& ei) {
-  uint32_t nb = launch_lc_start(ca_, cb_, dev(alpha), dev(beta), pin, K_, comb_, zv_, part_, st_);
+  uint32_t nb;
+  { Mark mk(this, ST_LINCHECK); nb = launch_lc_start(ca_, cb_, dev(alpha), dev(beta), pin, K_, comb_, zv_, part_, st_); }
   auto v = reduce(nb, 2);
   e1 = v[0];
   ei = v[1];
 }
 
 void GpuBackend::lc_round(F128 r, bool last, F128& e1, F128& ei) {
-  uint32_t nb = launch_lc_round(comb_, zv_, lc_len_, dev(r), !last, part_, st_);
+  uint32_t nb;
+  { Mark mk(this, ST_LINCHECK); nb = launch_lc_round(comb_, zv_, lc_len_, dev(r), !last, part_, st_); }
   lc_len_ /= 2;
   if (!last) {
     auto v = reduce(nb, 2);
@@ -350,7 +426,8 @@ void GpuBackend::lc_matrix_evals(const std::vector<F128>& rest, const std::vecto
   scr_off_ = 0;
   const F128d* der = upload(build_eq(rest));
   const F128d* dzp = upload(zp);
-  uint32_t nb = launch_lc_matrix_evals(ca_, cb_, der, dzp, K_, part_, st_);
+  uint32_t nb;
+  { Mark mk(this, ST_LINCHECK); nb = launch_lc_matrix_evals(ca_, cb_, der, dzp, K_, part_, st_); }
   auto v = reduce(nb, 2);
   ea = v[0];
   eb = v[1];
@@ -359,7 +436,7 @@ void GpuBackend::lc_matrix_evals(const std::vector<F128>& rest, const std::vecto
 void GpuBackend::lc_s_hat_v(const std::vector<F128>& tail, std::vector<F128>& out) {
   auto et = build_eq(tail);
   const F128d* det = upload(et);
-  launch_lc_s_hat_v(zvcap_, det, (uint32_t)et.size(), red_, st_);
+  { Mark mk(this, ST_LINCHECK); launch_lc_s_hat_v(zvcap_, det, (uint32_t)et.size(), red_, st_); }
   out = fetch(red_, 128);
 }
 
@@ -367,6 +444,7 @@ void GpuBackend::lc_s_hat_v(const std::vector<F128>& tail, std::vector<F128>& ou
 void GpuBackend::mo_build_w(const std::vector<WeightClaim>& cl, uint32_t nu, uint64_t area, F128& u0, F128& u2) {
   scr_off_ = 0;
   if (cl.size() != 2) throw std::runtime_error("merged open expects the AB and C claims");
+  Mark mk(this, ST_MO_BUILD_W);
   F128d* er[2];
   F128d* ec[2];
   for (int i = 0; i < 2; ++i) {
@@ -400,7 +478,11 @@ void GpuBackend::mo_round(F128 r, bool last, F128& g1, F128& gi) {
   F128d* ow = (mo_q_ == moAq_) ? moBw_ : moAw_;
   uint64_t n_pairs = mo_len_ / 4;
   uint32_t chunk_bits = std::min<uint32_t>(10, ceil_log2(n_pairs));  // chunking only sets the work split
-  uint32_t nb = launch_pair_fold(mo_q_, mo_w_, n_pairs, dev(r), nullptr, chunk_bits, nullptr, oq, ow, part_, !last, st_);
+  uint32_t nb;
+  {
+    Mark mk(this, ST_MO_ROUNDS);
+    nb = launch_pair_fold(mo_q_, mo_w_, n_pairs, dev(r), nullptr, chunk_bits, nullptr, oq, ow, part_, !last, st_);
+  }
   mo_q_ = oq;
   mo_w_ = ow;
   mo_len_ /= 2;
@@ -421,7 +503,7 @@ void GpuBackend::lg_basis_eq(F128 gamma, const std::vector<F128>& rho) {
   scr_off_ = 0;
   if ((uint64_t(1) << rho.size()) != W_) throw std::runtime_error("Ligerito basis size mismatch");
   EqSplit e = eq_split(rho, gamma, 10);
-  launch_lg_eq_fill(e.lo, e.lo_bits, e.hi, W_, lb128_, false, st_);
+  { Mark mk(this, ST_LIGERITO); launch_lg_eq_fill(e.lo, e.lo_bits, e.hi, W_, lb128_, false, st_); }
   lg_base_ = true;
   lg_n_ = W_;
   lg_cur_ = 0;
@@ -431,7 +513,8 @@ F128 GpuBackend::lg_eval_eq(const std::vector<F128>& zp) {
   scr_off_ = 0;
   if (!lg_base_) throw std::runtime_error("OOD evaluation expects the committed base vector");
   EqSplit e = eq_split(zp, F128::one(), 10);
-  uint32_t nb = launch_lg_dot_eq(z_, 1, e.lo, e.lo_bits, e.hi, W_, part_, st_);
+  uint32_t nb;
+  { Mark mk(this, ST_LIGERITO); nb = launch_lg_dot_eq(z_, 1, e.lo, e.lo_bits, e.hi, W_, part_, st_); }
   return reduce(nb, 1)[0];
 }
 
@@ -439,7 +522,7 @@ void GpuBackend::lg_add_eq(F128 beta, const std::vector<F128>& zp) {
   scr_off_ = 0;
   if (!lg_base_) throw std::runtime_error("basis update expects the base stage");
   EqSplit e = eq_split(zp, beta, 10);
-  launch_lg_eq_fill(e.lo, e.lo_bits, e.hi, W_, lb128_, true, st_);
+  { Mark mk(this, ST_LIGERITO); launch_lg_eq_fill(e.lo, e.lo_bits, e.hi, W_, lb128_, true, st_); }
 }
 
 Msg256 GpuBackend::lg_message(size_t d) {
@@ -447,12 +530,14 @@ Msg256 GpuBackend::lg_message(size_t d) {
   if (d == 1 || n == d) d = 1;
   Msg256 m;
   if (lg_base_) {
-    uint32_t nb = launch_lg_message128(z_, lb128_, n, d, part_, st_);
+    uint32_t nb;
+    { Mark mk(this, ST_LIGERITO); nb = launch_lg_message128(z_, lb128_, n, d, part_, st_); }
     auto v = reduce(nb, 2);
     m.u0 = F256(v[0]);
     m.u2 = F256(v[1]);
   } else {
-    uint32_t nb = launch_lg_message256(lf_[lg_cur_], lb_[lg_cur_], n, d, part_, st_);
+    uint32_t nb;
+    { Mark mk(this, ST_LIGERITO); nb = launch_lg_message256(lf_[lg_cur_], lb_[lg_cur_], n, d, part_, st_); }
     auto v = reduce(nb, 4);
     m.u0 = F256(v[0], v[1]);
     m.u2 = F256(v[2], v[3]);
@@ -462,6 +547,7 @@ Msg256 GpuBackend::lg_message(size_t d) {
 
 void GpuBackend::lg_fold(F256 r, size_t d) {
   uint64_t n_out = lg_n_ / 2;
+  Mark mk(this, ST_LIGERITO);
   if (lg_base_) {
     launch_lg_fold128(z_, lb128_, n_out, dev(r), d, lf_[0], lb_[0], st_);
     lg_cur_ = 0;
@@ -478,6 +564,7 @@ void GpuBackend::lg_code_switch() {
   if (lg_base_) throw std::runtime_error("code switch before the first fold");
   if (2 * lg_n_ > W_ / 2) throw std::runtime_error("code switch exceeds the Ligerito buffers");
   int nx = lg_cur_ ^ 1;
+  Mark mk(this, ST_LIGERITO);
   launch_lg_code_switch(lf_[lg_cur_], lb_[lg_cur_], lg_n_, lf_[nx], lb_[nx], st_);
   lg_cur_ = nx;
   lg_n_ *= 2;
@@ -497,9 +584,10 @@ void GpuBackend::lg_commit(uint32_t level, uint32_t log_cols, uint32_t log_lanes
     L.block_len = block_len;
     L.lanes = lanes;
   }
-  launch_lg_replicate(lf_[lg_cur_], lg_n_, block_len * lanes, L.mat, st_);
-  launch_ntt(L.mat, lanes, log_cols + log_rate, log_rate, twiddles(log_cols + log_rate), st_);
-  launch_merkle(L.mat, lanes, block_len, L.tree, st_);
+  const F128d* tw = twiddles(log_cols + log_rate);
+  { Mark mk(this, ST_LIGERITO); launch_lg_replicate(lf_[lg_cur_], lg_n_, block_len * lanes, L.mat, st_); }
+  { Mark mk(this, ST_LG_NTT); launch_ntt(L.mat, lanes, log_cols + log_rate, log_rate, tw, st_); }
+  { Mark mk(this, ST_LG_MERKLE); launch_merkle(L.mat, lanes, block_len, L.tree, st_); }
   cap = read_cap(L.tree, block_len, cap_depth);
 }
 
@@ -507,7 +595,8 @@ Msg256 GpuBackend::lg_introduce_eq(const std::vector<F128>& zp, F128& answer) {
   scr_off_ = 0;
   if ((uint64_t(1) << zp.size()) != lg_n_) throw std::runtime_error("OOD point size mismatch");
   EqSplit e = eq_split(zp, F128::one(), 10);
-  uint32_t nb = launch_lg_intro_eq(lf_[lg_cur_], e.lo, e.lo_bits, e.hi, lg_n_, pend_, part_, st_);
+  uint32_t nb;
+  { Mark mk(this, ST_LIGERITO); nb = launch_lg_intro_eq(lf_[lg_cur_], e.lo, e.lo_bits, e.hi, lg_n_, pend_, part_, st_); }
   auto v = reduce(nb, 3);
   answer = v[0];
   pend_induced_ = false;
@@ -531,7 +620,8 @@ Msg256 GpuBackend::lg_introduce_induced(uint32_t ln, const std::vector<F128>& w,
   uint32_t lo_bits = ln / 2;
   F128d* lo_tab = static_cast<F128d*>(scratch((size_t)nq * (size_t(16) << lo_bits)));
   F128d* hi_tab = static_cast<F128d*>(scratch((size_t)nq * (size_t(16) << (ln - lo_bits))));
-  uint32_t nb = launch_lg_induced(dwhat, dw, nq, ln, lf_[lg_cur_], lo_tab, hi_tab, pend_, part_, st_);
+  uint32_t nb;
+  { Mark mk(this, ST_LIGERITO); nb = launch_lg_induced(dwhat, dw, nq, ln, lf_[lg_cur_], lo_tab, hi_tab, pend_, part_, st_); }
   auto v = reduce(nb, 2);
   pend_induced_ = true;
   pend_n_ = uint64_t(1) << ln;
@@ -541,7 +631,10 @@ Msg256 GpuBackend::lg_introduce_induced(uint32_t ln, const std::vector<F128>& w,
   return m;
 }
 
-void GpuBackend::lg_glue(F128 beta) { launch_lg_glue(lb_[lg_cur_], pend_, dev(beta), pend_n_, pend_induced_, st_); }
+void GpuBackend::lg_glue(F128 beta) {
+  Mark mk(this, ST_LIGERITO);
+  launch_lg_glue(lb_[lg_cur_], pend_, dev(beta), pend_n_, pend_induced_, st_);
+}
 
 void GpuBackend::lg_open(uint32_t level, const std::vector<uint64_t>& pos, uint32_t cap_depth,
                          std::vector<std::vector<F128>>& rows, std::vector<Hash>& paths) {
@@ -561,12 +654,16 @@ void GpuBackend::lg_open(uint32_t level, const std::vector<uint64_t>& pos, uint3
   const uint64_t* dpos = static_cast<const uint64_t*>(upload(pos.data(), n * 8));
   F128d* drows = static_cast<F128d*>(scratch((size_t)n * lanes * 16));
   uint8_t* dpaths = static_cast<uint8_t*>(scratch((size_t)n * plen * 32 + 32));
-  launch_gather_rows(mat, lanes, dpos, n, drows, st_);
-  launch_gather_paths(tree, n_leaves, dpos, n, cap_depth, dpaths, st_);
+  {
+    Mark mk(this, ST_LIGERITO);
+    launch_gather_rows(mat, lanes, dpos, n, drows, st_);
+    launch_gather_paths(tree, n_leaves, dpos, n, cap_depth, dpaths, st_);
+  }
   std::vector<F128> hr((size_t)n * lanes);
   std::vector<Hash> hp((size_t)n * plen);
   CUDA_OK(cudaMemcpyAsync(hr.data(), drows, hr.size() * 16, cudaMemcpyDeviceToHost, st_));
   if (plen) CUDA_OK(cudaMemcpyAsync(hp.data(), dpaths, hp.size() * 32, cudaMemcpyDeviceToHost, st_));
+  d2h_ += hr.size() * 16 + (plen ? hp.size() * 32 : 0);
   sync();
   for (uint32_t q = 0; q < n; ++q) rows.emplace_back(hr.begin() + (size_t)q * lanes, hr.begin() + (size_t)(q + 1) * lanes);
   paths.insert(paths.end(), hp.begin(), hp.end());
@@ -575,6 +672,7 @@ void GpuBackend::lg_open(uint32_t level, const std::vector<uint64_t>& pos, uint3
 std::vector<F256> GpuBackend::lg_residual() {
   std::vector<F256> out(lg_n_);
   CUDA_OK(cudaMemcpyAsync(out.data(), lf_[lg_cur_], lg_n_ * sizeof(F256d), cudaMemcpyDeviceToHost, st_));
+  d2h_ += lg_n_ * sizeof(F256d);
   sync();
   return out;
 }

@@ -49,6 +49,20 @@ class GpuBackend : public ProverBackend {
                std::vector<std::vector<F128>>& rows, std::vector<Hash>& paths) override;
   std::vector<F256> lg_residual() override;
 
+  // Device-time breakdown of a prove (CUDA events on the backend's stream).
+  enum Stage {
+    ST_WITNESS, ST_L0_FILL, ST_L0_NTT, ST_L0_MERKLE, ST_ZC_ROUND1, ST_ZC_FOLD_SKIP, ST_ZC_FOLDS, ST_LINCHECK,
+    ST_MO_BUILD_W, ST_MO_ROUNDS, ST_LIGERITO, ST_LG_NTT, ST_LG_MERKLE, ST_COUNT
+  };
+  static const char* stage_name(int s);
+  void set_stage_timing(bool on) { timing_ = on; }
+  // Called before each prove: clears transfer counters and stage events.
+  void begin_prove(const void* d_inputs);
+  // Milliseconds per stage of the last prove and the launches counted in each.
+  void stage_ms(double out[ST_COUNT], uint32_t launches[ST_COUNT]);
+  uint64_t h2d_bytes() const { return h2d_; }
+  uint64_t d2h_bytes() const { return d2h_; }
+
   cudaStream_t stream() const { return st_; }
   int device() const { return device_; }
   // Device views for tests of single stages.
@@ -80,8 +94,25 @@ class GpuBackend : public ProverBackend {
   const F128d* twiddles(uint32_t log_d);
   std::vector<Hash> read_cap(const uint8_t* tree, uint64_t n_leaves, uint32_t cap_depth);
 
+  struct Mark {
+    GpuBackend* b;
+    int st;
+    uint64_t l0;
+    Mark(GpuBackend* be, int stage);
+    ~Mark();
+  };
+  friend struct Mark;
+  cudaEvent_t event();
+
   const Statement& S;
   int device_ = 0;
+  bool timing_ = false;
+  std::vector<cudaEvent_t> ev_pool_;
+  size_t ev_used_ = 0;
+  struct Span { int st; cudaEvent_t a, b; uint64_t launches; };
+  std::vector<Span> spans_;
+  uint64_t h2d_ = 0, d2h_ = 0;
+  const void* d_user_inputs_ = nullptr;
   cudaStream_t st_ = nullptr;
   uint64_t W_ = 0;
   uint32_t K_ = 0;

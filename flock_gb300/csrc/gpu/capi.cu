@@ -80,18 +80,20 @@ int flock_gb300_setup_new(int hash_kind, uint64_t n_blocks, flock_gb300_setup** 
 
 void flock_gb300_setup_free(flock_gb300_setup* setup) { delete setup; }
 
-int flock_gb300_setup_info(const flock_gb300_setup* setup, uint32_t* m, uint32_t* lanes, uint8_t digest[32]) {
+int flock_gb300_setup_info(const flock_gb300_setup* setup, uint32_t* m, uint32_t* lanes, uint32_t* log_code_len,
+                           uint8_t digest[32]) {
   if (!setup) return fail(FLOCK_GB300_EINVAL, "null setup");
   if (m) *m = setup->stmt->m;
   if (lanes) *lanes = setup->stmt->lanes;
+  if (log_code_len) *log_code_len = setup->stmt->k_code;
   if (digest) memcpy(digest, setup->stmt->registry_digest.data(), 32);
   return FLOCK_GB300_OK;
 }
 
-int flock_gb300_prove_fast(flock_gb300_setup* setup, const void* inputs, size_t n_inputs, const uint8_t* domain,
-                           size_t domain_len, uint8_t** out, size_t* out_len) {
+static int prove_common(flock_gb300_setup* setup, const void* inputs, const void* d_inputs, size_t n_inputs,
+                        const uint8_t* domain, size_t domain_len, uint8_t** out, size_t* out_len) {
   g_last_error.clear();
-  if (!setup || !inputs || !out || !out_len || (!domain && domain_len))
+  if (!setup || !(inputs || d_inputs) || !out || !out_len || (!domain && domain_len))
     return fail(FLOCK_GB300_EINVAL, "null argument");
   *out = nullptr;
   *out_len = 0;
@@ -101,6 +103,7 @@ int flock_gb300_prove_fast(flock_gb300_setup* setup, const void* inputs, size_t 
   return guarded([&] {
     std::lock_guard<std::mutex> g(setup->mu);
     CUDA_OK(cudaSetDevice(setup->backend->device()));
+    setup->backend->begin_prove(d_inputs);
     ProveResult R = prove_fast(*setup->stmt, *setup->backend, static_cast<const uint8_t*>(inputs), domain, domain_len);
     setup->last = R.t;
     std::vector<uint8_t> pb = proof_bytes(R.proof);
@@ -120,6 +123,56 @@ int flock_gb300_prove_fast(flock_gb300_setup* setup, const void* inputs, size_t 
     return FLOCK_GB300_OK;
   });
 }
+
+int flock_gb300_prove_fast(flock_gb300_setup* setup, const void* inputs, size_t n_inputs, const uint8_t* domain,
+                           size_t domain_len, uint8_t** out, size_t* out_len) {
+  return prove_common(setup, inputs, nullptr, n_inputs, domain, domain_len, out, out_len);
+}
+
+int flock_gb300_prove_fast_device(flock_gb300_setup* setup, const void* d_inputs, size_t n_inputs,
+                                  const uint8_t* domain, size_t domain_len, uint8_t** out, size_t* out_len) {
+  if (!d_inputs) return fail(FLOCK_GB300_EINVAL, "null device inputs");
+  return prove_common(setup, nullptr, d_inputs, n_inputs, domain, domain_len, out, out_len);
+}
+
+int flock_gb300_setup_stream(const flock_gb300_setup* setup, void** stream) {
+  if (!setup || !stream) return fail(FLOCK_GB300_EINVAL, "null argument");
+  *stream = (void*)setup->backend->stream();
+  return FLOCK_GB300_OK;
+}
+
+int flock_gb300_set_stage_timing(flock_gb300_setup* setup, int enabled) {
+  if (!setup) return fail(FLOCK_GB300_EINVAL, "null setup");
+  std::lock_guard<std::mutex> g(setup->mu);
+  setup->backend->set_stage_timing(enabled != 0);
+  return FLOCK_GB300_OK;
+}
+
+int flock_gb300_last_stage_ms(flock_gb300_setup* setup, double* ms, uint32_t* launches, int cap) {
+  if (!setup) return fail(FLOCK_GB300_EINVAL, "null setup");
+  return guarded([&] {
+    std::lock_guard<std::mutex> g(setup->mu);
+    double t[gpu::GpuBackend::ST_COUNT];
+    uint32_t l[gpu::GpuBackend::ST_COUNT];
+    setup->backend->stage_ms(t, l);
+    for (int i = 0; i < cap && i < gpu::GpuBackend::ST_COUNT; ++i) {
+      if (ms) ms[i] = t[i];
+      if (launches) launches[i] = l[i];
+    }
+    return (int)gpu::GpuBackend::ST_COUNT;
+  });
+}
+
+const char* flock_gb300_stage_name(int stage) { return gpu::GpuBackend::stage_name(stage); }
+
+int flock_gb300_last_transfer_bytes(const flock_gb300_setup* setup, uint64_t* h2d, uint64_t* d2h) {
+  if (!setup) return fail(FLOCK_GB300_EINVAL, "null setup");
+  if (h2d) *h2d = setup->backend->h2d_bytes();
+  if (d2h) *d2h = setup->backend->d2h_bytes();
+  return FLOCK_GB300_OK;
+}
+
+uint64_t flock_gb300_launch_count(void) { return gpu::launch_count(); }
 
 int flock_gb300_last_phase_ms(const flock_gb300_setup* setup, double out[6]) {
   if (!setup || !out) return fail(FLOCK_GB300_EINVAL, "null argument");

@@ -42,7 +42,7 @@ void launch_fill_lane_major(const F128d* q, F128d* cw, uint32_t lanes, uint32_t 
   uint64_t n_pos = 1ull << log_pos;
   dim3 grid((unsigned)((n_pos + 31) / 32), (lanes + 31) / 32), block(32, 8);
   fill_lane_major_kernel<<<grid, block, 0, s>>>(q, cw, lanes, log_dim, n_pos);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
 }
 
 // One butterfly layer: thread per (pair, lane). tw[(1 << layer) - 1 + block].
@@ -131,12 +131,12 @@ void launch_ntt(F128d* data, uint32_t lanes, uint32_t log_d, uint32_t start_laye
       }
       ntt_fused_kernel<NL><<<(unsigned)(n_groups * lane_tiles), 256, smem, s>>>(data, lanes, log_d, layer, tw,
                                                                                  lane_tile);
-      CUDA_OK(cudaGetLastError());
+      LAUNCH_OK();
       layer += NL;
     } else {
       uint64_t work = (1ull << (log_d - 1)) * lanes;
       ntt_layer_kernel<<<(unsigned)((work + 255) / 256), 256, 0, s>>>(data, lanes, log_d, layer, tw);
-      CUDA_OK(cudaGetLastError());
+      LAUNCH_OK();
       layer += 1;
     }
   }
@@ -165,12 +165,12 @@ __global__ void merkle_level_kernel(uint32_t* __restrict__ tree, uint64_t in_off
 }
 void launch_merkle(const F128d* rows, uint32_t lanes, uint64_t n_leaves, uint8_t* tree, cudaStream_t s) {
   merkle_leaves_kernel<<<(unsigned)((n_leaves + 127) / 128), 128, 0, s>>>(rows, lanes, n_leaves, (uint32_t*)tree);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
   uint64_t off = 0, len = n_leaves;
   while (len > 1) {
     uint64_t nout = len / 2;
     merkle_level_kernel<<<(unsigned)((nout + 127) / 128), 128, 0, s>>>((uint32_t*)tree, off, nout);
-    CUDA_OK(cudaGetLastError());
+    LAUNCH_OK();
     off += len;
     len = nout;
   }
@@ -188,7 +188,7 @@ void launch_gather_rows(const F128d* mat, uint32_t lanes, const uint64_t* d_pos,
                         cudaStream_t s) {
   uint32_t work = n * lanes;
   gather_rows_kernel<<<(work + 255) / 256, 256, 0, s>>>(mat, lanes, d_pos, n, out);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
 }
 __global__ void gather_paths_kernel(const uint8_t* __restrict__ tree, uint64_t n_leaves,
                                     const uint64_t* __restrict__ pos, uint32_t n, uint32_t cap_depth,
@@ -211,7 +211,7 @@ __global__ void gather_paths_kernel(const uint8_t* __restrict__ tree, uint64_t n
 void launch_gather_paths(const uint8_t* tree, uint64_t n_leaves, const uint64_t* d_pos, uint32_t n,
                          uint32_t cap_depth, uint8_t* out, cudaStream_t s) {
   gather_paths_kernel<<<(n + 127) / 128, 128, 0, s>>>(tree, n_leaves, d_pos, n, cap_depth, out);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
 }
 
 }  // namespace gpu

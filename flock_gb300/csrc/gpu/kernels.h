@@ -21,6 +21,15 @@
 namespace flock {
 namespace gpu {
 
+// Kernel launches made by this library (all threads); read through flock_gb300_launch_count.
+uint64_t launch_count();
+void note_launch();
+#define LAUNCH_OK()                    \
+  do {                                 \
+    CUDA_OK(cudaGetLastError());       \
+    ::flock::gpu::note_launch();       \
+  } while (0)
+
 int sm_count();
 
 // witness.cu — writes chunk columns [0, used_chunks) of z, a, b

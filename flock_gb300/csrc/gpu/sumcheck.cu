@@ -9,6 +9,7 @@
 // * hi[i >> lo_bits], and kernels that sum eq-weighted terms walk chunks of 2^lo_bits
 // consecutive indices, summing lo-weighted terms and multiplying by hi once per chunk.
 #include "kernels.h"
+#include <atomic>
 
 namespace flock {
 namespace gpu {
@@ -47,7 +48,7 @@ __global__ void eq_table_kernel(const F128d* __restrict__ p, uint32_t n, F128d s
 void launch_eq_table(const F128d* d_point, uint32_t n, F128d scale, F128d* out, cudaStream_t s) {
   uint64_t len = 1ull << n;
   eq_table_kernel<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(d_point, n, scale, out);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
 }
 
 __global__ void reduce_parts_kernel(const F128d* __restrict__ part, uint32_t n_blocks, uint32_t width,
@@ -61,8 +62,12 @@ __global__ void reduce_parts_kernel(const F128d* __restrict__ part, uint32_t n_b
 }
 void launch_reduce_parts(const F128d* part, uint32_t n_blocks, uint32_t width, F128d* out, cudaStream_t s) {
   reduce_parts_kernel<<<width, 256, 0, s>>>(part, n_blocks, width, out);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
 }
+
+static std::atomic<uint64_t> g_launches{0};
+uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 static int g_sm_count = 0;
 int sm_count() {
@@ -224,7 +229,7 @@ uint32_t launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32
   uint64_t groups = (n_xo + ZC_XPB - 1) / ZC_XPB;
   uint32_t blocks = (uint32_t)std::min<uint64_t>(groups, (uint64_t)sm_count());
   zc_round1_kernel<<<blocks, 256 * ZC_XPB, smem, s>>>(a, b, z, n_xo, g_zc_consts, eq_lo, lo_bits, eq_hi, part);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
   return blocks * ZC_XPB;  // partial rows of width 256
 }
 
@@ -285,7 +290,7 @@ uint32_t launch_zc_fold_skip(const F128d* a, const F128d* b, const F128d* w64, u
   uint64_t n_chunks = (n_words + (1ull << lo_bits) - 1) >> lo_bits;
   uint32_t blocks = (uint32_t)std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 8);
   zc_fold_skip_kernel<<<blocks, 256, 0, s>>>(a, b, w64, n_words, eq_lo, lo_bits, eq_hi, amlv, bmlv, part);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
   return blocks;
 }
 
@@ -341,7 +346,7 @@ uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, 
   uint64_t n_chunks = (n_pairs + (1ull << lo_bits) - 1) >> lo_bits;
   uint32_t blocks = (uint32_t)std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 8);
   pair_fold_kernel<<<blocks, 256, 0, s>>>(ain, bin, n_pairs, r, eq_lo, lo_bits, eq_hi, aout, bout, part, msg ? 1 : 0);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
   return blocks;
 }
 
@@ -353,7 +358,7 @@ __global__ void lc_eq_inner_kernel(const F128d* __restrict__ w64, const F128d* _
 }
 void launch_lc_eq_inner(const F128d* w64, const F128d* er, uint32_t K, F128d* eqi, cudaStream_t s) {
   lc_eq_inner_kernel<<<(K + 255) / 256, 256, 0, s>>>(w64, er, K, eqi);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
 }
 __global__ void csc_fold_kernel(const uint32_t* __restrict__ col_ptr, const uint32_t* __restrict__ rows,
                                 uint32_t K, const F128d* __restrict__ eqi, F128d* __restrict__ out) {
@@ -366,7 +371,7 @@ __global__ void csc_fold_kernel(const uint32_t* __restrict__ col_ptr, const uint
 void launch_csc_fold(const uint32_t* col_ptr, const uint32_t* rows, uint32_t K, const F128d* eqi, F128d* out,
                      cudaStream_t s) {
   csc_fold_kernel<<<(K + 255) / 256, 256, 0, s>>>(col_ptr, rows, K, eqi, out);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
 }
 
 // z_vec[128 cc + t] = sum_row eq(row) * bit_t(z[(cc << nu) + row]). Block = (cc, row split),
@@ -414,10 +419,10 @@ void launch_lc_zvec(const F128d* z, uint32_t nu, uint32_t used_chunks, const F12
   while ((uint64_t)used_chunks * n_split < (uint64_t)sm_count() * 8 && (n_split << 1) <= (1u << nu) / 64)
     n_split <<= 1;
   lc_zvec_kernel<<<used_chunks * n_split, 128, 0, s>>>(z, nu, n_split, eq, part);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
   uint32_t n_out = used_chunks * 128;
   lc_zvec_reduce_kernel<<<(n_out + 127) / 128, 128, 0, s>>>(part, n_split, n_out, zv);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
 }
 
 // comb = alpha comb_a + comb_b (+ beta at pin); message over the top variable:
@@ -445,7 +450,7 @@ uint32_t launch_lc_start(const F128d* ca, const F128d* cb, F128d alpha, F128d be
                          F128d* comb, const F128d* zv, F128d* part, cudaStream_t s) {
   uint32_t blocks = std::max(1u, std::min((K / 2 + 255) / 256, 256u));
   lc_start_kernel<<<blocks, 256, 0, s>>>(ca, cb, alpha, beta, pin, K, comb, zv, part);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
   return blocks;
 }
 // Bind the top variable of comb and zv (length len -> len/2) in place and emit the next
@@ -483,7 +488,7 @@ uint32_t launch_lc_round(F128d* comb, F128d* zv, uint32_t len, F128d r, bool msg
   uint32_t q = len / 4;
   uint32_t blocks = std::max(1u, std::min((q + 255) / 256, 256u));
   lc_round_kernel<<<blocks, 256, 0, s>>>(comb, zv, len, r, msg ? 1 : 0, part);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
   return blocks;
 }
 // (<w, comb_a>, <w, comb_b>), w[c] = er[c >> 6] * zp[c & 63].
@@ -505,7 +510,7 @@ uint32_t launch_lc_matrix_evals(const F128d* ca, const F128d* cb, const F128d* e
                                 F128d* part, cudaStream_t s) {
   uint32_t blocks = std::max(1u, std::min((K + 255) / 256, 256u));
   lc_matrix_evals_kernel<<<blocks, 256, 0, s>>>(ca, cb, er, zp, K, part);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
   return blocks;
 }
 // out[b] = sum_k et[k] * zv[b + 128 k]; one block per b.
@@ -520,7 +525,7 @@ __global__ void lc_s_hat_v_kernel(const F128d* __restrict__ zv, const F128d* __r
 }
 void launch_lc_s_hat_v(const F128d* zv, const F128d* et, uint32_t n_tail, F128d* out, cudaStream_t s) {
   lc_s_hat_v_kernel<<<128, 128, 0, s>>>(zv, et, n_tail, out);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
 }
 
 // ------------------------------------------------------------------ merged open
@@ -577,7 +582,7 @@ uint32_t launch_mo_build_w(const F128d* q, const F128d* er0, const F128d* ec0, c
   }
   uint32_t blocks = (uint32_t)std::min<uint64_t>((n / 2 + 511) / 512, (uint64_t)sm_count());
   mo_build_w_kernel<<<blocks, 512, smem, s>>>(q, er0, ec0, er1, ec1, tables, nu, area, n, w, part);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
   return blocks;
 }
 
@@ -594,7 +599,7 @@ __global__ void lg_eq_fill_kernel(const F128d* __restrict__ eq_lo, uint32_t lo_b
 void launch_lg_eq_fill(const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, uint64_t n, F128d* out, bool add,
                        cudaStream_t s) {
   lg_eq_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(eq_lo, lo_bits, eq_hi, n, out, add ? 1 : 0);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
 }
 // sum_i f[i * stride] (F128 words) * eq(i), chunked.
 __global__ void lg_dot_eq_kernel(const F128d* __restrict__ f, uint32_t stride, const F128d* __restrict__ eq_lo,
@@ -618,7 +623,7 @@ uint32_t launch_lg_dot_eq(const F128d* f, uint32_t stride, const F128d* eq_lo, u
   uint64_t n_chunks = (n + (1ull << lo_bits) - 1) >> lo_bits;
   uint32_t blocks = (uint32_t)std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 8);
   lg_dot_eq_kernel<<<blocks, 256, 0, s>>>(f, stride, eq_lo, lo_bits, eq_hi, n, part);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
   return blocks;
 }
 
@@ -642,7 +647,7 @@ __global__ void lg_message128_kernel(const F128d* __restrict__ f, const F128d* _
 uint32_t launch_lg_message128(const F128d* f, const F128d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s) {
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n / 2 + 255) / 256, (uint64_t)sm_count() * 8));
   lg_message128_kernel<<<blocks, 256, 0, s>>>(f, b, n, d, part);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
   return blocks;
 }
 __global__ void lg_message256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n, uint64_t d,
@@ -664,7 +669,7 @@ __global__ void lg_message256_kernel(const F256d* __restrict__ f, const F256d* _
 uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s) {
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n / 2 + 255) / 256, (uint64_t)sm_count() * 8));
   lg_message256_kernel<<<blocks, 256, 0, s>>>(f, b, n, d, part);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
   return blocks;
 }
 // o[i] = v[lo] + r (v[hi] + v[lo]), i = blk d + k, lo = 2 d blk + k.
@@ -680,7 +685,7 @@ __global__ void lg_fold128_kernel(const F128d* __restrict__ f, const F128d* __re
 void launch_lg_fold128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, uint64_t d, F256d* fo, F256d* bo,
                        cudaStream_t s) {
   lg_fold128_kernel<<<(unsigned)((n_out + 255) / 256), 256, 0, s>>>(f, b, n_out, r, d, fo, bo);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
 }
 __global__ void lg_fold256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n_out, F256d r,
                                   uint64_t d, F256d* __restrict__ fo, F256d* __restrict__ bo) {
@@ -694,7 +699,7 @@ __global__ void lg_fold256_kernel(const F256d* __restrict__ f, const F256d* __re
 void launch_lg_fold256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, uint64_t d, F256d* fo, F256d* bo,
                        cudaStream_t s) {
   lg_fold256_kernel<<<(unsigned)((n_out + 255) / 256), 256, 0, s>>>(f, b, n_out, r, d, fo, bo);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
 }
 // f' = (f.c0, f.c1) interleaved as base values; b' = (b, u b).
 __global__ void lg_code_switch_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n,
@@ -709,7 +714,7 @@ __global__ void lg_code_switch_kernel(const F256d* __restrict__ f, const F256d* 
 }
 void launch_lg_code_switch(const F256d* f, const F256d* b, uint64_t n, F256d* fo, F256d* bo, cudaStream_t s) {
   lg_code_switch_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(f, b, n, fo, bo);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
 }
 // mat[i] = f[i mod msg].c0
 __global__ void lg_replicate_kernel(const F256d* __restrict__ f, uint64_t msg, uint64_t total, F128d* __restrict__ mat) {
@@ -718,7 +723,7 @@ __global__ void lg_replicate_kernel(const F256d* __restrict__ f, uint64_t msg, u
 }
 void launch_lg_replicate(const F256d* f, uint64_t msg, uint64_t total, F128d* mat, cudaStream_t s) {
   lg_replicate_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(f, msg, total, mat);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
 }
 // Pending eq basis e = eq(z) over the (base-valued) f of length n: stores e, returns per
 // block (answer = sum f e, u0 = sum f[2j] e[2j], u2 = sum (f0 + f1)(e0 + e1)).
@@ -746,7 +751,7 @@ uint32_t launch_lg_intro_eq(const F256d* f, const F128d* eq_lo, uint32_t lo_bits
                             F128d* pend, F128d* part, cudaStream_t s) {
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n / 2 + 255) / 256, (uint64_t)sm_count() * 8));
   lg_intro_eq_kernel<<<blocks, 256, 0, s>>>(f, eq_lo, lo_bits, eq_hi, n, pend, part);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
   return blocks;
 }
 // Per-query tensor tables of the induced basis: lo_tab[q][l] = prod_{k < lo_bits, bit k of l}
@@ -801,11 +806,11 @@ uint32_t launch_lg_induced(const F128d* what, const F128d* w, uint32_t n_q, uint
   uint64_t per = (1ull << lo_bits) + (1ull << (ln - lo_bits));
   uint64_t total = per * n_q;
   lg_induced_tables_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(what, w, n_q, ln, lo_bits, lo_tab, hi_tab);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
   uint64_t n = 1ull << ln;
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, (uint64_t)sm_count() * 8));
   lg_induced_basis_kernel<<<blocks, 256, 0, s>>>(lo_tab, hi_tab, n_q, ln, lo_bits, f, basis, part);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
   return blocks;
 }
 // Glue a pending basis into b with weight beta.
@@ -825,7 +830,7 @@ __global__ void lg_glue_kernel(F256d* __restrict__ b, const F128d* __restrict__ 
 }
 void launch_lg_glue(F256d* b, const F128d* p, F128d beta, uint64_t n, bool induced, cudaStream_t s) {
   lg_glue_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, p, beta, n, induced ? 1 : 0);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
 }
 
 }  // namespace gpu

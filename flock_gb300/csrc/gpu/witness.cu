@@ -377,7 +377,7 @@ void launch_witness(int hash, const void* d_inputs, uint32_t n_inst, uint32_t nu
   else
     witness_keccak_kernel<<<blocks, threads, 0, s>>>((const uint64_t*)d_inputs, n_inst, nu, (uint64_t*)z,
                                                      (uint64_t*)a, (uint64_t*)b, used_chunks * 2);
-  CUDA_OK(cudaGetLastError());
+  LAUNCH_OK();
 }
 
 }  // namespace gpu

@@ -42,11 +42,12 @@ class _Setup:
         self._h = h
         self._lib = lib
         self.n_blocks = int(n_blocks)
-        m, lanes = ctypes.c_uint32(), ctypes.c_uint32()
+        m, lanes, kc = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
         dig = ctypes.create_string_buffer(32)
-        _native.check(lib.flock_gb300_setup_info(h, ctypes.byref(m), ctypes.byref(lanes), dig))
+        _native.check(lib.flock_gb300_setup_info(h, ctypes.byref(m), ctypes.byref(lanes), ctypes.byref(kc), dig))
         self.m = m.value
         self.lanes = lanes.value
+        self.log_code_len = kc.value
         self.registry_digest = dig.raw
 
     def close(self) -> None:
@@ -94,6 +95,42 @@ class _Setup:
         finally:
             self._lib.flock_gb300_free(out)
         del keep
+
+    def prove_fast_device_bytes(self, d_inputs: int, n_inputs: int, domain: bytes) -> bytes:
+        """prove_fast from input records already in device memory (raw device pointer)."""
+        if self._h is None:
+            raise RuntimeError("setup is closed")
+        out = ctypes.POINTER(ctypes.c_uint8)()
+        out_len = ctypes.c_size_t()
+        _native.check(self._lib.flock_gb300_prove_fast_device(self._h, ctypes.c_void_p(d_inputs), n_inputs, domain,
+                                                              len(domain), ctypes.byref(out), ctypes.byref(out_len)))
+        try:
+            return ctypes.string_at(out, out_len.value)
+        finally:
+            self._lib.flock_gb300_free(out)
+
+    def stream_handle(self) -> int:
+        """The cudaStream_t (as an integer) every kernel of this setup runs on."""
+        h = ctypes.c_void_p()
+        _native.check(self._lib.flock_gb300_setup_stream(self._h, ctypes.byref(h)))
+        return h.value or 0
+
+    def set_stage_timing(self, enabled: bool) -> None:
+        _native.check(self._lib.flock_gb300_set_stage_timing(self._h, 1 if enabled else 0))
+
+    def last_stage_ms(self) -> dict:
+        """{stage: (device ms, kernel launches)} of the last prove (stage timing enabled)."""
+        ms = (ctypes.c_double * 32)()
+        ln = (ctypes.c_uint32 * 32)()
+        n = self._lib.flock_gb300_last_stage_ms(self._h, ms, ln, 32)
+        if n < 0:
+            _native.check(n)
+        return {self._lib.flock_gb300_stage_name(i).decode(): (ms[i], ln[i]) for i in range(n)}
+
+    def last_transfer_bytes(self) -> tuple:
+        h2d, d2h = ctypes.c_uint64(), ctypes.c_uint64()
+        _native.check(self._lib.flock_gb300_last_transfer_bytes(self._h, ctypes.byref(h2d), ctypes.byref(d2h)))
+        return h2d.value, d2h.value
 
     def prove_fast(self, inputs: Inputs, domain: bytes) -> ProofBundle:
         return ProofBundle.parse(self.prove_fast_bytes(inputs, domain))

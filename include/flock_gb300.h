@@ -54,8 +54,10 @@ size_t flock_gb300_input_record_bytes(int hash_kind);
 int flock_gb300_setup_new(int hash_kind, uint64_t n_blocks, flock_gb300_setup** out);
 void flock_gb300_setup_free(flock_gb300_setup* setup);
 
-/* Committed dimension m, lanes t and the 32-byte registry digest of a setup. */
-int flock_gb300_setup_info(const flock_gb300_setup* setup, uint32_t* m, uint32_t* lanes, uint8_t digest[32]);
+/* Committed dimension m, commit lanes t, log2 of the L0 codeword length and the 32-byte
+ * registry digest of a setup (any output pointer may be null). */
+int flock_gb300_setup_info(const flock_gb300_setup* setup, uint32_t* m, uint32_t* lanes, uint32_t* log_code_len,
+                           uint8_t digest[32]);
 
 /* prove_fast(inputs, &mut FsChallenger::new(domain)) on the GPU. n_inputs must equal the
  * setup's n_blocks (the reference asserts the same). On success *out receives a malloc'd
@@ -70,6 +72,29 @@ int flock_gb300_setup_info(const flock_gb300_setup* setup, uint32_t* m, uint32_t
  * (cuda-ghash/prove_ffi.cu:420). */
 int flock_gb300_prove_fast(flock_gb300_setup* setup, const void* inputs, size_t n_inputs, const uint8_t* domain,
                            size_t domain_len, uint8_t** out, size_t* out_len);
+
+/* prove_fast with the input records already in device memory (a device pointer on the
+ * setup's device, n_inputs packed records, left unmodified). Same output as
+ * flock_gb300_prove_fast; the host-to-device copy of the inputs is skipped. No
+ * reference counterpart: the reference proves from host slices only. */
+int flock_gb300_prove_fast_device(flock_gb300_setup* setup, const void* d_inputs, size_t n_inputs,
+                                  const uint8_t* domain, size_t domain_len, uint8_t** out, size_t* out_len);
+
+/* The CUDA stream (cudaStream_t) every kernel of this setup runs on. */
+int flock_gb300_setup_stream(const flock_gb300_setup* setup, void** stream);
+
+/* Device-time breakdown. When enabled, each prove records CUDA events around its stages;
+ * flock_gb300_last_stage_ms then fills up to `cap` entries of milliseconds and kernel
+ * launch counts per stage (names from flock_gb300_stage_name) and returns the stage count. */
+int flock_gb300_set_stage_timing(flock_gb300_setup* setup, int enabled);
+int flock_gb300_last_stage_ms(flock_gb300_setup* setup, double* ms, uint32_t* launches, int cap);
+const char* flock_gb300_stage_name(int stage);
+
+/* Bytes copied host-to-device and device-to-host by the last prove on this setup. */
+int flock_gb300_last_transfer_bytes(const flock_gb300_setup* setup, uint64_t* h2d, uint64_t* d2h);
+
+/* Kernel launches issued by the library so far (all setups, all threads). */
+uint64_t flock_gb300_launch_count(void);
 
 /* Host wall-clock milliseconds of the last prove on this setup:
  * [witness, commit, zerocheck, lincheck, open, total]. */
