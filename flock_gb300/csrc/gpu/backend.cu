@@ -12,24 +12,10 @@ namespace gpu {
 
 namespace {
 
-// GF(2^8) exp / log tables with generator 0x03.
-void gf8_exp_log(uint8_t gexp[512], uint8_t glog[256]) {
-  uint8_t x = 1;
-  for (int i = 0; i < 255; ++i) {
-    gexp[i] = x;
-    glog[x] = (uint8_t)i;
-    x = gf8_mul(x, 3);
-  }
-  for (int i = 255; i < 512; ++i) gexp[i] = gexp[i - 255];
-  glog[0] = 0;
-}
-
 std::once_flag g_consts_once;
 void upload_constants_once() {
   std::call_once(g_consts_once, [] {
     const SkipTables& st = skip_tables();
-    uint8_t gexp[512], glog[256];
-    gf8_exp_log(gexp, glog);
     // eq factor of the three small zerocheck constants (bit j of K selects c_j or 1 + c_j)
     const uint8_t c[3] = {0xF7, 0x53, 0xB5};
     uint8_t mulk[8][256], e2[4];
@@ -43,7 +29,7 @@ void upload_constants_once() {
       for (int j = 0; j < 2; ++j) e = gf8_mul(e, ((K2 >> j) & 1) ? c[j + 1] : (uint8_t)(c[j + 1] ^ 1));
       e2[K2] = e;
     }
-    upload_zc_consts(st.ext.data(), reinterpret_cast<const F128d*>(phi8_table().data()), gexp, glog, mulk, e2);
+    upload_zc_consts(st.ext.data(), reinterpret_cast<const F128d*>(phi8_table().data()), mulk, e2);
   });
 }
 
@@ -124,8 +110,12 @@ GpuBackend::GpuBackend(const Statement& s) : S(s) {
   stage_cap_ = size_t(8) << 20;
   d_stage_ = dmalloc<uint8_t>(stage_cap_, owned_);
   CUDA_OK(cudaMallocHost(&h_stage_, stage_cap_));
-  // twiddles of the L0 transform
+  CUDA_OK(cudaStreamCreateWithFlags(&pow_st_, cudaStreamNonBlocking));
+  d_pow_ = dmalloc<unsigned long long>(1, owned_);
+  CUDA_OK(cudaMallocHost(&h_pow_, sizeof(unsigned long long)));
+  // twiddles of the L0 transform; host tables used by every prove
   tw0_ = twiddles(S.k_code);
+  (void)moore_inverse();
   CUDA_OK(cudaDeviceSynchronize());
 }
 
@@ -138,6 +128,8 @@ GpuBackend::~GpuBackend() {
   cudaFreeHost(h_in_);
   cudaFreeHost(h_red_);
   cudaFreeHost(h_stage_);
+  cudaFreeHost(h_pow_);
+  cudaStreamDestroy(pow_st_);
   cudaStreamDestroy(st_);
 }
 
@@ -199,6 +191,28 @@ void GpuBackend::stage_ms(double out[ST_COUNT], uint32_t launches[ST_COUNT]) {
     out[sp.st] += ms;
     launches[sp.st] += (uint32_t)sp.launches;
   }
+}
+
+// ---- proof of work
+uint64_t GpuBackend::gpu_pow(const std::array<uint8_t, 32>& digest, uint32_t bits) {
+  std::lock_guard<std::mutex> g(pow_mu_);
+  uint32_t words[8];
+  memcpy(words, digest.data(), 32);
+  // ~e^-16 chance that a window of 16 * 2^bits nonces holds no solution; then the next one
+  const uint64_t window = uint64_t(16) << bits;
+  for (uint64_t start = 0;; start += window) {
+    CUDA_OK(cudaMemsetAsync(d_pow_, 0xFF, sizeof(unsigned long long), pow_st_));
+    launch_pow(words, bits, start, window, d_pow_, pow_st_);
+    CUDA_OK(cudaMemcpyAsync(h_pow_, d_pow_, sizeof(unsigned long long), cudaMemcpyDeviceToHost, pow_st_));
+    CUDA_OK(cudaStreamSynchronize(pow_st_));
+    if (*h_pow_ != ~0ull) return *h_pow_;
+  }
+}
+PowSearchFn GpuBackend::pow_search() {
+  return [this](const std::array<uint8_t, 32>& digest, uint32_t bits) -> uint64_t {
+    if (bits < 6) return pow_search_host(digest, bits);
+    return gpu_pow(digest, bits);
+  };
 }
 
 // ---- staging helpers
@@ -305,15 +319,36 @@ void GpuBackend::zc_round1(const std::vector<F128>& r, std::vector<F128>& ab, st
     Mark mk(this, ST_ZC_ROUND1);
     nb = launch_zc_round1(a_, b_, z_, m, e.lo, e.lo_bits, e.hi, part_, st_);
   }
-  auto v = reduce(nb, 256);
+  auto v = reduce(nb, 192);
   // D = prod (1 + g_i)^-1 over the medium constants' g_i = x^1, x^2, x^4, x^8
   F128 D = F128::one();
   for (int e : {1, 2, 4, 8}) D = D * inv(F128::one() + F128(1ull << e, 0));
   ab.assign(64, F128());
-  c.assign(64, F128());
   svc.assign(128, F128());
-  for (int i = 0; i < 64; ++i) { ab[i] = D * v[i]; c[i] = D * v[64 + i]; }
-  for (int i = 0; i < 128; ++i) svc[i] = D * v[128 + i];
+  for (int i = 0; i < 64; ++i) ab[i] = D * v[i];
+  for (int i = 0; i < 128; ++i) svc[i] = D * v[64 + i];
+  // P_c(i) = sum_s phi8(unit_s(i)) * S_s with S_s = sum_x eq(x) bit_s(z_x); row x = 2w + h
+  // splits eq(r[6..m], x) = eq(r_6, h) * eq(r[7..m], w), so S_s = (1 + r_6) svc[s] + r_6 svc[64 + s].
+  // phi8 is additive: sum over the set bits b of unit_s(i) of phi8(2^b) * S_s.
+  const SkipTables& st = skip_tables();
+  F128 T[8][64];
+  for (int s = 0; s < 64; ++s) {
+    F128 Ss = (F128::one() + r[6]) * svc[s] + r[6] * svc[64 + s];
+    for (int bit = 0; bit < 8; ++bit) T[bit][s] = phi8((uint8_t)(1u << bit)) * Ss;
+  }
+  c.assign(64, F128());
+  for (int i = 0; i < 64; ++i) {
+    F128 acc;
+    for (int s = 0; s < 64; ++s) {
+      uint8_t u = st.unit[s][i];
+      while (u) {
+        int bit = __builtin_ctz(u);
+        acc += T[bit][s];
+        u &= u - 1;
+      }
+    }
+    c[i] = acc;
+  }
 }
 
 void GpuBackend::zc_fold_skip(const std::vector<F128>& w, const std::vector<F128>& eq_point, F128& g1, F128& gi) {
@@ -607,21 +642,24 @@ Msg256 GpuBackend::lg_introduce_eq(const std::vector<F128>& zp, F128& answer) {
   return m;
 }
 
-Msg256 GpuBackend::lg_introduce_induced(uint32_t ln, const std::vector<F128>& w,
-                                        const std::vector<std::vector<F128>>& what) {
+Msg256 GpuBackend::lg_introduce_induced(uint32_t ln, uint32_t log_rate, const std::vector<uint64_t>& pos,
+                                        const std::vector<F128>& w, const std::vector<std::vector<F128>>&) {
   scr_off_ = 0;
   if ((uint64_t(2) << ln) != lg_n_) throw std::runtime_error("induced basis size mismatch");
+  if (pos.size() != w.size()) throw std::runtime_error("induced basis: one weight per position");
+  uint32_t log_d = ln + log_rate;
+  for (uint64_t p : pos)
+    if (p >> log_d) throw std::runtime_error("induced basis: position outside the codeword");
   uint32_t nq = (uint32_t)w.size();
-  std::vector<F128> flat;
-  flat.reserve((size_t)nq * ln);
-  for (auto& q : what) flat.insert(flat.end(), q.begin(), q.end());
-  const F128d* dwhat = upload(flat);
+  const uint64_t* dpos = static_cast<const uint64_t*>(upload(pos.data(), pos.size() * 8));
   const F128d* dw = upload(w);
-  uint32_t lo_bits = ln / 2;
-  F128d* lo_tab = static_cast<F128d*>(scratch((size_t)nq * (size_t(16) << lo_bits)));
-  F128d* hi_tab = static_cast<F128d*>(scratch((size_t)nq * (size_t(16) << (ln - lo_bits))));
+  F128d* y = static_cast<F128d*>(scratch(size_t(16) << log_d));
+  const F128d* tw = twiddles(log_d);
   uint32_t nb;
-  { Mark mk(this, ST_LIGERITO); nb = launch_lg_induced(dwhat, dw, nq, ln, lf_[lg_cur_], lo_tab, hi_tab, pend_, part_, st_); }
+  {
+    Mark mk(this, ST_LIGERITO);
+    nb = launch_lg_induced(dpos, dw, nq, ln, log_rate, tw, lf_[lg_cur_], y, pend_, part_, st_);
+  }
   auto v = reduce(nb, 2);
   pend_induced_ = true;
   pend_n_ = uint64_t(1) << ln;

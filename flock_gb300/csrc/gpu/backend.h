@@ -42,12 +42,16 @@ class GpuBackend : public ProverBackend {
   void lg_commit(uint32_t level, uint32_t log_cols, uint32_t log_lanes, uint32_t log_rate, uint32_t cap_depth,
                  std::vector<Hash>& cap) override;
   Msg256 lg_introduce_eq(const std::vector<F128>& z, F128& answer) override;
-  Msg256 lg_introduce_induced(uint32_t log_msg_cols, const std::vector<F128>& w,
-                              const std::vector<std::vector<F128>>& what) override;
+  Msg256 lg_introduce_induced(uint32_t log_msg_cols, uint32_t log_rate, const std::vector<uint64_t>& positions,
+                              const std::vector<F128>& w, const std::vector<std::vector<F128>>& what) override;
+  bool induced_from_positions() const override { return true; }
   void lg_glue(F128 beta) override;
   void lg_open(uint32_t level, const std::vector<uint64_t>& positions, uint32_t cap_depth,
                std::vector<std::vector<F128>>& rows, std::vector<Hash>& paths) override;
   std::vector<F256> lg_residual() override;
+  // Proof-of-work searches of 6 or more bits run on the device (own stream, thread-safe:
+  // the forked multipoint transcript grinds concurrently with the main one).
+  PowSearchFn pow_search() override;
 
   // Device-time breakdown of a prove (CUDA events on the backend's stream).
   enum Stage {
@@ -152,6 +156,12 @@ class GpuBackend : public ProverBackend {
   bool pend_induced_ = false;
   uint64_t pend_n_ = 0;
   std::vector<Level> levels_;
+
+  std::mutex pow_mu_;
+  cudaStream_t pow_st_ = nullptr;
+  unsigned long long* d_pow_ = nullptr;
+  unsigned long long* h_pow_ = nullptr;
+  uint64_t gpu_pow(const std::array<uint8_t, 32>& digest, uint32_t bits);
 
   F128d* part_ = nullptr;
   uint32_t part_cap_ = 0;

@@ -41,6 +41,8 @@ void launch_fill_lane_major(const F128d* q, F128d* cw, uint32_t lanes, uint32_t 
                             cudaStream_t s);
 void launch_ntt(F128d* data, uint32_t lanes, uint32_t log_d, uint32_t start_layer, const F128d* tw, cudaStream_t s);
 void launch_merkle(const F128d* rows, uint32_t lanes, uint64_t n_leaves, uint8_t* tree, cudaStream_t s);
+void launch_pow(const uint32_t digest_le[8], uint32_t bits, uint64_t start, uint64_t count,
+                unsigned long long* d_result, cudaStream_t s);
 void launch_gather_rows(const F128d* mat, uint32_t lanes, const uint64_t* d_pos, uint32_t n, F128d* out,
                         cudaStream_t s);
 void launch_gather_paths(const uint8_t* tree, uint64_t n_leaves, const uint64_t* d_pos, uint32_t n,
@@ -51,10 +53,9 @@ void launch_gather_paths(const uint8_t* tree, uint64_t n_leaves, const uint64_t*
 void launch_eq_table(const F128d* d_point, uint32_t n, F128d scale, F128d* out, cudaStream_t s);
 void launch_reduce_parts(const F128d* part, uint32_t n_blocks, uint32_t width, F128d* out, cudaStream_t s);
 
-void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t* gexp, const uint8_t* glog,
-                      const uint8_t mulk[8][256], const uint8_t e2[4]);
+void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t mulk[8][256], const uint8_t e2[4]);
 uint32_t launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32_t m, const F128d* eq_lo,
-                          uint32_t lo_bits, const F128d* eq_hi, F128d* part, cudaStream_t s);          // width 256
+                          uint32_t lo_bits, const F128d* eq_hi, F128d* part, cudaStream_t s);          // width 192
 uint32_t launch_zc_fold_skip(const F128d* a, const F128d* b, const F128d* w64, uint64_t n_words, const F128d* eq_lo,
                              uint32_t lo_bits, const F128d* eq_hi, F128d* amlv, F128d* bmlv, F128d* part,
                              cudaStream_t s);                                                          // width 2
@@ -92,8 +93,9 @@ void launch_lg_code_switch(const F256d* f, const F256d* b, uint64_t n, F256d* fo
 void launch_lg_replicate(const F256d* f, uint64_t msg, uint64_t total, F128d* mat, cudaStream_t s);
 uint32_t launch_lg_intro_eq(const F256d* f, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, uint64_t n,
                             F128d* pend, F128d* part, cudaStream_t s);                                 // width 3
-uint32_t launch_lg_induced(const F128d* what, const F128d* w, uint32_t n_q, uint32_t ln, const F256d* f,
-                           F128d* lo_tab, F128d* hi_tab, F128d* basis, F128d* part, cudaStream_t s);   // width 2
+uint32_t launch_lg_induced(const uint64_t* pos, const F128d* w, uint32_t n_q, uint32_t ln, uint32_t log_rate,
+                           const F128d* tw, const F256d* f, F128d* y, F128d* basis, F128d* part,
+                           cudaStream_t s);                                                            // width 2
 void launch_lg_glue(F256d* b, const F128d* p, F128d beta, uint64_t n, bool induced, cudaStream_t s);
 
 }  // namespace gpu

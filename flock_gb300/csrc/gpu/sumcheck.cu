@@ -85,28 +85,39 @@ int sm_count() {
 //   eq(r[6..m], x) = phi8(e_K) * D * x^M * eq(r[13..m], xo),
 // e_K = prod_j (K_j ? c_j : 1 + c_j) over the three GF(2^8) constants c_j (phi8 is a
 // ring embedding), and D = prod_i (1 + g_i)^-1 over the medium constants g_i = x^(2^i)
-// (the bit-1 factor g/(1+g) and the bit-0 factor 1/(1+g)). Hence per output i
-//   P(i) = D * sum_xo eq_o(xo) * sum_M x^M * phi8( sum_K e_K * p_x(i) )
-// with p_x(i) the GF(2^8) value of the row at Lambda point i. The inner sums are
-// GF(2^8) byte arithmetic; each xo costs one F128 multiply per output. D is applied
-// by the host.
-//   ab[i]  : p = ext(a_x)[i] * ext(b_x)[i]    c[i] : p = ext(z_x)[i]
-//   svc[t] : per word w = (K2: 2 bits, M, xo), p = bit t of z_w with e2 over r[7], r[8].
+// (the bit-1 factor g/(1+g) and the bit-0 factor 1/(1+g)). Hence per Lambda point i
+//   P_ab(i) = D * sum_xo eq_o(xo) * sum_M x^M * phi8( sum_K e_K * ext(a_x)(i) * ext(b_x)(i) )
+// where the inner sums are GF(2^8) byte arithmetic and each xo costs one F128 multiply
+// per output. The same factorisation over words w = (K2: 2 bits, M, xo) with e2 over
+// r[7], r[8] gives s_hat_v_c[t] from bit t of z_w. P_c needs no pass of its own: it is
+// linear in the z bits and the host derives it from s_hat_v_c. D is applied by the host.
 struct ZcConsts {
-  uint8_t ext[8 * 256 * 64];
+  uint8_t ext[8 * 256 * 64];   // ext[c][v][i]: extension of byte v at S[8c..8c+8)
   F128d phi8[256];
-  uint8_t gexp[512], glog[256];
-  uint8_t mulk[8][256];
+  uint8_t mulk[8][256];        // e_K * v
   uint8_t e2[4];
 };
 
 constexpr int ZC_XPB = 4;  // xo groups in flight per block (256 threads each)
 struct ZcStage {
   F128d wa[64], wb[64], wz[64];
-  uint32_t gab[16][16], gc[16][16];
+  uint32_t gab[16][16];
   F128d eqo;
 };
 constexpr size_t ZC_CONST_BYTES = (sizeof(ZcConsts) + 15) & ~size_t(15);
+
+// Four GF(2^8) products (AES polynomial) of packed bytes, shift-and-add in registers.
+__device__ __forceinline__ uint32_t gf8_mul4(uint32_t a, uint32_t b) {
+  uint32_t r = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    uint32_t m = ((b >> k) & 0x01010101u) * 0xFFu;
+    r ^= a & m;
+    uint32_t hi = (a >> 7) & 0x01010101u;
+    a = ((a & 0x7F7F7F7Fu) << 1) ^ (hi * 0x1Bu);
+  }
+  return r;
+}
 
 __global__ void __launch_bounds__(256 * ZC_XPB, 1)
 zc_round1_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, const F128d* __restrict__ z,
@@ -118,10 +129,7 @@ zc_round1_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, const
   {
     const uint4* src = reinterpret_cast<const uint4*>(gconst);
     uint4* dst = reinterpret_cast<uint4*>(smem);
-    for (uint32_t i = threadIdx.x; i < sizeof(ZcConsts) / 16; i += blockDim.x) dst[i] = src[i];
-    // tail bytes (struct size need not be a multiple of 16)
-    for (uint32_t i = (sizeof(ZcConsts) / 16) * 16 + threadIdx.x; i < sizeof(ZcConsts); i += blockDim.x)
-      smem[i] = reinterpret_cast<const uint8_t*>(gconst)[i];
+    for (uint32_t i = threadIdx.x; i < ZC_CONST_BYTES / 16; i += blockDim.x) dst[i] = src[i];
   }
   const uint32_t sub = threadIdx.x >> 8, t = threadIdx.x & 255;
   ZcStage& S = stages[sub];
@@ -141,44 +149,34 @@ zc_round1_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, const
     __syncthreads();
     if (live) {
       const uint32_t M = t >> 4, lane = t & 15;
-      uint32_t gab = 0, gc = 0;
-#pragma unroll 1
+      uint32_t gab = 0;
+#pragma unroll 2
       for (uint32_t K = 0; K < 8; ++K) {
         uint32_t xl = 8 * M + K, w = xl >> 1;
         uint64_t ab = (xl & 1) ? S.wa[w].hi : S.wa[w].lo;
         uint64_t bb = (xl & 1) ? S.wb[w].hi : S.wb[w].lo;
-        uint64_t zb = (xl & 1) ? S.wz[w].hi : S.wz[w].lo;
-        uint32_t ea = 0, eb = 0, ec = 0;
+        uint32_t ea = 0, eb = 0;
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
           ea ^= ext32[((c << 8) + ((ab >> (8 * c)) & 255)) * 16 + lane];
           eb ^= ext32[((c << 8) + ((bb >> (8 * c)) & 255)) * 16 + lane];
-          ec ^= ext32[((c << 8) + ((zb >> (8 * c)) & 255)) * 16 + lane];
         }
-        uint32_t p = 0, q = 0;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          uint32_t x = (ea >> (8 * k)) & 255, y = (eb >> (8 * k)) & 255;
-          uint32_t pr = (x && y) ? C.gexp[C.glog[x] + C.glog[y]] : 0;
-          p |= (uint32_t)C.mulk[K][pr] << (8 * k);
-          q |= (uint32_t)C.mulk[K][(ec >> (8 * k)) & 255] << (8 * k);
-        }
-        gab ^= p;
-        gc ^= q;
+        uint32_t p = gf8_mul4(ea, eb);
+        const uint8_t* mk = C.mulk[K];
+        gab ^= (uint32_t)mk[p & 255] | ((uint32_t)mk[(p >> 8) & 255] << 8) | ((uint32_t)mk[(p >> 16) & 255] << 16) |
+               ((uint32_t)mk[p >> 24] << 24);
       }
       S.gab[M][lane] = gab;
-      S.gc[M][lane] = gc;
     }
     __syncthreads();
-    if (live) {
+    if (live && t < 192) {
       F128d F = f128_zero();
-      if (t < 128) {
-        const uint8_t* G = reinterpret_cast<const uint8_t*>(t < 64 ? &S.gab[0][0] : &S.gc[0][0]);
-        uint32_t i = t & 63;
+      if (t < 64) {
+        const uint8_t* G = reinterpret_cast<const uint8_t*>(&S.gab[0][0]);
 #pragma unroll
-        for (int M = 15; M >= 0; --M) F = mul_by_x(F) + C.phi8[G[M * 64 + i]];
+        for (int M = 15; M >= 0; --M) F = mul_by_x(F) + C.phi8[G[M * 64 + t]];
       } else {
-        uint32_t tb = t - 128, limb = tb >> 6, sh = tb & 63;
+        uint32_t tb = t - 64, limb = tb >> 6, sh = tb & 63;
 #pragma unroll
         for (int M = 15; M >= 0; --M) {
           uint32_t gv = 0;
@@ -186,7 +184,7 @@ zc_round1_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, const
           for (int K2 = 0; K2 < 4; ++K2) {
             const F128d& wv = S.wz[4 * M + K2];
             uint64_t bits = limb ? wv.hi : wv.lo;
-            if ((bits >> sh) & 1) gv ^= C.e2[K2];
+            gv ^= (uint32_t)C.e2[K2] & (0u - (uint32_t)((bits >> sh) & 1));
           }
           F = mul_by_x(F) + C.phi8[gv];
         }
@@ -195,22 +193,20 @@ zc_round1_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, const
     }
     __syncthreads();
   }
-  part[((uint64_t)blockIdx.x * ZC_XPB + sub) * 256 + t] = acc;
+  if (t < 192) part[((uint64_t)blockIdx.x * ZC_XPB + sub) * 192 + t] = acc;
 }
 
 static ZcConsts* g_zc_consts = nullptr;
-void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t* gexp, const uint8_t* glog,
-                      const uint8_t mulk[8][256], const uint8_t e2[4]) {
+void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t mulk[8][256], const uint8_t e2[4]) {
   if (g_zc_consts) return;
   ZcConsts* h = new ZcConsts();
   memcpy(h->ext, ext, sizeof(h->ext));
   memcpy(h->phi8, phi8, sizeof(h->phi8));
-  memcpy(h->gexp, gexp, 512);
-  memcpy(h->glog, glog, 256);
   memcpy(h->mulk, mulk, sizeof(h->mulk));
   memcpy(h->e2, e2, 4);
   ZcConsts* d = nullptr;
-  CUDA_OK(cudaMalloc(&d, sizeof(ZcConsts)));
+  CUDA_OK(cudaMalloc(&d, ZC_CONST_BYTES));
+  CUDA_OK(cudaMemset(d, 0, ZC_CONST_BYTES));
   CUDA_OK(cudaMemcpy(d, h, sizeof(ZcConsts), cudaMemcpyHostToDevice));
   delete h;
   g_zc_consts = d;
@@ -230,7 +226,7 @@ uint32_t launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32
   uint32_t blocks = (uint32_t)std::min<uint64_t>(groups, (uint64_t)sm_count());
   zc_round1_kernel<<<blocks, 256 * ZC_XPB, smem, s>>>(a, b, z, n_xo, g_zc_consts, eq_lo, lo_bits, eq_hi, part);
   LAUNCH_OK();
-  return blocks * ZC_XPB;  // partial rows of width 256
+  return blocks * ZC_XPB;  // partial rows of width 192: ab[64] then s_hat_v_c[128]
 }
 
 // ------------------------------------------------------------------ zerocheck skip fold
@@ -360,17 +356,22 @@ void launch_lc_eq_inner(const F128d* w64, const F128d* er, uint32_t K, F128d* eq
   lc_eq_inner_kernel<<<(K + 255) / 256, 256, 0, s>>>(w64, er, K, eqi);
   LAUNCH_OK();
 }
+// One warp per column: consecutive lanes read consecutive row indices.
 __global__ void csc_fold_kernel(const uint32_t* __restrict__ col_ptr, const uint32_t* __restrict__ rows,
                                 uint32_t K, const F128d* __restrict__ eqi, F128d* __restrict__ out) {
-  uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= K) return;
-  F128d acc = f128_zero();
-  for (uint32_t p = col_ptr[c]; p < col_ptr[c + 1]; ++p) acc += eqi[rows[p]];
-  out[c] = acc;
+  uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t c = warp; c < K; c += n_warps) {
+    F128d acc = f128_zero();
+    for (uint32_t p = col_ptr[c] + lane; p < col_ptr[c + 1]; p += 32) acc += eqi[__ldg(rows + p)];
+    acc = warp_xor(acc);
+    if (lane == 0) out[c] = acc;
+  }
 }
 void launch_csc_fold(const uint32_t* col_ptr, const uint32_t* rows, uint32_t K, const F128d* eqi, F128d* out,
                      cudaStream_t s) {
-  csc_fold_kernel<<<(K + 255) / 256, 256, 0, s>>>(col_ptr, rows, K, eqi, out);
+  uint32_t blocks = std::min<uint32_t>((K + 7) / 8, (uint32_t)sm_count() * 16);
+  csc_fold_kernel<<<blocks, 256, 0, s>>>(col_ptr, rows, K, eqi, out);
   LAUNCH_OK();
 }
 
@@ -754,43 +755,41 @@ uint32_t launch_lg_intro_eq(const F256d* f, const F128d* eq_lo, uint32_t lo_bits
   LAUNCH_OK();
   return blocks;
 }
-// Per-query tensor tables of the induced basis: lo_tab[q][l] = prod_{k < lo_bits, bit k of l}
-// what[q][k]; hi_tab[q][h] = w[q] * prod_{k >= lo_bits, bit (k - lo_bits) of h} what[q][k].
-__global__ void lg_induced_tables_kernel(const F128d* __restrict__ what, const F128d* __restrict__ w, uint32_t n_q,
-                                         uint32_t ln, uint32_t lo_bits, F128d* __restrict__ lo_tab,
-                                         F128d* __restrict__ hi_tab) {
-  uint32_t lo_n = 1u << lo_bits, hi_bits = ln - lo_bits, hi_n = 1u << hi_bits;
-  uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  uint64_t per = lo_n + hi_n;
-  if (e >= (uint64_t)n_q * per) return;
-  uint32_t q = (uint32_t)(e / per), i = (uint32_t)(e % per);
-  const F128d* wh = what + (uint64_t)q * ln;
-  if (i < lo_n) {
-    F128d v = f128_one();
-    for (uint32_t k = 0; k < lo_bits; ++k)
-      if ((i >> k) & 1) v = v * wh[k];
-    lo_tab[(uint64_t)q * lo_n + i] = v;
-  } else {
-    uint32_t h = i - lo_n;
-    F128d v = w[q];
-    for (uint32_t k = 0; k < hi_bits; ++k)
-      if ((h >> k) & 1) v = v * wh[lo_bits + k];
-    hi_tab[(uint64_t)q * hi_n + h] = v;
-  }
+// Induced basis of the queried positions. The level's codeword is the NTT (layers
+// [log_rate, log_d)) of the message replicated 2^log_rate times, so for weights w_q at
+// positions pos_q
+//   basis = R^T . L_rate^T ... L_{log_d-1}^T . (sum_q w_q e_{pos_q}),
+// with the transposed butterfly (u, v) -> (u + v, v + t (u + v)) and R^T the sum over
+// the replicas. One scatter, log_d - log_rate transposed layers and the replica fold.
+__global__ void lg_scatter_kernel(const uint64_t* __restrict__ pos, const F128d* __restrict__ w, uint32_t n_q,
+                                  F128d* __restrict__ y) {
+  uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n_q) return;
+  unsigned long long* p = reinterpret_cast<unsigned long long*>(y + pos[q]);
+  atomicXor(p, (unsigned long long)w[q].lo);
+  atomicXor(p + 1, (unsigned long long)w[q].hi);
 }
-// basis[i] = sum_q lo_tab[q][i & lo_mask] * hi_tab[q][i >> lo_bits]; with the split
-// f (length 2n): a = sum f[2i] basis[i], s = sum (f[2i] + f[2i+1]) basis[i].
-__global__ void lg_induced_basis_kernel(const F128d* __restrict__ lo_tab, const F128d* __restrict__ hi_tab,
-                                        uint32_t n_q, uint32_t ln, uint32_t lo_bits, const F256d* __restrict__ f,
-                                        F128d* __restrict__ basis, F128d* __restrict__ part) {
+__global__ void ntt_t_layer_kernel(F128d* __restrict__ y, uint32_t log_d, uint32_t layer, const F128d* __restrict__ tw) {
+  uint64_t pair = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pair >= (1ull << (log_d - 1))) return;
+  uint32_t sh = log_d - layer - 1;
+  uint64_t blk = pair >> sh, within = pair & ((1ull << sh) - 1);
+  uint64_t i0 = (blk << (sh + 1)) + within, i1 = i0 + (1ull << sh);
+  F128d t = tw[(1ull << layer) - 1 + blk];
+  F128d u = y[i0], v = y[i1], sum = u + v;
+  y[i0] = sum;
+  y[i1] = v + t * sum;
+}
+// basis[i] = sum_rep y[rep * n + i]; with the split f (length 2n):
+// a = sum f[2i] basis[i], s = sum (f[2i] + f[2i+1]) basis[i].
+__global__ void lg_induced_fold_kernel(const F128d* __restrict__ y, uint32_t ln, uint32_t log_rate,
+                                       const F256d* __restrict__ f, F128d* __restrict__ basis, F128d* __restrict__ part) {
   __shared__ F128d sh[32];
-  uint32_t lo_n = 1u << lo_bits, hi_n = 1u << (ln - lo_bits);
   uint64_t n = 1ull << ln;
   F128d A = f128_zero(), Sm = f128_zero();
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    uint32_t l = (uint32_t)(i & (lo_n - 1)), h = (uint32_t)(i >> lo_bits);
     F128d acc = f128_zero();
-    for (uint32_t q = 0; q < n_q; ++q) acc += lo_tab[(uint64_t)q * lo_n + l] * hi_tab[(uint64_t)q * hi_n + h];
+    for (uint64_t rep = 0; rep < (1ull << log_rate); ++rep) acc += y[rep * n + i];
     basis[i] = acc;
     F128d f0 = f[2 * i].c0, f1 = f[2 * i + 1].c0;
     A += f0 * acc;
@@ -800,16 +799,20 @@ __global__ void lg_induced_basis_kernel(const F128d* __restrict__ lo_tab, const 
   Sm = block_xor(Sm, sh);
   if (threadIdx.x == 0) { part[blockIdx.x * 2] = A; part[blockIdx.x * 2 + 1] = Sm; }
 }
-uint32_t launch_lg_induced(const F128d* what, const F128d* w, uint32_t n_q, uint32_t ln, const F256d* f,
-                           F128d* lo_tab, F128d* hi_tab, F128d* basis, F128d* part, cudaStream_t s) {
-  uint32_t lo_bits = ln / 2;
-  uint64_t per = (1ull << lo_bits) + (1ull << (ln - lo_bits));
-  uint64_t total = per * n_q;
-  lg_induced_tables_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(what, w, n_q, ln, lo_bits, lo_tab, hi_tab);
+uint32_t launch_lg_induced(const uint64_t* pos, const F128d* w, uint32_t n_q, uint32_t ln, uint32_t log_rate,
+                           const F128d* tw, const F256d* f, F128d* y, F128d* basis, F128d* part, cudaStream_t s) {
+  uint32_t log_d = ln + log_rate;
+  CUDA_OK(cudaMemsetAsync(y, 0, (sizeof(F128d)) << log_d, s));
+  lg_scatter_kernel<<<(n_q + 127) / 128, 128, 0, s>>>(pos, w, n_q, y);
   LAUNCH_OK();
+  uint64_t pairs = 1ull << (log_d - 1);
+  for (int layer = (int)log_d - 1; layer >= (int)log_rate; --layer) {
+    ntt_t_layer_kernel<<<(unsigned)((pairs + 255) / 256), 256, 0, s>>>(y, log_d, (uint32_t)layer, tw);
+    LAUNCH_OK();
+  }
   uint64_t n = 1ull << ln;
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, (uint64_t)sm_count() * 8));
-  lg_induced_basis_kernel<<<blocks, 256, 0, s>>>(lo_tab, hi_tab, n_q, ln, lo_bits, f, basis, part);
+  lg_induced_fold_kernel<<<blocks, 256, 0, s>>>(y, ln, log_rate, f, basis, part);
   LAUNCH_OK();
   return blocks;
 }

@@ -16,6 +16,7 @@
 #pragma once
 #include "field.h"
 #include "transcript.h"
+#include "parallel.h"
 #include "proof.h"
 #include "setup.h"
 #include <thread>
@@ -241,21 +242,28 @@ inline FrobeniusAssistProof prove_anchor_assist(Transcript& T, const std::vector
     size_t R = a.w.size();
     s.sfx.assign(L + 1, std::vector<std::array<F128, 4>>(R));
     for (size_t r = 0; r < R; ++r) { s.sfx[L][r] = {F128(), F128(), F128(), F128()}; s.sfx[L][r][BP_SUCCESS] = F128::one(); }
-    for (int l = L - 1; l >= 0; --l) {
-      F128 Mc[4][4][4];
-      for (int cd = 0; cd < 4; ++cd) bp_layer_matrix(s.eq4[l].data(), cd & 1, (cd >> 1) & 1, Mc[cd]);
-      for (size_t r = 0; r < R; ++r) {
+    std::vector<std::array<std::array<std::array<F128, 4>, 4>, 4>> Mc(L);
+    for (int l = 0; l < L; ++l)
+      for (int cd = 0; cd < 4; ++cd) {
+        F128 M[4][4];
+        bp_layer_matrix(s.eq4[l].data(), cd & 1, (cd >> 1) & 1, M);
+        for (int st = 0; st < 4; ++st)
+          for (int o = 0; o < 4; ++o) Mc[l][cd][st][o] = M[st][o];
+      }
+    parallel_for(R, [&](size_t r) {
+      for (int l = L - 1; l >= 0; --l) {
         int c = (int)((a.t[r].first >> l) & 1), d = (int)((a.t[r].second >> l) & 1);
-        auto& nx = s.sfx[l + 1][r];
+        const auto& nx = s.sfx[l + 1][r];
+        const auto& M = Mc[l][c + 2 * d];
         std::array<F128, 4> out{};
         for (int st = 0; st < 4; ++st) {
           F128 acc;
-          for (int o = 0; o < 4; ++o) acc += Mc[c + 2 * d][st][o] * nx[o];
+          for (int o = 0; o < 4; ++o) acc += M[st][o] * nx[o];
           out[st] = acc;
         }
         s.sfx[l][r] = out;
       }
-    }
+    });
     s.part = a.w;
     s.prefix = {F128(), F128(), F128(), F128()};
     s.prefix[BP_INITIAL] = F128::one();
@@ -399,12 +407,12 @@ inline MultipointTwistedProof prove_multipoint(Transcript& T, const AlignedJagge
     return prefix_product_sum(f, J.used);
   };
   pf.values.assign(R, std::vector<F128>(128));
-  for (size_t i = 0; i < R; ++i)
-    for (int j = 0; j < 128; ++j) {
-      F128 rowp = F128::one();
-      for (uint32_t t = 0; t < n; ++t) rowp = rowp * (F128::one() + claims[i].z_row[t] + rp[j][t]);
-      pf.values[i][j] = rowp * col_pps(claims[i].z_col, rp[j], n);
-    }
+  parallel_for(R * 128, [&](size_t ij) {
+    size_t i = ij / 128, j = ij % 128;
+    F128 rowp = F128::one();
+    for (uint32_t t = 0; t < n; ++t) rowp = rowp * (F128::one() + claims[i].z_row[t] + rp[j][t]);
+    pf.values[i][j] = rowp * col_pps(claims[i].z_col, rp[j], n);
+  });
   T.observe_label("flock-multipoint-twisted-v1");
   for (auto& vs : pf.values) for (auto& v : vs) T.observe_f128(v);
   uint32_t gamma_bits = std::max<uint32_t>(1, grinding_bits_for_degree(128 * R - 1));
@@ -417,30 +425,32 @@ inline MultipointTwistedProof prove_multipoint(Transcript& T, const AlignedJagge
   // ---- closed-form two-product sumcheck
   // coef_ij = gamma^(128 i + j); prefix products over bound bits; row suffix products.
   std::vector<std::vector<F128>> P(R, std::vector<F128>(128)), rowsuf(R, std::vector<F128>(128 * (n + 1)));
-  for (size_t i = 0; i < R; ++i)
-    for (int j = 0; j < 128; ++j) {
-      P[i][j] = gpow[128 * i + j];
-      F128* sf = &rowsuf[i][j * (n + 1)];
-      sf[n] = F128::one();
-      for (int t = (int)n - 1; t >= 0; --t) sf[t] = sf[t + 1] * (F128::one() + claims[i].z_row[t] + rp[j][t]);
-    }
   std::vector<std::vector<F128>> Ccol(R, std::vector<F128>(128));
-  for (size_t i = 0; i < R; ++i)
-    for (int j = 0; j < 128; ++j) Ccol[i][j] = col_pps(claims[i].z_col, rp[j], n);
+  parallel_for(R * 128, [&](size_t ij) {
+    size_t i = ij / 128, j = ij % 128;
+    P[i][j] = gpow[128 * i + j];
+    F128* sf = &rowsuf[i][j * (n + 1)];
+    sf[n] = F128::one();
+    for (int t = (int)n - 1; t >= 0; --t) sf[t] = sf[t + 1] * (F128::one() + claims[i].z_row[t] + rp[j][t]);
+    Ccol[i][j] = col_pps(claims[i].z_col, rp[j], n);
+  });
   std::vector<F128> s;  // bound challenges
+  std::vector<F128> c1v(R * 128), civ(R * 128);
   auto message = [&](uint32_t t, F128& g1, F128& gi) {
     g1 = F128(); gi = F128();
     if (t < n) {
-      for (size_t i = 0; i < R; ++i)
-        for (int j = 0; j < 128; ++j) {
-          F128 c = P[i][j] * rowsuf[i][j * (n + 1) + t + 1] * Ccol[i][j];
-          g1 += c * claims[i].z_row[t] * rp[j][t];
-          gi += c;
-        }
+      parallel_for(R * 128, [&](size_t ij) {
+        size_t i = ij / 128, j = ij % 128;
+        F128 c = P[i][j] * rowsuf[i][j * (n + 1) + t + 1] * Ccol[i][j];
+        c1v[ij] = c * claims[i].z_row[t] * rp[j][t];
+        civ[ij] = c;
+      });
+      for (size_t ij = 0; ij < R * 128; ++ij) { g1 += c1v[ij]; gi += civ[ij]; }
     } else {
       uint32_t b = t - n;
-      for (size_t i = 0; i < R; ++i)
-        for (int j = 0; j < 128; ++j) {
+      parallel_for(R * 128, [&](size_t ij) {
+        size_t i = ij / 128, j = ij % 128;
+        {
           // column weights: u < b bound to s, u = b the round variable, u > b summed against rho_j
           std::vector<std::pair<F128, F128>> f0(k), f1(k);
           for (uint32_t u = 0; u < k; ++u) {
@@ -453,9 +463,11 @@ inline MultipointTwistedProof prove_multipoint(Transcript& T, const AlignedJagge
           }
           F128 l20 = prefix_product_sum(f0, J.used), l21 = prefix_product_sum(f1, J.used);
           F128 c = P[i][j];  // row factors and bound column factors of g already folded in
-          g1 += c * rp[j][n + b] * l21;
-          gi += c * (l20 + l21);
+          c1v[ij] = c * rp[j][n + b] * l21;
+          civ[ij] = c * (l20 + l21);
         }
+      });
+      for (size_t ij = 0; ij < R * 128; ++ij) { g1 += c1v[ij]; gi += civ[ij]; }
     }
   };
   F128 g1, gi;
@@ -469,21 +481,23 @@ inline MultipointTwistedProof prove_multipoint(Transcript& T, const AlignedJagge
     s.push_back(r);
     if (t + 1 == m) break;
     // absorb the bound variable into the prefix products
-    for (size_t i = 0; i < R; ++i)
-      for (int j = 0; j < 128; ++j) {
-        F128 f = F128::one() + rp[j][t] + r;  // eq(rho_j[t], r)
-        if (t < n) f = f * (F128::one() + claims[i].z_row[t] + r);
-        P[i][j] = P[i][j] * f;
-      }
+    parallel_for(R * 128, [&](size_t ij) {
+      size_t i = ij / 128, j = ij % 128;
+      F128 f = F128::one() + rp[j][t] + r;  // eq(rho_j[t], r)
+      if (t < n) f = f * (F128::one() + claims[i].z_row[t] + r);
+      P[i][j] = P[i][j] * f;
+    });
     message(t + 1, g1, gi);
   }
   // ---- anchor at the endpoint rho'' = s
   F128 g_at;
-  for (int j = 0; j < 128; ++j) {
+  std::vector<F128> gj(128);
+  parallel_for(128, [&](size_t j) {
     F128 prod = gpow[j];
     for (uint32_t t = 0; t < m; ++t) prod = prod * (s[t] * rp[j][t] + (F128::one() + s[t]) * (F128::one() + rp[j][t]));
-    g_at += prod;
-  }
+    gj[j] = prod;
+  });
+  for (int j = 0; j < 128; ++j) g_at += gj[j];
   std::vector<AssistStatement> sts;
   for (size_t i = 0; i < R; ++i) sts.push_back(aligned_statement(J, claims[i].z_row, claims[i].z_col, gpow[128 * i] * g_at));
   pf.anchor = prove_anchor_assist(T, sts, s, m, anchor_round_bits);

@@ -81,9 +81,15 @@ class ProverBackend {
                          uint32_t cap_depth, std::vector<Hash>& cap) = 0;
   // Introduce a pending basis (eq(z), base values) : returns (message, answer).
   virtual Msg256 lg_introduce_eq(const std::vector<F128>& z, F128& answer) = 0;
-  // Introduce the induced basis of `queries` (weights w_i, point images what[q][k]) split.
-  virtual Msg256 lg_introduce_induced(uint32_t log_msg_cols, const std::vector<F128>& w,
-                                      const std::vector<std::vector<F128>>& what) = 0;
+  // Introduce the induced basis of the queried positions (weights w_i) split:
+  //   basis[i] = sum_q w_q prod_{k in bits(i)} W_k(pos_q),
+  // what[q][k] = W_k(pos_q) (normalised LCH basis factors). The codeword of that level is
+  // the NTT (from layer log_rate) of the replicated message, so basis = NTT^T(sum_q w_q e_pos_q)
+  // folded over the replicas: a backend may use the positions instead of `what`, in which
+  // case induced_from_positions() is true and `what` is passed empty.
+  virtual Msg256 lg_introduce_induced(uint32_t log_msg_cols, uint32_t log_rate, const std::vector<uint64_t>& positions,
+                                      const std::vector<F128>& w, const std::vector<std::vector<F128>>& what) = 0;
+  virtual bool induced_from_positions() const { return false; }
   virtual void lg_glue(F128 beta) = 0;
   // Rows of level `level` (0 = the L0 commit) at positions, and capped paths.
   virtual void lg_open(uint32_t level, const std::vector<uint64_t>& positions, uint32_t cap_depth,
@@ -412,13 +418,17 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
       }
     return q;
   };
-  auto induce = [&](uint32_t log_msg_cols, const std::vector<uint64_t>& q, const std::vector<F128>& alpha) {
+  auto induce = [&](uint32_t log_msg_cols, uint32_t log_rate, const std::vector<uint64_t>& q,
+                    const std::vector<F128>& alpha) {
     auto rw = build_eq(alpha);
     std::vector<F128> w(rw.begin(), rw.begin() + q.size());
-    std::vector<std::vector<F128>> what(q.size());
-    LchSks sk = lch_sks(log_msg_cols);
-    for (size_t i = 0; i < q.size(); ++i) what[i] = lch_basis_factors(q[i], log_msg_cols, sk);
-    return B.lg_introduce_induced(log_msg_cols, w, what);
+    std::vector<std::vector<F128>> what;
+    if (!B.induced_from_positions()) {
+      what.resize(q.size());
+      LchSks sk = lch_sks(log_msg_cols);
+      for (size_t i = 0; i < q.size(); ++i) what[i] = lch_basis_factors(q[i], log_msg_cols, sk);
+    }
+    return B.lg_introduce_induced(log_msg_cols, log_rate, q, w, what);
   };
   {
     uint64_t nonce;
@@ -427,7 +437,7 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
     auto pr = T.grind_pow_and_sample_f128_vec(P.consistency_bits[0], ceil_log2(P.queries[0]));
     lp.consistency_batch_grinding_nonces.push_back(pr.first);
     B.lg_open(0, q0, level_cap_depth(0), lp.initial_proof.opened_rows, lp.initial_proof.merkle_proof);
-    observe_msg(induce(n1, q0, pr.second));
+    observe_msg(induce(n1, P.log_inv_rates[0], q0, pr.second));
     auto pb2 = T.grind_pow_and_sample_f128(P.claim_bits[1]);
     lp.claim_batch_grinding_nonces.push_back(pb2.first);
     B.lg_glue(pb2.second);
@@ -479,7 +489,7 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
     RecursiveProof rp;
     B.lg_open(level, q, level_cap_depth(level), rp.opened_rows, rp.merkle_proof);
     lp.recursive_proofs.push_back(rp);
-    observe_msg(induce(ext_dim, q, pc.second));
+    observe_msg(induce(ext_dim, P.log_inv_rates[level], q, pc.second));
     auto pb3 = T.grind_pow_and_sample_f128(P.claim_bits[next_level]);
     lp.claim_batch_grinding_nonces.push_back(pb3.first);
     B.lg_glue(pb3.second);

@@ -471,7 +471,7 @@ class CpuBackend : public ProverBackend {
     for (size_t i = 0; i < e.size(); ++i) { answer += lf[i].c0 * e[i]; pending[i] = F256(e[i]); }
     return round_msg(lf, pending, 1);
   }
-  Msg256 lg_introduce_induced(uint32_t ln, const std::vector<F128>& w,
+  Msg256 lg_introduce_induced(uint32_t ln, uint32_t, const std::vector<uint64_t>&, const std::vector<F128>& w,
                               const std::vector<std::vector<F128>>& what) override {
     size_t n = size_t(1) << ln;
     std::vector<F128> basis(n), tmp(n);

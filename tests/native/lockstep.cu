@@ -135,8 +135,9 @@ struct Lockstep : ProverBackend {
     Msg256 a = C.lg_introduce_eq(z, ans), b = G.lg_introduce_eq(z, a2);
     check("lg intro_eq answer", ans, a2); check("lg intro_eq msg", a, b); return a;
   }
-  Msg256 lg_introduce_induced(uint32_t ln, const std::vector<F128>& w, const std::vector<std::vector<F128>>& wh) override {
-    Msg256 a = C.lg_introduce_induced(ln, w, wh), b = G.lg_introduce_induced(ln, w, wh);
+  Msg256 lg_introduce_induced(uint32_t ln, uint32_t lr, const std::vector<uint64_t>& pos, const std::vector<F128>& w,
+                              const std::vector<std::vector<F128>>& wh) override {
+    Msg256 a = C.lg_introduce_induced(ln, lr, pos, w, wh), b = G.lg_introduce_induced(ln, lr, pos, w, {});
     check("lg induced msg", a, b); return a;
   }
   void lg_glue(F128 b) override { C.lg_glue(b); G.lg_glue(b); }
