@@ -6,6 +6,8 @@
 // field elements.
 #include "backend.h"
 #include "../host/tables.h"
+#include <atomic>
+#include <thread>
 
 namespace flock {
 namespace gpu {
@@ -46,6 +48,17 @@ static T* dmalloc(size_t n, std::vector<void*>& owned) {
   CUDA_OK(cudaMalloc(&p, n * sizeof(T)));
   owned.push_back(p);
   return static_cast<T*>(p);
+}
+
+// Entries of the split eq tables of the skip fold (over L coordinates) and of every
+// later zerocheck fold round (over the suffixes of L - 1, L - 2, ..., 0 coordinates).
+static uint64_t zc_tables_entries(uint32_t L) {
+  uint64_t total = (uint64_t(1) << 10) + (uint64_t(1) << (L - 10));
+  for (uint32_t i = 0; i < L; ++i) {
+    uint32_t n = L - 1 - i, lo = std::min(n, 10u);
+    total += (uint64_t(1) << lo) + (uint64_t(1) << (n - lo));
+  }
+  return total;
 }
 
 GpuBackend::GpuBackend(const Statement& s) : S(s) {
@@ -110,6 +123,13 @@ GpuBackend::GpuBackend(const Statement& s) : S(s) {
   stage_cap_ = size_t(8) << 20;
   d_stage_ = dmalloc<uint8_t>(stage_cap_, owned_);
   CUDA_OK(cudaMallocHost(&h_stage_, stage_cap_));
+  CUDA_OK(cudaHostAlloc(&h_pub_, 64 * sizeof(F128d), cudaHostAllocMapped));
+  CUDA_OK(cudaHostGetDevicePointer(&d_pub_, h_pub_, 0));
+  CUDA_OK(cudaHostAlloc(&h_flag_, 64, cudaHostAllocMapped));
+  CUDA_OK(cudaHostGetDevicePointer(&d_flag_, h_flag_, 0));
+  *(volatile uint32_t*)h_flag_ = 0;
+  zc_tabs_cap_ = zc_tables_entries(S.m - 7);
+  zc_tabs_ = dmalloc<F128d>(zc_tabs_cap_, owned_);
   CUDA_OK(cudaStreamCreateWithFlags(&pow_st_, cudaStreamNonBlocking));
   d_pow_ = dmalloc<unsigned long long>(1, owned_);
   CUDA_OK(cudaMallocHost(&h_pow_, sizeof(unsigned long long)));
@@ -129,6 +149,8 @@ GpuBackend::~GpuBackend() {
   cudaFreeHost(h_red_);
   cudaFreeHost(h_stage_);
   cudaFreeHost(h_pow_);
+  cudaFreeHost(h_pub_);
+  cudaFreeHost(h_flag_);
   cudaStreamDestroy(pow_st_);
   cudaStreamDestroy(st_);
 }
@@ -243,8 +265,37 @@ void GpuBackend::sync() {
 }
 std::vector<F128> GpuBackend::reduce(uint32_t n_blocks, uint32_t width) {
   if ((uint64_t)n_blocks * width > part_cap_) throw std::runtime_error("partials buffer too small");
-  launch_reduce_parts(part_, n_blocks, width, red_, st_);
-  return fetch(red_, width);
+  if (width > 64) {
+    launch_reduce_parts(part_, n_blocks, width, red_, st_);
+    return fetch(red_, width);
+  }
+  // round messages: one block reduces and publishes into mapped host memory
+  uint32_t seq = ++seq_;
+  launch_reduce_publish(part_, n_blocks, width, d_pub_, d_flag_, seq, st_);
+  wait_published(seq);
+  std::vector<F128> out(width);
+  const volatile F128d* p = h_pub_;
+  for (uint32_t j = 0; j < width; ++j) out[j] = F128(p[j].lo, p[j].hi);
+  d2h_ += width * sizeof(F128d) + sizeof(uint32_t);
+  return out;
+}
+// Spin on the published sequence number (the stream keeps running; no synchronisation).
+// A stalled stream is reported after 20 s.
+void GpuBackend::wait_published(uint32_t seq) {
+  const volatile uint32_t* f = h_flag_;
+  uint64_t spins = 0;
+  double t0 = 0;
+  while (*f != seq) {
+    if ((++spins & 0xFFFF) == 0) {
+      double t = now_ms();
+      if (t0 == 0) t0 = t;
+      else if (t - t0 > 20000) throw std::runtime_error("device reduction did not publish within 20 s");
+      cudaError_t e = cudaStreamQuery(st_);
+      if (e != cudaSuccess && e != cudaErrorNotReady) CUDA_OK(e);
+      std::this_thread::yield();
+    }
+  }
+  std::atomic_thread_fence(std::memory_order_acquire);
 }
 std::vector<F128> GpuBackend::fetch(const F128d* d, size_t n) {
   std::vector<F128> out(n);
@@ -265,6 +316,19 @@ GpuBackend::EqSplit GpuBackend::eq_split(const std::vector<F128>& point, F128 sc
   e.lo_bits = std::min(n, max_lo);
   uint32_t hi_bits = n - e.lo_bits;
   const F128d* dp = upload(point);
+  F128d* lo = static_cast<F128d*>(scratch((size_t(16)) << e.lo_bits));
+  F128d* hi = static_cast<F128d*>(scratch((size_t(16)) << hi_bits));
+  launch_eq_table(dp, e.lo_bits, dev(F128::one()), lo, st_);
+  launch_eq_table(dp + e.lo_bits, hi_bits, dev(scale), hi, st_);
+  e.lo = lo;
+  e.hi = hi;
+  return e;
+}
+
+GpuBackend::EqSplit GpuBackend::eq_split_dev(const F128d* dp, uint32_t n, F128 scale, uint32_t max_lo) {
+  EqSplit e;
+  e.lo_bits = std::min(n, max_lo);
+  uint32_t hi_bits = n - e.lo_bits;
   F128d* lo = static_cast<F128d*>(scratch((size_t(16)) << e.lo_bits));
   F128d* hi = static_cast<F128d*>(scratch((size_t(16)) << hi_bits));
   launch_eq_table(dp, e.lo_bits, dev(F128::one()), lo, st_);
@@ -309,7 +373,7 @@ void GpuBackend::zc_round1(const std::vector<F128>& r, std::vector<F128>& ab, st
                            std::vector<F128>& svc) {
   scr_off_ = 0;
   const uint32_t m = S.m;
-  auto fixed = zc_fixed_challenges();
+  const auto& fixed = zc_fixed_challenges();
   for (int i = 0; i < 7; ++i)
     if (r[6 + i] != fixed[i]) throw std::runtime_error("zerocheck round 1 expects the fixed challenges at r[6..13)");
   std::vector<F128> outer(r.begin() + 13, r.end());
@@ -321,8 +385,11 @@ void GpuBackend::zc_round1(const std::vector<F128>& r, std::vector<F128>& ab, st
   }
   auto v = reduce(nb, 192);
   // D = prod (1 + g_i)^-1 over the medium constants' g_i = x^1, x^2, x^4, x^8
-  F128 D = F128::one();
-  for (int e : {1, 2, 4, 8}) D = D * inv(F128::one() + F128(1ull << e, 0));
+  static const F128 D = [] {
+    F128 d = F128::one();
+    for (int e : {1, 2, 4, 8}) d = d * inv(F128::one() + F128(1ull << e, 0));
+    return d;
+  }();
   ab.assign(64, F128());
   svc.assign(128, F128());
   for (int i = 0; i < 64; ++i) ab[i] = D * v[i];
@@ -353,13 +420,37 @@ void GpuBackend::zc_round1(const std::vector<F128>& r, std::vector<F128>& ab, st
 
 void GpuBackend::zc_fold_skip(const std::vector<F128>& w, const std::vector<F128>& eq_point, F128& g1, F128& gi) {
   scr_off_ = 0;
+  const uint32_t L = (uint32_t)eq_point.size();  // m - 7
+  if (L < 10) throw std::runtime_error("zerocheck skip fold needs m >= 17");
   const F128d* dw = upload(w);
-  EqSplit e = eq_split(eq_point, F128::one(), 10);
-  if (e.lo_bits != 10) throw std::runtime_error("zerocheck skip fold needs m >= 17");
+  const F128d* dp = upload(eq_point);
+  // Every later fold round i uses eq over the suffix eq_point[1 + i ..]: build all the
+  // split tables now, in one launch.
+  zc_desc_.clear();
+  uint64_t total = 0;
+  auto add = [&](uint32_t off, uint32_t n) {
+    EqDesc d;
+    d.p_off = off;
+    d.n = n;
+    d.out_off = total;
+    d.scale = dev(F128::one());
+    zc_desc_.push_back(d);
+    total += uint64_t(1) << n;
+  };
+  add(0, 10);
+  add(10, L - 10);
+  for (uint32_t i = 0; i < L; ++i) {  // round i: eq over eq_point[1 + i ..), L - 1 - i coordinates
+    uint32_t n = L - 1 - i, lo = std::min(n, 10u);
+    add(1 + i, lo);
+    add(1 + i + lo, n - lo);
+  }
+  if (total != zc_tables_entries(L)) throw std::runtime_error("zerocheck eq tables: size mismatch");
+  const EqDesc* ddesc = static_cast<const EqDesc*>(upload(zc_desc_.data(), zc_desc_.size() * sizeof(EqDesc)));
   uint32_t nb;
   {
     Mark mk(this, ST_ZC_FOLD_SKIP);
-    nb = launch_zc_fold_skip(a_, b_, dw, W_, e.lo, e.lo_bits, e.hi, zc1a_, zc1b_, part_, st_);
+    launch_eq_tables(dp, ddesc, (uint32_t)zc_desc_.size(), total, zc_tabs_, st_);
+    nb = launch_zc_fold_skip(a_, b_, dw, W_, zc_tabs_, 10, zc_tabs_ + zc_desc_[1].out_off, zc1a_, zc1b_, part_, st_);
   }
   auto v = reduce(nb, 2);
   g1 = v[0];
@@ -367,19 +458,24 @@ void GpuBackend::zc_fold_skip(const std::vector<F128>& w, const std::vector<F128
   zc_cur_a_ = zc1a_;
   zc_cur_b_ = zc1b_;
   zc_len_ = 2 * W_;
+  zc_round_ = 0;
 }
 
 void GpuBackend::zc_fold(F128 rho, const std::vector<F128>& eq_point, F128& g1, F128& gi) {
-  scr_off_ = 0;
   uint64_t n_pairs = zc_len_ / 4;
   if ((uint64_t(1) << eq_point.size()) != n_pairs) throw std::runtime_error("zerocheck fold: eq size mismatch");
-  EqSplit e = eq_split(eq_point, F128::one(), 10);
+  size_t k = 2 + 2 * zc_round_;
+  if (k + 1 >= zc_desc_.size() || zc_desc_[k].n + zc_desc_[k + 1].n != eq_point.size())
+    throw std::runtime_error("zerocheck fold: round tables out of step");
+  const EqDesc& lo = zc_desc_[k];
+  const EqDesc& hi = zc_desc_[k + 1];
   F128d* oa = (zc_cur_a_ == zc1a_) ? zc2a_ : zc1a_;
   F128d* ob = (zc_cur_a_ == zc1a_) ? zc2b_ : zc1b_;
   uint32_t nb;
   {
     Mark mk(this, ST_ZC_FOLDS);
-    nb = launch_pair_fold(zc_cur_a_, zc_cur_b_, n_pairs, dev(rho), e.lo, e.lo_bits, e.hi, oa, ob, part_, true, st_);
+    nb = launch_pair_fold(zc_cur_a_, zc_cur_b_, n_pairs, dev(rho), nullptr, zc_tabs_ + lo.out_off, lo.n,
+                          zc_tabs_ + hi.out_off, oa, ob, part_, true, st_);
   }
   auto v = reduce(nb, 2);
   g1 = v[0];
@@ -387,6 +483,7 @@ void GpuBackend::zc_fold(F128 rho, const std::vector<F128>& eq_point, F128& g1, 
   zc_cur_a_ = oa;
   zc_cur_b_ = ob;
   zc_len_ /= 2;
+  zc_round_++;
 }
 
 void GpuBackend::zc_final(F128 rho, F128& ae, F128& be) {
@@ -476,10 +573,8 @@ void GpuBackend::lc_s_hat_v(const std::vector<F128>& tail, std::vector<F128>& ou
 }
 
 // ------------------------------------------------------------------ merged open
-void GpuBackend::mo_build_w(const std::vector<WeightClaim>& cl, uint32_t nu, uint64_t area, F128& u0, F128& u2) {
-  scr_off_ = 0;
+uint32_t GpuBackend::launch_build_w(const std::vector<WeightClaim>& cl, uint32_t nu, uint64_t area) {
   if (cl.size() != 2) throw std::runtime_error("merged open expects the AB and C claims");
-  Mark mk(this, ST_MO_BUILD_W);
   F128d* er[2];
   F128d* ec[2];
   for (int i = 0; i < 2; ++i) {
@@ -493,7 +588,16 @@ void GpuBackend::mo_build_w(const std::vector<WeightClaim>& cl, uint32_t nu, uin
   std::vector<F128> tabs(cl[0].table);
   tabs.insert(tabs.end(), cl[1].table.begin(), cl[1].table.end());
   const F128d* dt = upload(tabs);
-  uint32_t nb = launch_mo_build_w(z_, er[0], ec[0], er[1], ec[1], dt, nu, area, W_, mw_, part_, st_);
+  return launch_mo_build_w(z_, er[0], ec[0], er[1], ec[1], dt, nu, area, W_, mw_, part_, st_);
+}
+
+void GpuBackend::mo_build_w(const std::vector<WeightClaim>& cl, uint32_t nu, uint64_t area, F128& u0, F128& u2) {
+  scr_off_ = 0;
+  uint32_t nb;
+  {
+    Mark mk(this, ST_MO_BUILD_W);
+    nb = launch_build_w(cl, nu, area);
+  }
   auto v = reduce(nb, 2);
   u0 = v[0];
   u2 = v[1];
@@ -516,7 +620,7 @@ void GpuBackend::mo_round(F128 r, bool last, F128& g1, F128& gi) {
   uint32_t nb;
   {
     Mark mk(this, ST_MO_ROUNDS);
-    nb = launch_pair_fold(mo_q_, mo_w_, n_pairs, dev(r), nullptr, chunk_bits, nullptr, oq, ow, part_, !last, st_);
+    nb = launch_pair_fold(mo_q_, mo_w_, n_pairs, dev(r), nullptr, nullptr, chunk_bits, nullptr, oq, ow, part_, !last, st_);
   }
   mo_q_ = oq;
   mo_w_ = ow;
@@ -584,12 +688,12 @@ void GpuBackend::lg_fold(F256 r, size_t d) {
   uint64_t n_out = lg_n_ / 2;
   Mark mk(this, ST_LIGERITO);
   if (lg_base_) {
-    launch_lg_fold128(z_, lb128_, n_out, dev(r), d, lf_[0], lb_[0], st_);
+    launch_lg_fold128(z_, lb128_, n_out, dev(r), nullptr, d, lf_[0], lb_[0], st_);
     lg_cur_ = 0;
     lg_base_ = false;
   } else {
     int nx = lg_cur_ ^ 1;
-    launch_lg_fold256(lf_[lg_cur_], lb_[lg_cur_], n_out, dev(r), d, lf_[nx], lb_[nx], st_);
+    launch_lg_fold256(lf_[lg_cur_], lb_[lg_cur_], n_out, dev(r), nullptr, d, lf_[nx], lb_[nx], st_);
     lg_cur_ = nx;
   }
   lg_n_ = n_out;

@@ -52,7 +52,6 @@ class GpuBackend : public ProverBackend {
   // Proof-of-work searches of 6 or more bits run on the device (own stream, thread-safe:
   // the forked multipoint transcript grinds concurrently with the main one).
   PowSearchFn pow_search() override;
-
   // Device-time breakdown of a prove (CUDA events on the backend's stream).
   enum Stage {
     ST_WITNESS, ST_L0_FILL, ST_L0_NTT, ST_L0_MERKLE, ST_ZC_ROUND1, ST_ZC_FOLD_SKIP, ST_ZC_FOLDS, ST_LINCHECK,
@@ -95,6 +94,9 @@ class GpuBackend : public ProverBackend {
   std::vector<F128> reduce(uint32_t n_blocks, uint32_t width);
   std::vector<F128> fetch(const F128d* d, size_t n);
   EqSplit eq_split(const std::vector<F128>& point, F128 scale, uint32_t max_lo);
+  EqSplit eq_split_dev(const F128d* d_point, uint32_t n, F128 scale, uint32_t max_lo);
+  // build the merged-open weight and launch its round-0 reduction (per-block partials)
+  uint32_t launch_build_w(const std::vector<WeightClaim>& cl, uint32_t nu, uint64_t area);
   const F128d* twiddles(uint32_t log_d);
   std::vector<Hash> read_cap(const uint8_t* tree, uint64_t n_leaves, uint32_t cap_depth);
 
@@ -135,6 +137,7 @@ class GpuBackend : public ProverBackend {
   F128d *zc1a_ = nullptr, *zc1b_ = nullptr, *zc2a_ = nullptr, *zc2b_ = nullptr;
   F128d *zc_cur_a_ = nullptr, *zc_cur_b_ = nullptr;
   uint64_t zc_len_ = 0;
+  uint32_t zc_round_ = 0;
 
   F128d *eqi_ = nullptr, *ca_ = nullptr, *cb_ = nullptr, *comb_ = nullptr, *zv_ = nullptr, *zvcap_ = nullptr;
   uint32_t *cola_ = nullptr, *rowa_ = nullptr, *colb_ = nullptr, *rowb_ = nullptr;
@@ -156,6 +159,18 @@ class GpuBackend : public ProverBackend {
   bool pend_induced_ = false;
   uint64_t pend_n_ = 0;
   std::vector<Level> levels_;
+
+  // mapped pinned memory the message reductions publish into
+  F128d* h_pub_ = nullptr;
+  F128d* d_pub_ = nullptr;
+  uint32_t* h_flag_ = nullptr;
+  uint32_t* d_flag_ = nullptr;
+  uint32_t seq_ = 0;
+  void wait_published(uint32_t seq);
+  // eq tables of every zerocheck fold round, built once from the skip-fold point
+  F128d* zc_tabs_ = nullptr;
+  uint64_t zc_tabs_cap_ = 0;
+  std::vector<EqDesc> zc_desc_;
 
   std::mutex pow_mu_;
   cudaStream_t pow_st_ = nullptr;

@@ -174,10 +174,11 @@ int flock_gb300_last_transfer_bytes(const flock_gb300_setup* setup, uint64_t* h2
 
 uint64_t flock_gb300_launch_count(void) { return gpu::launch_count(); }
 
-int flock_gb300_last_phase_ms(const flock_gb300_setup* setup, double out[6]) {
+int flock_gb300_last_phase_ms(const flock_gb300_setup* setup, double out[8]) {
   if (!setup || !out) return fail(FLOCK_GB300_EINVAL, "null argument");
   const ProveTimings& t = setup->last;
   out[0] = t.witness; out[1] = t.commit; out[2] = t.zerocheck; out[3] = t.lincheck; out[4] = t.open; out[5] = t.total;
+  out[6] = t.assist; out[7] = t.assist_wait;
   return FLOCK_GB300_OK;
 }
 

@@ -22,12 +22,12 @@ struct __align__(16) F256d {
   F128d c0, c1;
 };
 
-__device__ __forceinline__ F128d f128(uint64_t lo, uint64_t hi) { F128d r; r.lo = lo; r.hi = hi; return r; }
-__device__ __forceinline__ F128d f128_zero() { return f128(0, 0); }
-__device__ __forceinline__ F128d f128_one() { return f128(1, 0); }
-__device__ __forceinline__ F128d operator+(F128d a, F128d b) { return f128(a.lo ^ b.lo, a.hi ^ b.hi); }
-__device__ __forceinline__ F128d& operator+=(F128d& a, F128d b) { a.lo ^= b.lo; a.hi ^= b.hi; return a; }
-__device__ __forceinline__ bool is_zero(F128d a) { return (a.lo | a.hi) == 0; }
+__host__ __device__ __forceinline__ F128d f128(uint64_t lo, uint64_t hi) { F128d r; r.lo = lo; r.hi = hi; return r; }
+__host__ __device__ __forceinline__ F128d f128_zero() { return f128(0, 0); }
+__host__ __device__ __forceinline__ F128d f128_one() { return f128(1, 0); }
+__host__ __device__ __forceinline__ F128d operator+(F128d a, F128d b) { return f128(a.lo ^ b.lo, a.hi ^ b.hi); }
+__host__ __device__ __forceinline__ F128d& operator+=(F128d& a, F128d b) { a.lo ^= b.lo; a.hi ^= b.hi; return a; }
+__host__ __device__ __forceinline__ bool is_zero(F128d a) { return (a.lo | a.hi) == 0; }
 
 __device__ __forceinline__ uint64_t mulw(uint32_t a, uint32_t b) { return (uint64_t)a * (uint64_t)b; }
 
@@ -82,10 +82,10 @@ __device__ __forceinline__ F128d mul_by_x_inv(F128d z) {
 }
 
 // ---- F256
-__device__ __forceinline__ F256d f256(F128d a, F128d b) { F256d r; r.c0 = a; r.c1 = b; return r; }
-__device__ __forceinline__ F256d f256_base(F128d a) { return f256(a, f128_zero()); }
-__device__ __forceinline__ F256d operator+(F256d a, F256d b) { return f256(a.c0 + b.c0, a.c1 + b.c1); }
-__device__ __forceinline__ F256d& operator+=(F256d& a, F256d b) { a.c0 += b.c0; a.c1 += b.c1; return a; }
+__host__ __device__ __forceinline__ F256d f256(F128d a, F128d b) { F256d r; r.c0 = a; r.c1 = b; return r; }
+__host__ __device__ __forceinline__ F256d f256_base(F128d a) { return f256(a, f128_zero()); }
+__host__ __device__ __forceinline__ F256d operator+(F256d a, F256d b) { return f256(a.c0 + b.c0, a.c1 + b.c1); }
+__host__ __device__ __forceinline__ F256d& operator+=(F256d& a, F256d b) { a.c0 += b.c0; a.c1 += b.c1; return a; }
 __device__ __forceinline__ F256d operator*(F256d a, F256d b) {
   F128d p0 = a.c0 * b.c0, p1 = a.c1 * b.c1, p2 = (a.c0 + a.c1) * (b.c0 + b.c1);
   return f256(p0 + mul_by_x_inv(p1), p2 + p0);

@@ -59,9 +59,10 @@ uint32_t launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32
 uint32_t launch_zc_fold_skip(const F128d* a, const F128d* b, const F128d* w64, uint64_t n_words, const F128d* eq_lo,
                              uint32_t lo_bits, const F128d* eq_hi, F128d* amlv, F128d* bmlv, F128d* part,
                              cudaStream_t s);                                                          // width 2
-uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, F128d r, const F128d* eq_lo,
-                          uint32_t lo_bits, const F128d* eq_hi, F128d* aout, F128d* bout, F128d* part, bool msg,
-                          cudaStream_t s);                                                             // width 2
+// r_dev (when not null) is the device address of the challenge, read by the kernel.
+uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, F128d r, const F128d* r_dev,
+                          const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* aout, F128d* bout,
+                          F128d* part, bool msg, cudaStream_t s);                                      // width 2
 
 void launch_lc_eq_inner(const F128d* w64, const F128d* er, uint32_t K, F128d* eqi, cudaStream_t s);
 void launch_csc_fold(const uint32_t* col_ptr, const uint32_t* rows, uint32_t K, const F128d* eqi, F128d* out,
@@ -85,10 +86,10 @@ uint32_t launch_lg_dot_eq(const F128d* f, uint32_t stride, const F128d* eq_lo, u
                           uint64_t n, F128d* part, cudaStream_t s);                                    // width 1
 uint32_t launch_lg_message128(const F128d* f, const F128d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s);
 uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s);
-void launch_lg_fold128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, uint64_t d, F256d* fo, F256d* bo,
-                       cudaStream_t s);
-void launch_lg_fold256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, uint64_t d, F256d* fo, F256d* bo,
-                       cudaStream_t s);
+void launch_lg_fold128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, const F256d* r_dev, uint64_t d,
+                       F256d* fo, F256d* bo, cudaStream_t s);
+void launch_lg_fold256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, const F256d* r_dev, uint64_t d,
+                       F256d* fo, F256d* bo, cudaStream_t s);
 void launch_lg_code_switch(const F256d* f, const F256d* b, uint64_t n, F256d* fo, F256d* bo, cudaStream_t s);
 void launch_lg_replicate(const F256d* f, uint64_t msg, uint64_t total, F128d* mat, cudaStream_t s);
 uint32_t launch_lg_intro_eq(const F256d* f, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, uint64_t n,
@@ -97,6 +98,19 @@ uint32_t launch_lg_induced(const uint64_t* pos, const F128d* w, uint32_t n_q, ui
                            const F128d* tw, const F256d* f, F128d* y, F128d* basis, F128d* part,
                            cudaStream_t s);                                                            // width 2
 void launch_lg_glue(F256d* b, const F128d* p, F128d beta, uint64_t n, bool induced, cudaStream_t s);
+
+// rounds.cu
+// XOR-reduce width-wide partials with one block and publish the sums to mapped host
+// memory, then set *flag = seq (after a system-scope fence).
+void launch_reduce_publish(const F128d* part, uint32_t nb, uint32_t width, F128d* out_mapped, uint32_t* flag_mapped,
+                           uint32_t seq, cudaStream_t s);
+struct EqDesc {
+  uint32_t p_off, n;   // coordinates point[p_off .. p_off + n)
+  uint64_t out_off;    // first entry in the output (tables in increasing out_off)
+  F128d scale;
+};
+void launch_eq_tables(const F128d* point, const EqDesc* d_desc, uint32_t n_desc, uint64_t total, F128d* out,
+                      cudaStream_t s);
 
 }  // namespace gpu
 }  // namespace flock

@@ -297,9 +297,10 @@ uint32_t launch_zc_fold_skip(const F128d* a, const F128d* b, const F128d* w64, u
 // eq_lo == nullptr means eq = 1. n_pairs = output length / 2 (>= 1).
 __global__ void __launch_bounds__(256)
 pair_fold_kernel(const F128d* __restrict__ ain, const F128d* __restrict__ bin, uint64_t n_pairs, F128d r,
-                 const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F128d* __restrict__ eq_hi,
+                 const F128d* __restrict__ r_dev, const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F128d* __restrict__ eq_hi,
                  F128d* __restrict__ aout, F128d* __restrict__ bout, F128d* __restrict__ part, int msg) {
   __shared__ F128d sh[32];
+  if (r_dev) r = *r_dev;
   const uint64_t chunk = 1ull << lo_bits;
   const uint64_t n_chunks = (n_pairs + chunk - 1) / chunk;
   F128d G1 = f128_zero(), GI = f128_zero();
@@ -336,12 +337,13 @@ pair_fold_kernel(const F128d* __restrict__ ain, const F128d* __restrict__ bin, u
   }
   if (msg && threadIdx.x == 0) { part[blockIdx.x * 2] = G1; part[blockIdx.x * 2 + 1] = GI; }
 }
-uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, F128d r, const F128d* eq_lo,
-                          uint32_t lo_bits, const F128d* eq_hi, F128d* aout, F128d* bout, F128d* part, bool msg,
-                          cudaStream_t s) {
+uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, F128d r, const F128d* r_dev,
+                          const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* aout, F128d* bout,
+                          F128d* part, bool msg, cudaStream_t s) {
   uint64_t n_chunks = (n_pairs + (1ull << lo_bits) - 1) >> lo_bits;
   uint32_t blocks = (uint32_t)std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 8);
-  pair_fold_kernel<<<blocks, 256, 0, s>>>(ain, bin, n_pairs, r, eq_lo, lo_bits, eq_hi, aout, bout, part, msg ? 1 : 0);
+  pair_fold_kernel<<<blocks, 256, 0, s>>>(ain, bin, n_pairs, r, r_dev, eq_lo, lo_bits, eq_hi, aout, bout, part,
+                                          msg ? 1 : 0);
   LAUNCH_OK();
   return blocks;
 }
@@ -675,31 +677,35 @@ uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64
 }
 // o[i] = v[lo] + r (v[hi] + v[lo]), i = blk d + k, lo = 2 d blk + k.
 __global__ void lg_fold128_kernel(const F128d* __restrict__ f, const F128d* __restrict__ b, uint64_t n_out, F256d r,
-                                  uint64_t d, F256d* __restrict__ fo, F256d* __restrict__ bo) {
+                                  const F256d* __restrict__ r_dev, uint64_t d, F256d* __restrict__ fo,
+                                  F256d* __restrict__ bo) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_out) return;
+  if (r_dev) r = *r_dev;
   uint64_t blk = i / d, k = i - blk * d, lo = 2 * blk * d + k, hi = lo + d;
   F128d f0 = f[lo], df = f[hi] + f0, b0 = b[lo], db = b[hi] + b0;
   fo[i] = f256(f0 + r.c0 * df, r.c1 * df);
   bo[i] = f256(b0 + r.c0 * db, r.c1 * db);
 }
-void launch_lg_fold128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, uint64_t d, F256d* fo, F256d* bo,
-                       cudaStream_t s) {
-  lg_fold128_kernel<<<(unsigned)((n_out + 255) / 256), 256, 0, s>>>(f, b, n_out, r, d, fo, bo);
+void launch_lg_fold128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, const F256d* r_dev, uint64_t d,
+                       F256d* fo, F256d* bo, cudaStream_t s) {
+  lg_fold128_kernel<<<(unsigned)((n_out + 255) / 256), 256, 0, s>>>(f, b, n_out, r, r_dev, d, fo, bo);
   LAUNCH_OK();
 }
 __global__ void lg_fold256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n_out, F256d r,
-                                  uint64_t d, F256d* __restrict__ fo, F256d* __restrict__ bo) {
+                                  const F256d* __restrict__ r_dev, uint64_t d, F256d* __restrict__ fo,
+                                  F256d* __restrict__ bo) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_out) return;
+  if (r_dev) r = *r_dev;
   uint64_t blk = i / d, k = i - blk * d, lo = 2 * blk * d + k, hi = lo + d;
   F256d f0 = f[lo], b0 = b[lo];
   fo[i] = f0 + r * (f[hi] + f0);
   bo[i] = b0 + r * (b[hi] + b0);
 }
-void launch_lg_fold256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, uint64_t d, F256d* fo, F256d* bo,
-                       cudaStream_t s) {
-  lg_fold256_kernel<<<(unsigned)((n_out + 255) / 256), 256, 0, s>>>(f, b, n_out, r, d, fo, bo);
+void launch_lg_fold256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, const F256d* r_dev, uint64_t d,
+                       F256d* fo, F256d* bo, cudaStream_t s) {
+  lg_fold256_kernel<<<(unsigned)((n_out + 255) / 256), 256, 0, s>>>(f, b, n_out, r, r_dev, d, fo, bo);
   LAUNCH_OK();
 }
 // f' = (f.c0, f.c1) interleaved as base values; b' = (b, u b).

@@ -50,7 +50,19 @@ inline std::vector<F128> lagrange_weights64(F128 z, int offset) {
     return w;
   }
   F128 scale = zn * subspace_den6().second;
-  for (int i = 0; i < 64; ++i) w[i] = scale * inv(z + phi8((uint8_t)(offset + i)));
+  // batched inversion of the 64 differences: one field inversion and 3 * 63 products
+  F128 d[64], pre[64];
+  F128 run = F128::one();
+  for (int i = 0; i < 64; ++i) {
+    d[i] = z + phi8((uint8_t)(offset + i));
+    pre[i] = run;
+    run = run * d[i];
+  }
+  F128 inv_run = inv(run) * scale;
+  for (int i = 63; i >= 0; --i) {
+    w[i] = inv_run * pre[i];
+    inv_run = inv_run * d[i];
+  }
   return w;
 }
 inline F128 interpolate_on_lambda(const std::vector<F128>& vals, F128 z) {
@@ -121,11 +133,13 @@ inline std::vector<F128> linearized_coefficients(const std::vector<F128>& tab) {
   const auto& mi = moore_inverse();
   std::vector<F128> phi(128), c(128);
   for (int t = 0; t < 128; ++t) phi[t] = fold_one_slot(bit_basis(t), tab.data());
-  for (int j = 0; j < 128; ++j) {
-    F128 acc;
-    for (int t = 0; t < 128; ++t) acc += mi[j * 128 + t] * phi[t];
-    c[j] = acc;
-  }
+  parallel_for(16, [&](size_t blk) {
+    for (int j = 8 * (int)blk; j < 8 * (int)blk + 8; ++j) {
+      F128 acc;
+      for (int t = 0; t < 128; ++t) acc += mi[j * 128 + t] * phi[t];
+      c[j] = acc;
+    }
+  });
   return c;
 }
 

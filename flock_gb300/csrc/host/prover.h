@@ -98,10 +98,12 @@ class ProverBackend {
 
   // Device proof-of-work search (optional): smallest nonce with the PoW property.
   virtual PowSearchFn pow_search() { return {}; }
+
 };
 
 struct ProveTimings {
   double witness = 0, commit = 0, zerocheck = 0, lincheck = 0, open = 0, total = 0;
+  double assist = 0, assist_wait = 0;  // multipoint assist thread, and the open phase's wait for it
 };
 
 inline double now_ms() {
@@ -109,14 +111,17 @@ inline double now_ms() {
 }
 
 // Small constants of the zerocheck (univariate_skip_optimized.rs:70-125).
-inline std::vector<F128> zc_fixed_challenges() {
-  std::vector<F128> v;
-  const uint8_t small[3] = {0xF7, 0x53, 0xB5};
-  for (int i = 0; i < 3; ++i) v.push_back(phi8(small[i]));
-  for (int e : {1, 2, 4, 8}) {
-    F128 g(1ull << e, 0);
-    v.push_back(g * inv(F128::one() + g));
-  }
+inline const std::vector<F128>& zc_fixed_challenges() {
+  static const std::vector<F128> v = [] {
+    std::vector<F128> c;
+    const uint8_t small[3] = {0xF7, 0x53, 0xB5};
+    for (int i = 0; i < 3; ++i) c.push_back(phi8(small[i]));
+    for (int e : {1, 2, 4, 8}) {
+      F128 g(1ull << e, 0);
+      c.push_back(g * inv(F128::one() + g));
+    }
+    return c;
+  }();
   return v;
 }
 
@@ -197,7 +202,7 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
     auto pr = T.grind_pow_and_sample_f128_vec(bits_for(m), 6);
     zc.grinding_nonces.push_back(pr.first);
     for (int i = 0; i < 6; ++i) r[i] = pr.second[i];
-    auto fixed = zc_fixed_challenges();
+    const auto& fixed = zc_fixed_challenges();
     for (int i = 0; i < 7; ++i) r[6 + i] = fixed[i];
     auto ro = T.sample_f128_vec(m - 13);
     for (uint32_t i = 0; i < m - 13; ++i) r[13 + i] = ro[i];
@@ -214,10 +219,11 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
   }
   zc.final_c_eval = interpolate_on_lambda(zc.round1_c, zskip);
   std::vector<F128> mlv;
+  const std::vector<F128> skip_w = lagrange_weights64(zskip, 0);
   {
     std::vector<F128> eqp(r.begin() + 7, r.end());
     F128 g1, gi;
-    B.zc_fold_skip(lagrange_weights64(zskip, 0), eqp, g1, gi);
+    B.zc_fold_skip(skip_w, eqp, g1, gi);
     zc.multilinear_rounds.push_back({g1, gi});
     T.observe_f128(g1); T.observe_f128(gi);
     auto pr = T.grind_pow_and_sample_f128(2);
@@ -247,7 +253,7 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
   auto pa = T.grind_pow_and_sample_f128(1);
   lc.grinding_nonces.push_back(pa.first);
   F128 alpha = pa.second;
-  B.lc_comb(lagrange_weights64(zskip, 0), x_inner_rest);
+  B.lc_comb(skip_w, x_inner_rest);
   auto pb = T.grind_pow_and_sample_f128(1);
   lc.grinding_nonces.push_back(pb.first);
   F128 beta = pb.second;
@@ -315,10 +321,10 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
   wc[1].z_row.assign(x_c.begin() + 1, x_c.begin() + 1 + nu);
   wc[1].z_col.assign(x_c.begin() + 1 + nu, x_c.end());
   wc[1].table = rs_c.table;
-  F128 u0, u2;
-  B.mo_build_w(wc, nu, J.area(), u0, u2);
   std::vector<F128> rho;
   {
+    F128 u0, u2;
+    B.mo_build_w(wc, nu, J.area(), u0, u2);
     F128 g1 = target + u0, gi = u2;
     for (uint32_t rd = 0; rd < dense_log; ++rd) {
       T.observe_f128(g1); T.observe_f128(gi);
@@ -328,14 +334,19 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
       rho.push_back(pr.second);
       B.mo_round(pr.second, rd + 1 == dense_log, g1, gi);
     }
+    mo.q_eval = B.mo_q_eval();
   }
-  mo.q_eval = B.mo_q_eval();
   // Frobenius multipoint assist on a forked chain, concurrent with the inner open.
   std::vector<RsClaimPoint> fcl(2);
   fcl[0].z_row = wc[0].z_row; fcl[0].z_col = wc[0].z_col; fcl[0].coeffs = linearized_coefficients(rs_ab.table);
   fcl[1].z_row = wc[1].z_row; fcl[1].z_col = wc[1].z_col; fcl[1].coeffs = linearized_coefficients(rs_c.table);
   Transcript ch_a = T.fork("flock-par-assist-v1");
-  std::thread assist([&] { mo.frobenius = prove_multipoint(ch_a, J, fcl, rho, 2, 2); });
+  double assist_ms = 0;
+  std::thread assist([&] {
+    double a0 = now_ms();
+    mo.frobenius = prove_multipoint(ch_a, J, fcl, rho, 2, 2);
+    assist_ms = now_ms() - a0;
+  });
 
   // ---- inner open of q_hat(rho) = q_eval (packed-direct EqPoint claim)
   BatchOpeningProofLigerito& in = mo.inner;
@@ -371,10 +382,8 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
     B.lg_add_eq(pr.second, z);
   }
   observe_msg(B.lg_message(fold_block));
-  std::vector<F256> lane_ch;
   for (uint32_t j = 0; j < initial_k; ++j) {
     F256 ch = T.sample_f256();
-    lane_ch.push_back(ch);
     B.lg_fold(ch, fold_block);
     if (j + 1 < initial_k) observe_msg(B.lg_message(fold_block));
     else { B.lg_code_switch(); observe_msg(B.lg_message(1)); }
@@ -444,10 +453,8 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
   }
   for (uint32_t i = 0; i < P.r; ++i) {
     uint32_t k = P.recursive_ks[i];
-    std::vector<F256> level_ch;
     for (uint32_t j = 0; j < k; ++j) {
       F256 ch = T.sample_f256();
-      level_ch.push_back(ch);
       bool switching = (j + 1 == k) && (i + 1 != P.r);
       B.lg_fold(ch, 1);
       if (switching) { B.lg_code_switch(); observe_msg(B.lg_message(1)); }
@@ -494,7 +501,10 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
     lp.claim_batch_grinding_nonces.push_back(pb3.first);
     B.lg_glue(pb3.second);
   }
+  double w0 = now_ms();
   assist.join();
+  R.t.assist_wait = now_ms() - w0;
+  R.t.assist = assist_ms;
   T.merge_child(ch_a);
   double t5 = now_ms();
   R.t.witness = t1 - t0; R.t.commit = t2 - t1; R.t.zerocheck = t3 - t2; R.t.lincheck = t4 - t3;

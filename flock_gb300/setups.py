@@ -136,9 +136,10 @@ class _Setup:
         return ProofBundle.parse(self.prove_fast_bytes(inputs, domain))
 
     def last_phase_ms(self) -> dict:
-        v = (ctypes.c_double * 6)()
+        v = (ctypes.c_double * 8)()
         _native.check(self._lib.flock_gb300_last_phase_ms(self._h, v))
-        return dict(zip(("witness", "commit", "zerocheck", "lincheck", "open", "total"), list(v)))
+        return dict(zip(("witness", "commit", "zerocheck", "lincheck", "open", "total", "assist", "assist_wait"),
+                        list(v)))
 
 
 class Blake3Setup(_Setup):

@@ -97,8 +97,9 @@ int flock_gb300_last_transfer_bytes(const flock_gb300_setup* setup, uint64_t* h2
 uint64_t flock_gb300_launch_count(void);
 
 /* Host wall-clock milliseconds of the last prove on this setup:
- * [witness, commit, zerocheck, lincheck, open, total]. */
-int flock_gb300_last_phase_ms(const flock_gb300_setup* setup, double out[6]);
+ * [witness, commit, zerocheck, lincheck, open, total, multipoint assist (its own thread),
+ *  time the open phase waited for the assist]. */
+int flock_gb300_last_phase_ms(const flock_gb300_setup* setup, double out[8]);
 
 /* Releases a bundle returned by flock_gb300_prove_fast (cuda-ghash/prove_ffi.cu:417 flock_cuda_free). */
 void flock_gb300_free(uint8_t* p);
