@@ -69,6 +69,9 @@ def algorithmic_bytes(stage: str, m: int, lanes: int, k_code: int, n: int, kind:
         "zc_round1": 3 * 16 * W,
         "zc_fold_skip": 2 * 16 * W + 2 * 32 * W,
         "mo_build_w": 16 * W + 16 * W,
+        # folds: each round reads both vectors and writes both halves
+        "zc_folds": sum(2 * 16 * (3 * (1 << (m - 6 - i)) // 2) for i in range(1, m - 6)),
+        "mo_rounds": sum(2 * 16 * (3 * (W >> i) // 2) for i in range(0, m - 8)),
     }
     return table.get(stage)
 
@@ -255,9 +258,18 @@ def run_gpu(args, world, rank, local):
         raise SystemExit("device-input and host-input proves differ")
     bundle_len = len(b)
 
-    # ---- value: inputs resident in HBM
+    # ---- stage breakdown of one prove (outside the timed region): picks the roofline kernel
     setup.set_stage_timing(True)
-    stage_tot = {}
+    prove_dev()
+    calib = setup.last_stage_ms()
+    phases_calib = setup.last_phase_ms()
+    ranked = sorted(calib.items(), key=lambda kv: -kv[1][0])
+    dominant = next((k for k, _ in ranked if algorithmic_bytes(k, setup.m, setup.lanes, setup.log_code_len, n, kind)),
+                    ranked[0][0])
+
+    # ---- value: inputs resident in HBM; events only around the roofline stage
+    setup.set_stage_timing([dominant])
+    dom_ms, dom_launches = 0.0, 0
     step_ms = []
     barrier(world)
     torch.cuda.synchronize()
@@ -272,10 +284,9 @@ def run_gpu(args, world, rank, local):
             s0.record(stream)
             prove_dev()
             s1.record(stream)
-            for k, (ms, ln) in setup.last_stage_ms().items():
-                t = stage_tot.setdefault(k, [0.0, 0])
-                t[0] += ms
-                t[1] += ln
+            d_ms, d_l = setup.last_stage_ms()[dominant]
+            dom_ms += d_ms
+            dom_launches += d_l
             step_ms.append((s0, s1))
         ev1.record(stream)
         torch.cuda.synchronize()
@@ -305,26 +316,22 @@ def run_gpu(args, world, rank, local):
     # ---- roofline of the stage with the most device time
     peak, peak_src = peaks()
     m, lanes = setup.m, setup.lanes
-    ranked = sorted(stage_tot.items(), key=lambda kv: -kv[1][0])
+    alg = algorithmic_bytes(dominant, m, lanes, setup.log_code_len, n, kind)
     roof = None
-    for stage, (tot_ms, tot_launch) in ranked:
-        alg = algorithmic_bytes(stage, m, lanes, setup.log_code_len, n, kind)
-        if alg is None or tot_launch == 0:
-            continue
-        per_prove_ms = tot_ms / args.steps
+    if alg and dom_launches:
+        per_prove_ms = dom_ms / args.steps
         achieved = alg / (per_prove_ms / 1e3) / 1e9
         traffic = None
         tf = os.path.join(ROOT, "profiles", "traffic.json")
         if os.path.exists(tf):
             try:
-                traffic = json.load(open(tf)).get(wl, {}).get(stage)
+                traffic = json.load(open(tf)).get(wl, {}).get(dominant)
             except Exception:
                 traffic = None
-        roof = {"bound": "hbm", "kernel": stage, "achieved": achieved, "peak": peak, "unit": "GB/s",
+        roof = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": alg,
-                "launches_per_prove": tot_launch / args.steps, "device_ms_per_prove": per_prove_ms,
+                "launches_per_prove": dom_launches / args.steps, "device_ms_per_prove": per_prove_ms,
                 "peak_source": f"{peak_src} hbm_gbs", "share_of_step": per_prove_ms / (ms / args.steps)}
-        break
     if rank != 0:
         return 0
 
@@ -345,7 +352,7 @@ def run_gpu(args, world, rank, local):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "bundle_bytes": bundle_len},
         "roofline": roof,
-        "stages_ms_per_prove": {k: round(v[0] / args.steps, 4) for k, v in ranked},
+        "stages_ms_per_prove": {k: round(v[0], 4) for k, v in ranked},
         "host_phase_ms": {k: round(v, 3) for k, v in phases.items()},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),

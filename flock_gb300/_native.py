@@ -86,7 +86,7 @@ def load() -> ctypes.CDLL:
         lib.flock_gb300_prove_fast_device.restype = c.c_int
         lib.flock_gb300_setup_stream.argtypes = [c.c_void_p, c.POINTER(c.c_void_p)]
         lib.flock_gb300_setup_stream.restype = c.c_int
-        lib.flock_gb300_set_stage_timing.argtypes = [c.c_void_p, c.c_int]
+        lib.flock_gb300_set_stage_timing.argtypes = [c.c_void_p, c.c_uint32]
         lib.flock_gb300_set_stage_timing.restype = c.c_int
         lib.flock_gb300_last_stage_ms.argtypes = [c.c_void_p, c.POINTER(c.c_double), c.POINTER(c.c_uint32), c.c_int]
         lib.flock_gb300_last_stage_ms.restype = c.c_int

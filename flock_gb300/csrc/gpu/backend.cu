@@ -81,10 +81,12 @@ GpuBackend::GpuBackend(const Statement& s) : S(s) {
   n_pos0_ = uint64_t(1) << S.k_code;
   cw0_ = dmalloc<F128d>(n_pos0_ * S.lanes, owned_);
   tree0_ = dmalloc<uint8_t>((2 * n_pos0_) * 32, owned_);
-  zc1a_ = dmalloc<F128d>(2 * W, owned_);
-  zc1b_ = dmalloc<F128d>(2 * W, owned_);
+  // fold buffers: round 2 writes W words per vector (zc2), later rounds alternate (zc1, zc2)
+  zc1a_ = dmalloc<F128d>(W / 2, owned_);
+  zc1b_ = dmalloc<F128d>(W / 2, owned_);
   zc2a_ = dmalloc<F128d>(W, owned_);
   zc2b_ = dmalloc<F128d>(W, owned_);
+  zc_w64_ = dmalloc<F128d>(64, owned_);
   eqi_ = dmalloc<F128d>(K_, owned_);
   ca_ = dmalloc<F128d>(K_, owned_);
   cb_ = dmalloc<F128d>(K_, owned_);
@@ -182,14 +184,14 @@ cudaEvent_t GpuBackend::event() {
   return ev_pool_[ev_used_++];
 }
 GpuBackend::Mark::Mark(GpuBackend* be, int stage) : b(be), st(stage), l0(launch_count()) {
-  if (b->timing_) {
+  if ((b->timing_mask_ >> st) & 1) {
     cudaEvent_t a = b->event();
     CUDA_OK(cudaEventRecord(a, b->st_));
     b->spans_.push_back({st, a, nullptr, 0});
   }
 }
 GpuBackend::Mark::~Mark() {
-  if (b->timing_ && !b->spans_.empty()) {
+  if (((b->timing_mask_ >> st) & 1) && !b->spans_.empty()) {
     cudaEvent_t e = b->event();
     if (cudaEventRecord(e, b->st_) == cudaSuccess) {
       b->spans_.back().b = e;
@@ -450,13 +452,14 @@ void GpuBackend::zc_fold_skip(const std::vector<F128>& w, const std::vector<F128
   {
     Mark mk(this, ST_ZC_FOLD_SKIP);
     launch_eq_tables(dp, ddesc, (uint32_t)zc_desc_.size(), total, zc_tabs_, st_);
-    nb = launch_zc_fold_skip(a_, b_, dw, W_, zc_tabs_, 10, zc_tabs_ + zc_desc_[1].out_off, zc1a_, zc1b_, part_, st_);
+    nb = launch_zc_fold_skip(a_, b_, dw, W_, zc_tabs_, 10, zc_tabs_ + zc_desc_[1].out_off, part_, st_);
+    CUDA_OK(cudaMemcpyAsync(zc_w64_, dw, 64 * sizeof(F128d), cudaMemcpyDeviceToDevice, st_));
   }
   auto v = reduce(nb, 2);
   g1 = v[0];
   gi = v[1];
-  zc_cur_a_ = zc1a_;
-  zc_cur_b_ = zc1b_;
+  zc_cur_a_ = nullptr;  // the skip-folded vectors live only implicitly (a, b bits and the weights)
+  zc_cur_b_ = nullptr;
   zc_len_ = 2 * W_;
   zc_round_ = 0;
 }
@@ -469,13 +472,20 @@ void GpuBackend::zc_fold(F128 rho, const std::vector<F128>& eq_point, F128& g1, 
     throw std::runtime_error("zerocheck fold: round tables out of step");
   const EqDesc& lo = zc_desc_[k];
   const EqDesc& hi = zc_desc_[k + 1];
-  F128d* oa = (zc_cur_a_ == zc1a_) ? zc2a_ : zc1a_;
-  F128d* ob = (zc_cur_a_ == zc1a_) ? zc2b_ : zc1b_;
+  // round 0 writes W words per vector into zc2; later rounds alternate zc1 <-> zc2
+  F128d* oa = (zc_round_ == 0 || zc_cur_a_ == zc1a_) ? zc2a_ : zc1a_;
+  F128d* ob = (zc_round_ == 0 || zc_cur_a_ == zc1a_) ? zc2b_ : zc1b_;
   uint32_t nb;
   {
     Mark mk(this, ST_ZC_FOLDS);
-    nb = launch_pair_fold(zc_cur_a_, zc_cur_b_, n_pairs, dev(rho), nullptr, zc_tabs_ + lo.out_off, lo.n,
-                          zc_tabs_ + hi.out_off, oa, ob, part_, true, st_);
+    if (zc_round_ == 0) {
+      F128d* tabs = static_cast<F128d*>(scratch(4096 * sizeof(F128d)));
+      nb = launch_zc_fold2(a_, b_, zc_w64_, dev(rho), tabs, n_pairs, zc_tabs_ + lo.out_off, lo.n, zc_tabs_ + hi.out_off,
+                           oa, ob, part_, st_);
+    } else {
+      nb = launch_pair_fold(zc_cur_a_, zc_cur_b_, n_pairs, dev(rho), nullptr, zc_tabs_ + lo.out_off, lo.n,
+                            zc_tabs_ + hi.out_off, oa, ob, part_, true, st_);
+    }
   }
   auto v = reduce(nb, 2);
   g1 = v[0];

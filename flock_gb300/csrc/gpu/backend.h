@@ -58,7 +58,8 @@ class GpuBackend : public ProverBackend {
     ST_MO_BUILD_W, ST_MO_ROUNDS, ST_LIGERITO, ST_LG_NTT, ST_LG_MERKLE, ST_COUNT
   };
   static const char* stage_name(int s);
-  void set_stage_timing(bool on) { timing_ = on; }
+  // bit s of `mask` records CUDA events around stage s (0: none)
+  void set_stage_timing(uint32_t mask) { timing_mask_ = mask; }
   // Called before each prove: clears transfer counters and stage events.
   void begin_prove(const void* d_inputs);
   // Milliseconds per stage of the last prove and the launches counted in each.
@@ -112,7 +113,7 @@ class GpuBackend : public ProverBackend {
 
   const Statement& S;
   int device_ = 0;
-  bool timing_ = false;
+  uint32_t timing_mask_ = 0;
   std::vector<cudaEvent_t> ev_pool_;
   size_t ev_used_ = 0;
   struct Span { int st; cudaEvent_t a, b; uint64_t launches; };
@@ -138,6 +139,7 @@ class GpuBackend : public ProverBackend {
   F128d *zc_cur_a_ = nullptr, *zc_cur_b_ = nullptr;
   uint64_t zc_len_ = 0;
   uint32_t zc_round_ = 0;
+  F128d* zc_w64_ = nullptr;  // skip-point Lagrange weights (device)
 
   F128d *eqi_ = nullptr, *ca_ = nullptr, *cb_ = nullptr, *comb_ = nullptr, *zv_ = nullptr, *zvcap_ = nullptr;
   uint32_t *cola_ = nullptr, *rowa_ = nullptr, *colb_ = nullptr, *rowb_ = nullptr;

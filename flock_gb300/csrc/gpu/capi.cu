@@ -141,10 +141,10 @@ int flock_gb300_setup_stream(const flock_gb300_setup* setup, void** stream) {
   return FLOCK_GB300_OK;
 }
 
-int flock_gb300_set_stage_timing(flock_gb300_setup* setup, int enabled) {
+int flock_gb300_set_stage_timing(flock_gb300_setup* setup, uint32_t stage_mask) {
   if (!setup) return fail(FLOCK_GB300_EINVAL, "null setup");
   std::lock_guard<std::mutex> g(setup->mu);
-  setup->backend->set_stage_timing(enabled != 0);
+  setup->backend->set_stage_timing(stage_mask);
   return FLOCK_GB300_OK;
 }
 

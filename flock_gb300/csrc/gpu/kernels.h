@@ -57,8 +57,12 @@ void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t mulk[
 uint32_t launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32_t m, const F128d* eq_lo,
                           uint32_t lo_bits, const F128d* eq_hi, F128d* part, cudaStream_t s);          // width 192
 uint32_t launch_zc_fold_skip(const F128d* a, const F128d* b, const F128d* w64, uint64_t n_words, const F128d* eq_lo,
-                             uint32_t lo_bits, const F128d* eq_hi, F128d* amlv, F128d* bmlv, F128d* part,
-                             cudaStream_t s);                                                          // width 2
+                             uint32_t lo_bits, const F128d* eq_hi, F128d* part, cudaStream_t s);       // width 2
+// First multilinear fold (at rho) of the skip-folded a, b, computed from the bits; writes
+// n_pairs * 2 words of each folded vector and the next message. tabs: 4096-word scratch.
+uint32_t launch_zc_fold2(const F128d* a, const F128d* b, const F128d* w64, F128d rho, F128d* tabs, uint64_t n_pairs,
+                         const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* aout, F128d* bout, F128d* part,
+                         cudaStream_t s);                                                              // width 2
 // r_dev (when not null) is the device address of the challenge, read by the kernel.
 uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, F128d r, const F128d* r_dev,
                           const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* aout, F128d* bout,

@@ -232,12 +232,12 @@ uint32_t launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32
 // ------------------------------------------------------------------ zerocheck skip fold
 // a_mlv[x] = sum_{s in bits(a_x)} w[s] via 8 byte tables of the 64 Lagrange weights;
 // word w holds rows 2w (lo) and 2w+1 (hi), which is exactly the first multilinear pair.
-// Message: g1 = sum_w eq(w) a1 b1, ginf = sum_w eq(w) (a0 + a1)(b0 + b1).
+// Message: g1 = sum_w eq(w) a1 b1, ginf = sum_w eq(w) (a0 + a1)(b0 + b1). The folded
+// vectors are not stored: the next round recomputes them from the bits (below).
 __global__ void __launch_bounds__(256)
 zc_fold_skip_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, const F128d* __restrict__ w64,
                     uint64_t n_words, const F128d* __restrict__ eq_lo, uint32_t lo_bits,
-                    const F128d* __restrict__ eq_hi, F128d* __restrict__ amlv, F128d* __restrict__ bmlv,
-                    F128d* __restrict__ part) {
+                    const F128d* __restrict__ eq_hi, F128d* __restrict__ part) {
   __shared__ F128d T[8][256];
   __shared__ F128d sh[32];
   for (uint32_t e = threadIdx.x; e < 2048; e += blockDim.x) {
@@ -264,8 +264,6 @@ zc_fold_skip_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, co
         b0 += T[c][(bv.lo >> (8 * c)) & 255];
         b1 += T[c][(bv.hi >> (8 * c)) & 255];
       }
-      amlv[2 * wi] = a0; amlv[2 * wi + 1] = a1;
-      bmlv[2 * wi] = b0; bmlv[2 * wi + 1] = b1;
       F128d e = eq_lo[wi & (chunk - 1)];
       g1 += e * (a1 * b1);
       gi += e * ((a0 + a1) * (b0 + b1));
@@ -281,11 +279,94 @@ zc_fold_skip_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, co
   if (threadIdx.x == 0) { part[blockIdx.x * 2] = G1; part[blockIdx.x * 2 + 1] = GI; }
 }
 uint32_t launch_zc_fold_skip(const F128d* a, const F128d* b, const F128d* w64, uint64_t n_words, const F128d* eq_lo,
-                             uint32_t lo_bits, const F128d* eq_hi, F128d* amlv, F128d* bmlv, F128d* part,
-                             cudaStream_t s) {
+                             uint32_t lo_bits, const F128d* eq_hi, F128d* part, cudaStream_t s) {
   uint64_t n_chunks = (n_words + (1ull << lo_bits) - 1) >> lo_bits;
   uint32_t blocks = (uint32_t)std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 8);
-  zc_fold_skip_kernel<<<blocks, 256, 0, s>>>(a, b, w64, n_words, eq_lo, lo_bits, eq_hi, amlv, bmlv, part);
+  zc_fold_skip_kernel<<<blocks, 256, 0, s>>>(a, b, w64, n_words, eq_lo, lo_bits, eq_hi, part);
+  LAUNCH_OK();
+  return blocks;
+}
+
+// The first multilinear fold at rho straight from the bits: the skip-folded pair of word
+// w is (sum_s lo_s w_s, sum_s hi_s w_s), so its fold is
+//   A'[w] = sum_s lo_s (1 + rho) w_s + sum_s hi_s rho w_s,
+// two byte-table sums with the weights pre-scaled by (1 + rho) and rho (no per-word
+// multiply). Then the next message over the pairs (A'[2j], A'[2j+1]) with eq(j).
+__global__ void zc_scaled_tables_kernel(const F128d* __restrict__ w64, F128d rho, F128d* __restrict__ tabs) {
+  __shared__ F128d ws[2][64];
+  if (threadIdx.x < 64) {
+    F128d v = rho * w64[threadIdx.x];
+    ws[1][threadIdx.x] = v;                    // rho * w
+    ws[0][threadIdx.x] = v + w64[threadIdx.x];  // (1 + rho) * w
+  }
+  __syncthreads();
+  for (uint32_t e = threadIdx.x; e < 2 * 2048; e += blockDim.x) {
+    uint32_t t = e >> 11, c = (e >> 8) & 7, v = e & 255;
+    F128d acc = f128_zero();
+    for (int k = 0; k < 8; ++k)
+      if ((v >> k) & 1) acc += ws[t][8 * c + k];
+    tabs[e] = acc;
+  }
+}
+__global__ void __launch_bounds__(256)
+zc_fold2_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, const F128d* __restrict__ tabs,
+                uint64_t n_pairs, const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F128d* __restrict__ eq_hi,
+                F128d* __restrict__ aout, F128d* __restrict__ bout, F128d* __restrict__ part) {
+  extern __shared__ __align__(16) F128d T[];  // [2][8][256]: (1 + rho) w tables, then rho w tables
+  __shared__ F128d sh[32];
+  for (uint32_t e = threadIdx.x; e < 4096; e += blockDim.x) T[e] = tabs[e];
+  __syncthreads();
+  const F128d* T0 = T;
+  const F128d* T1 = T + 2048;
+  const uint64_t chunk = 1ull << lo_bits;
+  const uint64_t n_chunks = (n_pairs + chunk - 1) / chunk;
+  F128d G1 = f128_zero(), GI = f128_zero();
+  for (uint64_t ch = blockIdx.x; ch < n_chunks; ch += gridDim.x) {
+    F128d g1 = f128_zero(), gi = f128_zero();
+    uint64_t end = min(n_pairs, (ch + 1) * chunk);
+    for (uint64_t j = ch * chunk + threadIdx.x; j < end; j += blockDim.x) {
+      F128d A[2], B[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        F128d av = a[2 * j + h], bv = b[2 * j + h];
+        F128d sa = f128_zero(), sb = f128_zero();
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          sa += T0[c * 256 + ((av.lo >> (8 * c)) & 255)] + T1[c * 256 + ((av.hi >> (8 * c)) & 255)];
+          sb += T0[c * 256 + ((bv.lo >> (8 * c)) & 255)] + T1[c * 256 + ((bv.hi >> (8 * c)) & 255)];
+        }
+        A[h] = sa;
+        B[h] = sb;
+      }
+      aout[2 * j] = A[0]; aout[2 * j + 1] = A[1];
+      bout[2 * j] = B[0]; bout[2 * j + 1] = B[1];
+      F128d e = eq_lo[j & (chunk - 1)];
+      g1 += e * (A[1] * B[1]);
+      gi += e * ((A[0] + A[1]) * (B[0] + B[1]));
+    }
+    g1 = block_xor(g1, sh);
+    gi = block_xor(gi, sh);
+    if (threadIdx.x == 0) {
+      F128d hh = eq_hi ? eq_hi[ch] : f128_one();
+      G1 += hh * g1;
+      GI += hh * gi;
+    }
+  }
+  if (threadIdx.x == 0) { part[blockIdx.x * 2] = G1; part[blockIdx.x * 2 + 1] = GI; }
+}
+uint32_t launch_zc_fold2(const F128d* a, const F128d* b, const F128d* w64, F128d rho, F128d* tabs, uint64_t n_pairs,
+                         const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* aout, F128d* bout, F128d* part,
+                         cudaStream_t s) {
+  zc_scaled_tables_kernel<<<16, 256, 0, s>>>(w64, rho, tabs);
+  LAUNCH_OK();
+  static bool attr = false;
+  if (!attr) {
+    CUDA_OK(cudaFuncSetAttribute(zc_fold2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 4096 * 16));
+    attr = true;
+  }
+  uint64_t n_chunks = (n_pairs + (1ull << lo_bits) - 1) >> lo_bits;
+  uint32_t blocks = (uint32_t)std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 3);
+  zc_fold2_kernel<<<blocks, 256, 4096 * 16, s>>>(a, b, tabs, n_pairs, eq_lo, lo_bits, eq_hi, aout, bout, part);
   LAUNCH_OK();
   return blocks;
 }

@@ -115,8 +115,19 @@ class _Setup:
         _native.check(self._lib.flock_gb300_setup_stream(self._h, ctypes.byref(h)))
         return h.value or 0
 
-    def set_stage_timing(self, enabled: bool) -> None:
-        _native.check(self._lib.flock_gb300_set_stage_timing(self._h, 1 if enabled else 0))
+    def set_stage_timing(self, stages=True) -> None:
+        """Record CUDA events around stages: True = all, False/None = none, or an
+        iterable of stage names."""
+        if stages is True:
+            mask = 0xFFFFFFFF
+        elif not stages:
+            mask = 0
+        else:
+            names = [self._lib.flock_gb300_stage_name(i).decode() for i in range(32)]
+            mask = 0
+            for s in stages:
+                mask |= 1 << names.index(s)
+        _native.check(self._lib.flock_gb300_set_stage_timing(self._h, mask))
 
     def last_stage_ms(self) -> dict:
         """{stage: (device ms, kernel launches)} of the last prove (stage timing enabled)."""

@@ -83,10 +83,11 @@ int flock_gb300_prove_fast_device(flock_gb300_setup* setup, const void* d_inputs
 /* The CUDA stream (cudaStream_t) every kernel of this setup runs on. */
 int flock_gb300_setup_stream(const flock_gb300_setup* setup, void** stream);
 
-/* Device-time breakdown. When enabled, each prove records CUDA events around its stages;
- * flock_gb300_last_stage_ms then fills up to `cap` entries of milliseconds and kernel
- * launch counts per stage (names from flock_gb300_stage_name) and returns the stage count. */
-int flock_gb300_set_stage_timing(flock_gb300_setup* setup, int enabled);
+/* Device-time breakdown. Each prove records CUDA events around the stages whose bit is
+ * set in stage_mask (0 = none, the default); flock_gb300_last_stage_ms then fills up to
+ * `cap` entries of milliseconds and kernel launch counts per stage (names from
+ * flock_gb300_stage_name) and returns the stage count. */
+int flock_gb300_set_stage_timing(flock_gb300_setup* setup, uint32_t stage_mask);
 int flock_gb300_last_stage_ms(flock_gb300_setup* setup, double* ms, uint32_t* launches, int cap);
 const char* flock_gb300_stage_name(int stage);
 
