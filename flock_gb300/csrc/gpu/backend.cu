@@ -31,7 +31,15 @@ void upload_constants_once() {
       for (int j = 0; j < 2; ++j) e = gf8_mul(e, ((K2 >> j) & 1) ? c[j + 1] : (uint8_t)(c[j + 1] ^ 1));
       e2[K2] = e;
     }
-    upload_zc_consts(st.ext.data(), reinterpret_cast<const F128d*>(phi8_table().data()), mulk, e2);
+    // word 4M + K2 of an xo carries eq weight x^M * phi8(e2[K2]) (times D * eq_o(xo))
+    F128 wconst[64];
+    for (int M = 0; M < 16; ++M) {
+      F128 xm = F128::one();
+      for (int i = 0; i < M; ++i) xm = mul_by_x(xm);
+      for (int K2 = 0; K2 < 4; ++K2) wconst[4 * M + K2] = xm * phi8(e2[K2]);
+    }
+    upload_zc_consts(st.ext.data(), reinterpret_cast<const F128d*>(phi8_table().data()), mulk,
+                     reinterpret_cast<const F128d*>(wconst));
   });
 }
 
@@ -380,12 +388,17 @@ void GpuBackend::zc_round1(const std::vector<F128>& r, std::vector<F128>& ab, st
     if (r[6 + i] != fixed[i]) throw std::runtime_error("zerocheck round 1 expects the fixed challenges at r[6..13)");
   std::vector<F128> outer(r.begin() + 13, r.end());
   EqSplit e = eq_split(outer, F128::one(), 10);
-  uint32_t nb;
+  uint32_t nab = 0, nsvc = 0;
+  F128d* part_svc = part_ + part_cap_ / 2;
   {
     Mark mk(this, ST_ZC_ROUND1);
-    nb = launch_zc_round1(a_, b_, z_, m, e.lo, e.lo_bits, e.hi, part_, st_);
+    launch_zc_round1(a_, b_, z_, m, e.lo, e.lo_bits, e.hi, part_, &nab, part_svc, &nsvc, st_);
   }
-  auto v = reduce(nb, 192);
+  if ((uint64_t)nab * 64 > part_cap_ / 2 || (uint64_t)nsvc * 128 > part_cap_ / 2)
+    throw std::runtime_error("round-1 partials exceed the partials buffer");
+  launch_reduce_parts(part_, nab, 64, red_, st_);
+  launch_reduce_parts(part_svc, nsvc, 128, red_ + 64, st_);
+  auto v = fetch(red_, 192);
   // D = prod (1 + g_i)^-1 over the medium constants' g_i = x^1, x^2, x^4, x^8
   static const F128 D = [] {
     F128 d = F128::one();

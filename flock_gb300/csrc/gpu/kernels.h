@@ -33,6 +33,7 @@ void note_launch();
 int sm_count();
 
 // witness.cu — writes chunk columns [0, used_chunks) of z, a, b
+void upload_witness_constants();  // once per process (synchronous symbol copies)
 void launch_witness(int hash, const void* d_inputs, uint32_t n_inst, uint32_t nu, F128d* z, F128d* a, F128d* b,
                     uint32_t used_chunks, cudaStream_t s);
 
@@ -53,9 +54,11 @@ void launch_gather_paths(const uint8_t* tree, uint64_t n_leaves, const uint64_t*
 void launch_eq_table(const F128d* d_point, uint32_t n, F128d scale, F128d* out, cudaStream_t s);
 void launch_reduce_parts(const F128d* part, uint32_t n_blocks, uint32_t width, F128d* out, cudaStream_t s);
 
-void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t mulk[8][256], const uint8_t e2[4]);
-uint32_t launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32_t m, const F128d* eq_lo,
-                          uint32_t lo_bits, const F128d* eq_hi, F128d* part, cudaStream_t s);          // width 192
+void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t mulk[8][256], const F128d* wconst);
+// Round-1 partials: P_ab rows of width 64 into part_ab, s_hat_v_c rows of width 128 into part_svc.
+void launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32_t m, const F128d* eq_lo, uint32_t lo_bits,
+                      const F128d* eq_hi, F128d* part_ab, uint32_t* nrows_ab, F128d* part_svc, uint32_t* nrows_svc,
+                      cudaStream_t s);
 uint32_t launch_zc_fold_skip(const F128d* a, const F128d* b, const F128d* w64, uint64_t n_words, const F128d* eq_lo,
                              uint32_t lo_bits, const F128d* eq_hi, F128d* part, cudaStream_t s);       // width 2
 // First multilinear fold (at rho) of the skip-folded a, b, computed from the bits; writes

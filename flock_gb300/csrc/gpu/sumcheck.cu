@@ -95,115 +95,136 @@ struct ZcConsts {
   uint8_t ext[8 * 256 * 64];   // ext[c][v][i]: extension of byte v at S[8c..8c+8)
   F128d phi8[256];
   uint8_t mulk[8][256];        // e_K * v
-  uint8_t e2[4];
-};
-
-constexpr int ZC_XPB = 4;  // xo groups in flight per block (256 threads each)
-struct ZcStage {
-  F128d wa[64], wb[64], wz[64];
-  uint32_t gab[16][16];
-  F128d eqo;
+  F128d wconst[64];            // word weights within an xo: x^M * phi8(e2[K2]) for word 4M + K2
 };
 constexpr size_t ZC_CONST_BYTES = (sizeof(ZcConsts) + 15) & ~size_t(15);
+
+// Byte b of a word (zero-extended) and every byte of v set to 0xFF where its bit 7 is set:
+// one byte-permute each.
+__device__ __forceinline__ uint32_t byte_of(uint32_t v, int b) { return __byte_perm(v, 0, 0x4440 | b); }
+// prmt with the sign-replicate bit set in each selector nibble (not expressible through
+// __byte_perm, which ignores that bit)
+__device__ __forceinline__ uint32_t msb_spread(uint32_t v) {
+  uint32_t r;
+  asm("prmt.b32 %0, %1, %2, 0xBA98;" : "=r"(r) : "r"(v), "r"(0u));
+  return r;
+}
 
 // Four GF(2^8) products (AES polynomial) of packed bytes, shift-and-add in registers.
 __device__ __forceinline__ uint32_t gf8_mul4(uint32_t a, uint32_t b) {
   uint32_t r = 0;
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    uint32_t m = ((b >> k) & 0x01010101u) * 0xFFu;
-    r ^= a & m;
-    uint32_t hi = (a >> 7) & 0x01010101u;
-    a = ((a & 0x7F7F7F7Fu) << 1) ^ (hi * 0x1Bu);
+    r ^= a & msb_spread(b << (7 - k));  // bit k of each byte of b selects a * x^k
+    if (k < 7) a = ((a << 1) & 0xFEFEFEFEu) ^ (msb_spread(a) & 0x1B1B1B1Bu);
   }
   return r;
 }
 
-__global__ void __launch_bounds__(256 * ZC_XPB, 1)
-zc_round1_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, const F128d* __restrict__ z,
-                 uint64_t n_xo, const ZcConsts* __restrict__ gconst, const F128d* __restrict__ eq_lo,
-                 uint32_t lo_bits, const F128d* __restrict__ eq_hi, F128d* __restrict__ part) {
+// P_ab: one team of 16 threads per xo, thread = four Lambda points; no block barriers
+// after the constants are staged. Per row x = 8M + K the team extends the a and b rows
+// (8 byte-table lookups each), multiplies pointwise in GF(2^8) and accumulates e_K * p
+// into g_M; then F = sum_M x^M phi8(g_M) (Horner) and acc += eq_o(xo) * F.
+constexpr int ZC_TEAMS = 24;  // teams per block (384 threads)
+__global__ void __launch_bounds__(16 * ZC_TEAMS, 1)
+zc_round1_ab_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, uint64_t n_xo,
+                    const ZcConsts* __restrict__ gconst, const F128d* __restrict__ eq_lo, uint32_t lo_bits,
+                    const F128d* __restrict__ eq_hi, F128d* __restrict__ part) {
   extern __shared__ __align__(16) uint8_t smem[];
   ZcConsts& C = *reinterpret_cast<ZcConsts*>(smem);
-  ZcStage* stages = reinterpret_cast<ZcStage*>(smem + ZC_CONST_BYTES);
   {
     const uint4* src = reinterpret_cast<const uint4*>(gconst);
     uint4* dst = reinterpret_cast<uint4*>(smem);
     for (uint32_t i = threadIdx.x; i < ZC_CONST_BYTES / 16; i += blockDim.x) dst[i] = src[i];
   }
-  const uint32_t sub = threadIdx.x >> 8, t = threadIdx.x & 255;
-  ZcStage& S = stages[sub];
-  const uint32_t* ext32 = reinterpret_cast<const uint32_t*>(C.ext);
-  F128d acc = f128_zero();
   __syncthreads();
-  const uint64_t n_groups = (n_xo + ZC_XPB - 1) / ZC_XPB;
-  for (uint64_t g = blockIdx.x; g < n_groups; g += gridDim.x) {
-    uint64_t xo = g * ZC_XPB + sub;
-    bool live = xo < n_xo;
-    if (live) {
-      if (t < 64) S.wa[t] = a[xo * 64 + t];
-      else if (t < 128) S.wb[t - 64] = b[xo * 64 + t - 64];
-      else if (t < 192) S.wz[t - 128] = z[xo * 64 + t - 128];
-      else if (t == 192) S.eqo = eq_at(eq_lo, lo_bits, eq_hi, xo);
-    }
-    __syncthreads();
-    if (live) {
-      const uint32_t M = t >> 4, lane = t & 15;
-      uint32_t gab = 0;
-#pragma unroll 2
-      for (uint32_t K = 0; K < 8; ++K) {
-        uint32_t xl = 8 * M + K, w = xl >> 1;
-        uint64_t ab = (xl & 1) ? S.wa[w].hi : S.wa[w].lo;
-        uint64_t bb = (xl & 1) ? S.wb[w].hi : S.wb[w].lo;
-        uint32_t ea = 0, eb = 0;
+  const uint32_t team = threadIdx.x >> 4, lane = threadIdx.x & 15;
+  // ext as bytes: table c, value v, this lane's four points at c * 16384 + v * 64 + 4 * lane
+  const uint8_t* extb = C.ext + 4 * lane;
+  F128d acc[4] = {f128_zero(), f128_zero(), f128_zero(), f128_zero()};
+  const uint64_t stride = (uint64_t)gridDim.x * ZC_TEAMS;
+  for (uint64_t xo = (uint64_t)blockIdx.x * ZC_TEAMS + team; xo < n_xo; xo += stride) {
+    const uint4* wa = reinterpret_cast<const uint4*>(a + xo * 64);
+    const uint4* wb = reinterpret_cast<const uint4*>(b + xo * 64);
+    uint32_t G[16];
+#pragma unroll 1
+    for (int M = 0; M < 16; ++M) {
+      uint32_t g = 0;
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-          ea ^= ext32[((c << 8) + ((ab >> (8 * c)) & 255)) * 16 + lane];
-          eb ^= ext32[((c << 8) + ((bb >> (8 * c)) & 255)) * 16 + lane];
-        }
-        uint32_t p = gf8_mul4(ea, eb);
-        const uint8_t* mk = C.mulk[K];
-        gab ^= (uint32_t)mk[p & 255] | ((uint32_t)mk[(p >> 8) & 255] << 8) | ((uint32_t)mk[(p >> 16) & 255] << 16) |
-               ((uint32_t)mk[p >> 24] << 24);
-      }
-      S.gab[M][lane] = gab;
-    }
-    __syncthreads();
-    if (live && t < 192) {
-      F128d F = f128_zero();
-      if (t < 64) {
-        const uint8_t* G = reinterpret_cast<const uint8_t*>(&S.gab[0][0]);
+      for (int kk = 0; kk < 4; ++kk) {
+        uint4 A = wa[4 * M + kk], B = wb[4 * M + kk];
 #pragma unroll
-        for (int M = 15; M >= 0; --M) F = mul_by_x(F) + C.phi8[G[M * 64 + t]];
-      } else {
-        uint32_t tb = t - 64, limb = tb >> 6, sh = tb & 63;
+        for (int h = 0; h < 2; ++h) {
+          uint32_t a0 = h ? A.z : A.x, a1 = h ? A.w : A.y;  // the 64-bit row as two words
+          uint32_t b0 = h ? B.z : B.x, b1 = h ? B.w : B.y;
+          uint32_t ea = 0, eb = 0;
 #pragma unroll
-        for (int M = 15; M >= 0; --M) {
-          uint32_t gv = 0;
-#pragma unroll
-          for (int K2 = 0; K2 < 4; ++K2) {
-            const F128d& wv = S.wz[4 * M + K2];
-            uint64_t bits = limb ? wv.hi : wv.lo;
-            gv ^= (uint32_t)C.e2[K2] & (0u - (uint32_t)((bits >> sh) & 1));
+          for (int c = 0; c < 4; ++c) {
+            ea ^= *reinterpret_cast<const uint32_t*>(extb + c * 16384 + (byte_of(a0, c) << 6)) ^
+                  *reinterpret_cast<const uint32_t*>(extb + (c + 4) * 16384 + (byte_of(a1, c) << 6));
+            eb ^= *reinterpret_cast<const uint32_t*>(extb + c * 16384 + (byte_of(b0, c) << 6)) ^
+                  *reinterpret_cast<const uint32_t*>(extb + (c + 4) * 16384 + (byte_of(b1, c) << 6));
           }
-          F = mul_by_x(F) + C.phi8[gv];
+          uint32_t p = gf8_mul4(ea, eb);
+          const uint8_t* mk = C.mulk[2 * kk + h];
+          g ^= (uint32_t)mk[byte_of(p, 0)] | ((uint32_t)mk[byte_of(p, 1)] << 8) | ((uint32_t)mk[byte_of(p, 2)] << 16) |
+               ((uint32_t)mk[byte_of(p, 3)] << 24);
         }
       }
-      acc += S.eqo * F;
+      G[M] = g;
+    }
+    F128d e = eq_at(eq_lo, lo_bits, eq_hi, xo);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      F128d F = f128_zero();
+#pragma unroll
+      for (int M = 15; M >= 0; --M) F = mul_by_x(F) + C.phi8[(G[M] >> (8 * k)) & 255];
+      acc[k] += e * F;
+    }
+  }
+  uint64_t row = (uint64_t)blockIdx.x * ZC_TEAMS + team;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) part[row * 64 + 4 * lane + k] = acc[k];
+}
+
+// s_hat_v_c: per xo the 64 word weights eq_o(xo) * x^M * phi8(e2[K2]) (one multiply each),
+// then thread t XORs the weights of the words whose bit t is set.
+__global__ void __launch_bounds__(128)
+zc_svc_kernel(const F128d* __restrict__ z, uint64_t n_xo, const ZcConsts* __restrict__ gconst,
+              const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F128d* __restrict__ eq_hi,
+              F128d* __restrict__ part) {
+  __shared__ F128d wc[64], wt[64];
+  __shared__ F128d wz[64];
+  const uint32_t t = threadIdx.x;
+  if (t < 64) wc[t] = gconst->wconst[t];
+  F128d acc = f128_zero();
+  const uint32_t limb = t >> 6, sh = t & 63;
+  for (uint64_t xo = blockIdx.x; xo < n_xo; xo += gridDim.x) {
+    __syncthreads();
+    if (t < 64) {
+      wt[t] = eq_at(eq_lo, lo_bits, eq_hi, xo) * wc[t];
+      wz[t] = z[xo * 64 + t];
     }
     __syncthreads();
+#pragma unroll 8
+    for (int w = 0; w < 64; ++w) {
+      uint64_t bits = limb ? wz[w].hi : wz[w].lo;
+      uint64_t m = 0ull - ((bits >> sh) & 1);
+      acc.lo ^= wt[w].lo & m;
+      acc.hi ^= wt[w].hi & m;
+    }
   }
-  if (t < 192) part[((uint64_t)blockIdx.x * ZC_XPB + sub) * 192 + t] = acc;
+  part[(uint64_t)blockIdx.x * 128 + t] = acc;
 }
 
 static ZcConsts* g_zc_consts = nullptr;
-void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t mulk[8][256], const uint8_t e2[4]) {
+void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t mulk[8][256], const F128d* wconst) {
   if (g_zc_consts) return;
   ZcConsts* h = new ZcConsts();
   memcpy(h->ext, ext, sizeof(h->ext));
   memcpy(h->phi8, phi8, sizeof(h->phi8));
   memcpy(h->mulk, mulk, sizeof(h->mulk));
-  memcpy(h->e2, e2, 4);
+  memcpy(h->wconst, wconst, sizeof(h->wconst));
   ZcConsts* d = nullptr;
   CUDA_OK(cudaMalloc(&d, ZC_CONST_BYTES));
   CUDA_OK(cudaMemset(d, 0, ZC_CONST_BYTES));
@@ -212,21 +233,25 @@ void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t mulk[
   g_zc_consts = d;
 }
 
-uint32_t launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32_t m, const F128d* eq_lo,
-                          uint32_t lo_bits, const F128d* eq_hi, F128d* part, cudaStream_t s) {
+void launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32_t m, const F128d* eq_lo, uint32_t lo_bits,
+                      const F128d* eq_hi, F128d* part_ab, uint32_t* nrows_ab, F128d* part_svc, uint32_t* nrows_svc,
+                      cudaStream_t s) {
   if (!g_zc_consts) throw std::runtime_error("zerocheck constants not uploaded");
   uint64_t n_xo = 1ull << (m - 13);
-  size_t smem = ZC_CONST_BYTES + ZC_XPB * sizeof(ZcStage);
+  size_t smem = ZC_CONST_BYTES;
   static bool attr = false;
   if (!attr) {
-    CUDA_OK(cudaFuncSetAttribute(zc_round1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CUDA_OK(cudaFuncSetAttribute(zc_round1_ab_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
-  uint64_t groups = (n_xo + ZC_XPB - 1) / ZC_XPB;
-  uint32_t blocks = (uint32_t)std::min<uint64_t>(groups, (uint64_t)sm_count());
-  zc_round1_kernel<<<blocks, 256 * ZC_XPB, smem, s>>>(a, b, z, n_xo, g_zc_consts, eq_lo, lo_bits, eq_hi, part);
+  uint32_t blocks = (uint32_t)std::min<uint64_t>((n_xo + ZC_TEAMS - 1) / ZC_TEAMS, (uint64_t)sm_count());
+  zc_round1_ab_kernel<<<blocks, 16 * ZC_TEAMS, smem, s>>>(a, b, n_xo, g_zc_consts, eq_lo, lo_bits, eq_hi, part_ab);
   LAUNCH_OK();
-  return blocks * ZC_XPB;  // partial rows of width 192: ab[64] then s_hat_v_c[128]
+  *nrows_ab = blocks * ZC_TEAMS;
+  uint32_t sblocks = (uint32_t)std::min<uint64_t>(n_xo, (uint64_t)sm_count() * 8);
+  zc_svc_kernel<<<sblocks, 128, 0, s>>>(z, n_xo, g_zc_consts, eq_lo, lo_bits, eq_hi, part_svc);
+  LAUNCH_OK();
+  *nrows_svc = sblocks;
 }
 
 // ------------------------------------------------------------------ zerocheck skip fold
