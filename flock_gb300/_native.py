@@ -28,6 +28,7 @@ EXPORTS = (
     "flock_gb300_last_transfer_bytes",
     "flock_gb300_launch_count",
     "flock_gb300_last_phase_ms",
+    "flock_gb300_commit_cap_noalloc",
     "flock_gb300_free",
     "flock_gb300_device_count",
     "flock_gb300_last_error",
@@ -98,6 +99,9 @@ def load() -> ctypes.CDLL:
         lib.flock_gb300_launch_count.restype = c.c_uint64
         lib.flock_gb300_last_phase_ms.argtypes = [c.c_void_p, c.POINTER(c.c_double)]
         lib.flock_gb300_last_phase_ms.restype = c.c_int
+        lib.flock_gb300_commit_cap_noalloc.argtypes = [c.c_int, c.c_void_p, c.c_uint64, c.c_char_p, c.c_size_t,
+                                                       c.POINTER(c.c_size_t), c.c_void_p]
+        lib.flock_gb300_commit_cap_noalloc.restype = c.c_int
         lib.flock_gb300_free.argtypes = [c.POINTER(c.c_uint8)]
         lib.flock_gb300_free.restype = None
         lib.flock_gb300_device_count.argtypes = []

@@ -48,6 +48,10 @@ int guarded(F&& f) {
 
 }  // namespace
 
+namespace flock {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace flock
+
 struct flock_gb300_setup {
   std::shared_ptr<Statement> stmt;
   std::unique_ptr<gpu::GpuBackend> backend;

@@ -102,6 +102,28 @@ uint64_t flock_gb300_launch_count(void);
  *  time the open phase waited for the assist]. */
 int flock_gb300_last_phase_ms(const flock_gb300_setup* setup, double out[8]);
 
+/* The L0 commitment cap of a batch without any device allocation by the library.
+ *
+ * For callers that cannot let a library allocate device memory: inside a pre-reserved
+ * memory budget (an HBM-budgeted serving process), or on a stream whose work must not be
+ * interleaved with allocator calls. Runs witness generation, the lane-major codeword fill,
+ * the additive NTT and the Merkle tree of the batch's committed stack in a fixed static
+ * device array (32 MiB, codewords of at most 2^13 rows: e.g. up to 2^11 BLAKE3 or SHA-256
+ * compressions); larger batches are rejected with FLOCK_GB300_EINVAL and a message naming
+ * the bytes needed. d_inputs: n_blocks packed input records in device memory. On success
+ * cap_out receives the 2^c x 32-byte Merkle cap, identical to the cap in the bundle of
+ * flock_gb300_prove_fast for the same inputs, and *cap_len its length; the call returns
+ * after the work on `stream` (a cudaStream_t, 0 = legacy default) completes.
+ * The first call on a device looks up the static arrays and copies the twiddle tables in
+ * (synchronous copies): make it before any stream capture. The chunk columns past the
+ * witness are cleared on every call (nothing needs to start zeroed). All calls on a device
+ * share the one static array: calls are serialised by a per-device lock, and the caller
+ * must not run two of them concurrently through other means (e.g. from two processes
+ * sharing a context). No reference counterpart: the reference commits only inside
+ * prove_fast. */
+int flock_gb300_commit_cap_noalloc(int hash_kind, const void* d_inputs, uint64_t n_blocks, uint8_t* cap_out,
+                                   size_t cap_out_bytes, size_t* cap_len, void* stream);
+
 /* Releases a bundle returned by flock_gb300_prove_fast (cuda-ghash/prove_ffi.cu:417 flock_cuda_free). */
 void flock_gb300_free(uint8_t* p);
 
