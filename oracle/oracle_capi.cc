@@ -101,3 +101,78 @@ int oracle_registry_digest_kat(int which, uint8_t out[32]) {
 }
 
 }  // extern "C"
+
+// R1CS self-checks of one block per hash on seeded inputs (the encoders' satisfiability
+// and, for the walker-based Keccak type, the walker's transpose identity):
+//   out[0] = rows where a != A z, out[1] = rows where b != B z (BLAKE3 / SHA-256, the
+//            materialised matrices; Keccak: 0 / 1 walker identity failures),
+//   out[2] = rows where a AND b != z (C = I),
+//   out[3] = Keccak only: 1 if Keccak-f of the zero state starts with lane 0xf1258f7940e1dde7.
+extern "C" int oracle_r1cs_check(int hash_kind, uint64_t seed, uint64_t out[4]) {
+  try {
+    out[0] = out[1] = out[2] = out[3] = 0;
+    uint64_t s = seed;
+    auto next = [&]() {
+      s += 0x9E3779B97F4A7C15ull;
+      uint64_t z = s;
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+      return z ^ (z >> 31);
+    };
+    auto bit = [](const std::vector<uint64_t>& v, uint32_t i) { return (uint32_t)((v[i >> 6] >> (i & 63)) & 1); };
+    if (hash_kind == HASH_KECCAK) {
+      const uint32_t K = kr1cs::K;
+      std::vector<uint64_t> z(K / 64), a(K / 64), b(K / 64);
+      uint64_t w[25] = {0};
+      kr1cs::witness_block(w, z.data(), a.data(), b.data());
+      out[3] = z[kr1cs::STATE24_BIT_BASE / 64] == 0xf1258f7940e1dde7ull ? 1 : 0;
+      for (auto& x : w) x = next();
+      std::fill(z.begin(), z.end(), 0); std::fill(a.begin(), a.end(), 0); std::fill(b.begin(), b.end(), 0);
+      kr1cs::witness_block(w, z.data(), a.data(), b.data());
+      std::vector<F128> eq(K);
+      for (auto& e : eq) e = F128(next(), next());
+      std::vector<F128> ca, cb;
+      kr1cs::fold_split(eq.data(), ca, cb);
+      F128 l1, r1, l2, r2;
+      for (uint32_t i = 0; i < K; ++i) {
+        if (bit(a, i)) l1 += eq[i];
+        if (bit(z, i)) r1 += ca[i];
+        if (bit(b, i)) l2 += eq[i];
+        if (bit(z, i)) r2 += cb[i];
+      }
+      out[0] = l1 == r1 ? 0 : 1;
+      out[1] = l2 == r2 ? 0 : 1;
+      for (uint32_t i = 0; i < K; ++i) out[2] += (bit(a, i) & bit(b, i)) != bit(z, i);
+      return 0;
+    }
+    MatrixCache& mc = matrices_for((HashKind)hash_kind);
+    const uint32_t K = mc.a->num_rows;
+    std::vector<uint64_t> z(K / 64), a(K / 64), b(K / 64);
+    if (hash_kind == HASH_BLAKE3) {
+      b3r1cs::Compression c;
+      for (auto& x : c.cv) x = (uint32_t)next();
+      for (auto& x : c.m) x = (uint32_t)next();
+      c.counter = next();
+      c.block_len = 64;
+      c.flags = 11;
+      b3r1cs::witness_block(c, z.data(), a.data(), b.data());
+    } else {
+      s2r1cs::Compression c;
+      for (auto& x : c.h) x = (uint32_t)next();
+      for (auto& x : c.w) x = (uint32_t)next();
+      s2r1cs::witness_block(c, z.data(), a.data(), b.data());
+    }
+    for (uint32_t r = 0; r < K; ++r) {
+      uint32_t pa = 0, pb = 0;
+      for (uint32_t col : mc.a->rows[r]) pa ^= bit(z, col);
+      for (uint32_t col : mc.b->rows[r]) pb ^= bit(z, col);
+      out[0] += pa != bit(a, r);
+      out[1] += pb != bit(b, r);
+      out[2] += (bit(a, r) & bit(b, r)) != bit(z, r);
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+}

@@ -35,3 +35,17 @@ def test_fixture_generator_is_splitmix64():
     # first draws of SplitMix64 from seed 0: the published reference sequence
     # 0xe220a8397b1dcdaf, 0x6e789e6aa1b965f4 (low 32 bits kept)
     assert list(inputs.splitmix_u32(0, 2)) == [0x7B1DCDAF, 0xA1B965F4]
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2])
+@pytest.mark.parametrize("seed", [1, 2])
+def test_block_r1cs_is_satisfied(kind, seed):
+    """a = A z, b = B z (materialised matrices, or the Keccak walker's transpose
+    identity) and a AND b = z on a seeded block of every hash encoder."""
+    lib = oracle.load()
+    out = (ctypes.c_uint64 * 4)()
+    lib.oracle_r1cs_check.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
+    assert lib.oracle_r1cs_check(kind, seed, out) == 0
+    assert list(out)[:3] == [0, 0, 0]
+    if kind == 2:
+        assert out[3] == 1  # Keccak-f[1600] of the zero state, lane 0 = 0xf1258f7940e1dde7
