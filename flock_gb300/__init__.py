@@ -8,9 +8,10 @@ from .bundle import ProofBundle
 from .setups import (BLAKE3_DTYPE, KECCAK_DTYPE, SHA256_DTYPE, SETUPS, Blake3Setup, KeccakSetup,
                      Sha256HybridSetup)
 from . import inputs
+from .serving import ProofServer, prove_batch
 
 __all__ = [
     "BLAKE3", "SHA256", "KECCAK", "FlockError", "NativeLibraryError", "load", "ProofBundle",
     "Blake3Setup", "Sha256HybridSetup", "KeccakSetup", "SETUPS",
-    "BLAKE3_DTYPE", "SHA256_DTYPE", "KECCAK_DTYPE", "inputs",
+    "BLAKE3_DTYPE", "SHA256_DTYPE", "KECCAK_DTYPE", "inputs", "ProofServer", "prove_batch",
 ]

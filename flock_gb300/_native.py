@@ -29,13 +29,28 @@ EXPORTS = (
     "flock_gb300_launch_count",
     "flock_gb300_last_phase_ms",
     "flock_gb300_commit_cap_noalloc",
+    "flock_gb300_prove_batch",
+    "flock_gb300_server_new",
+    "flock_gb300_server_submit",
+    "flock_gb300_server_poll",
+    "flock_gb300_server_free",
     "flock_gb300_free",
     "flock_gb300_device_count",
     "flock_gb300_last_error",
 )
 
 BLAKE3, SHA256, KECCAK = 0, 1, 2
-OK, EINVAL, ECUDA, EINTERNAL = 0, 1, 2, 3
+OK, EINVAL, ECUDA, EINTERNAL, PENDING = 0, 1, 2, 3, 4
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("hash_kind", ctypes.c_int), ("n_blocks", ctypes.c_uint64), ("inputs", ctypes.c_void_p),
+                ("domain", ctypes.c_char_p), ("domain_len", ctypes.c_size_t)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("bundle", ctypes.POINTER(ctypes.c_uint8)), ("bundle_len", ctypes.c_size_t),
+                ("latency_ms", ctypes.c_double)]
 
 
 class NativeLibraryError(RuntimeError):
@@ -102,6 +117,16 @@ def load() -> ctypes.CDLL:
         lib.flock_gb300_commit_cap_noalloc.argtypes = [c.c_int, c.c_void_p, c.c_uint64, c.c_char_p, c.c_size_t,
                                                        c.POINTER(c.c_size_t), c.c_void_p]
         lib.flock_gb300_commit_cap_noalloc.restype = c.c_int
+        lib.flock_gb300_prove_batch.argtypes = [c.POINTER(Request), c.c_size_t, c.c_int, c.c_uint64, c.POINTER(Result)]
+        lib.flock_gb300_prove_batch.restype = c.c_int
+        lib.flock_gb300_server_new.argtypes = [c.c_uint64, c.c_int, c.POINTER(c.c_void_p)]
+        lib.flock_gb300_server_new.restype = c.c_int
+        lib.flock_gb300_server_submit.argtypes = [c.c_void_p, c.POINTER(Request), c.POINTER(c.c_uint64)]
+        lib.flock_gb300_server_submit.restype = c.c_int
+        lib.flock_gb300_server_poll.argtypes = [c.c_void_p, c.c_uint64, c.c_int, c.POINTER(Result)]
+        lib.flock_gb300_server_poll.restype = c.c_int
+        lib.flock_gb300_server_free.argtypes = [c.c_void_p]
+        lib.flock_gb300_server_free.restype = None
         lib.flock_gb300_free.argtypes = [c.POINTER(c.c_uint8)]
         lib.flock_gb300_free.restype = None
         lib.flock_gb300_device_count.argtypes = []

@@ -50,11 +50,12 @@ inline F128 host(F128d v) { return F128(v.lo, v.hi); }
 }  // namespace
 
 template <class T>
-static T* dmalloc(size_t n, std::vector<void*>& owned) {
+static T* dmalloc(size_t n, std::vector<void*>& owned, uint64_t& counter) {
   void* p = nullptr;
   if (n == 0) n = 1;
   CUDA_OK(cudaMalloc(&p, n * sizeof(T)));
   owned.push_back(p);
+  counter += n * sizeof(T);
   return static_cast<T*>(p);
 }
 
@@ -69,6 +70,34 @@ static uint64_t zc_tables_entries(uint32_t L) {
   return total;
 }
 
+// Device bytes a backend for this statement holds after its first prove (the buffers of
+// the constructor, the Ligerito level codewords and trees, the twiddle tables).
+uint64_t GpuBackend::estimate_device_bytes(const Statement& S) {
+  const uint64_t W = uint64_t(1) << (S.m - 7), K = uint64_t(1) << S.k_log, n_pos = uint64_t(1) << S.k_code;
+  uint64_t b = (uint64_t)S.n_blocks * input_record_bytes(S.hash);
+  b += 3 * W * 16;                          // z, a, b
+  b += n_pos * S.lanes * 16 + 2 * n_pos * 32;  // L0 codeword and tree
+  b += (W / 2 * 2 + W * 2 + 64) * 16;       // zerocheck folds
+  b += zc_tables_entries(S.m - 7) * 16;
+  b += 6 * K * 16;                          // lincheck vectors
+  if (S.csc_a) b += 4 * (S.csc_a->col_ptr.size() + S.csc_a->rows_flat.size() + S.csc_b->col_ptr.size() + S.csc_b->rows_flat.size());
+  b += (W + W + W / 2) * 16;                // merged weight and fold buffers
+  b += W * 16 + 4 * (W / 2) * 32 + (W / 2) * 16;  // Ligerito basis, f/b ping-pong, pending
+  b += (uint64_t(1) << 20) * 16 + 4096 * 16 + (size_t(96) << 20) + (size_t(8) << 20);  // partials, scratch, staging
+  b += n_pos * 16;                          // L0 twiddles
+  // recursive levels: codeword 2^(log_cols + rate) x 2^k, tree, twiddles
+  const LigeritoParams& P = S.lig;
+  uint32_t split_dim = (P.log_n - P.initial_k) + 1;
+  for (uint32_t i = 0; i < P.r; ++i) {
+    uint32_t k = P.recursive_ks[i], rate = P.log_inv_rates[i + 1];
+    uint32_t log_cols = split_dim - k;
+    uint64_t bl = uint64_t(1) << (log_cols + rate);
+    b += bl * (uint64_t(1) << k) * 16 + 2 * bl * 32 + bl * 16;
+    split_dim = (split_dim - k) + 1;
+  }
+  return b;
+}
+
 GpuBackend::GpuBackend(const Statement& s) : S(s) {
   CUDA_OK(cudaGetDevice(&device_));
   CUDA_OK(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
@@ -77,61 +106,61 @@ GpuBackend::GpuBackend(const Statement& s) : S(s) {
   K_ = 1u << S.k_log;
   const uint64_t W = W_;
   in_bytes_ = (size_t)S.n_blocks * input_record_bytes(S.hash);
-  d_in_ = dmalloc<uint8_t>(in_bytes_, owned_);
+  d_in_ = dmalloc<uint8_t>(in_bytes_, owned_, device_bytes_);
   CUDA_OK(cudaMallocHost(&h_in_, in_bytes_));
-  z_ = dmalloc<F128d>(W, owned_);
-  a_ = dmalloc<F128d>(W, owned_);
-  b_ = dmalloc<F128d>(W, owned_);
+  z_ = dmalloc<F128d>(W, owned_, device_bytes_);
+  a_ = dmalloc<F128d>(W, owned_, device_bytes_);
+  b_ = dmalloc<F128d>(W, owned_, device_bytes_);
   // chunk columns the witness never writes stay zero for the life of the backend
   CUDA_OK(cudaMemset(z_, 0, W * 16));
   CUDA_OK(cudaMemset(a_, 0, W * 16));
   CUDA_OK(cudaMemset(b_, 0, W * 16));
   n_pos0_ = uint64_t(1) << S.k_code;
-  cw0_ = dmalloc<F128d>(n_pos0_ * S.lanes, owned_);
-  tree0_ = dmalloc<uint8_t>((2 * n_pos0_) * 32, owned_);
+  cw0_ = dmalloc<F128d>(n_pos0_ * S.lanes, owned_, device_bytes_);
+  tree0_ = dmalloc<uint8_t>((2 * n_pos0_) * 32, owned_, device_bytes_);
   // fold buffers: round 2 writes W words per vector (zc2), later rounds alternate (zc1, zc2)
-  zc1a_ = dmalloc<F128d>(W / 2, owned_);
-  zc1b_ = dmalloc<F128d>(W / 2, owned_);
-  zc2a_ = dmalloc<F128d>(W, owned_);
-  zc2b_ = dmalloc<F128d>(W, owned_);
-  zc_w64_ = dmalloc<F128d>(64, owned_);
-  eqi_ = dmalloc<F128d>(K_, owned_);
-  ca_ = dmalloc<F128d>(K_, owned_);
-  cb_ = dmalloc<F128d>(K_, owned_);
-  comb_ = dmalloc<F128d>(K_, owned_);
-  zv_ = dmalloc<F128d>(K_, owned_);
-  zvcap_ = dmalloc<F128d>(K_, owned_);
+  zc1a_ = dmalloc<F128d>(W / 2, owned_, device_bytes_);
+  zc1b_ = dmalloc<F128d>(W / 2, owned_, device_bytes_);
+  zc2a_ = dmalloc<F128d>(W, owned_, device_bytes_);
+  zc2b_ = dmalloc<F128d>(W, owned_, device_bytes_);
+  zc_w64_ = dmalloc<F128d>(64, owned_, device_bytes_);
+  eqi_ = dmalloc<F128d>(K_, owned_, device_bytes_);
+  ca_ = dmalloc<F128d>(K_, owned_, device_bytes_);
+  cb_ = dmalloc<F128d>(K_, owned_, device_bytes_);
+  comb_ = dmalloc<F128d>(K_, owned_, device_bytes_);
+  zv_ = dmalloc<F128d>(K_, owned_, device_bytes_);
+  zvcap_ = dmalloc<F128d>(K_, owned_, device_bytes_);
   if (S.hash != HASH_KECCAK) {
     const Csc& A = *S.csc_a;
     const Csc& B = *S.csc_b;
-    cola_ = dmalloc<uint32_t>(A.col_ptr.size(), owned_);
-    rowa_ = dmalloc<uint32_t>(A.rows_flat.size(), owned_);
-    colb_ = dmalloc<uint32_t>(B.col_ptr.size(), owned_);
-    rowb_ = dmalloc<uint32_t>(B.rows_flat.size(), owned_);
+    cola_ = dmalloc<uint32_t>(A.col_ptr.size(), owned_, device_bytes_);
+    rowa_ = dmalloc<uint32_t>(A.rows_flat.size(), owned_, device_bytes_);
+    colb_ = dmalloc<uint32_t>(B.col_ptr.size(), owned_, device_bytes_);
+    rowb_ = dmalloc<uint32_t>(B.rows_flat.size(), owned_, device_bytes_);
     CUDA_OK(cudaMemcpy(cola_, A.col_ptr.data(), A.col_ptr.size() * 4, cudaMemcpyHostToDevice));
     CUDA_OK(cudaMemcpy(rowa_, A.rows_flat.data(), A.rows_flat.size() * 4, cudaMemcpyHostToDevice));
     CUDA_OK(cudaMemcpy(colb_, B.col_ptr.data(), B.col_ptr.size() * 4, cudaMemcpyHostToDevice));
     CUDA_OK(cudaMemcpy(rowb_, B.rows_flat.data(), B.rows_flat.size() * 4, cudaMemcpyHostToDevice));
   }
-  mw_ = dmalloc<F128d>(W, owned_);
-  moAq_ = dmalloc<F128d>(W / 2, owned_);
-  moAw_ = dmalloc<F128d>(W / 2, owned_);
-  moBq_ = dmalloc<F128d>(W / 4, owned_);
-  moBw_ = dmalloc<F128d>(W / 4, owned_);
-  lb128_ = dmalloc<F128d>(W, owned_);
+  mw_ = dmalloc<F128d>(W, owned_, device_bytes_);
+  moAq_ = dmalloc<F128d>(W / 2, owned_, device_bytes_);
+  moAw_ = dmalloc<F128d>(W / 2, owned_, device_bytes_);
+  moBq_ = dmalloc<F128d>(W / 4, owned_, device_bytes_);
+  moBw_ = dmalloc<F128d>(W / 4, owned_, device_bytes_);
+  lb128_ = dmalloc<F128d>(W, owned_, device_bytes_);
   for (int k = 0; k < 2; ++k) {
-    lf_[k] = dmalloc<F256d>(W / 2, owned_);
-    lb_[k] = dmalloc<F256d>(W / 2, owned_);
+    lf_[k] = dmalloc<F256d>(W / 2, owned_, device_bytes_);
+    lb_[k] = dmalloc<F256d>(W / 2, owned_, device_bytes_);
   }
-  pend_ = dmalloc<F128d>(W / 2, owned_);
+  pend_ = dmalloc<F128d>(W / 2, owned_, device_bytes_);
   part_cap_ = 1u << 20;
-  part_ = dmalloc<F128d>(part_cap_, owned_);
-  red_ = dmalloc<F128d>(4096, owned_);
+  part_ = dmalloc<F128d>(part_cap_, owned_, device_bytes_);
+  red_ = dmalloc<F128d>(4096, owned_, device_bytes_);
   CUDA_OK(cudaMallocHost(&h_red_, 4096 * sizeof(F128d)));
   scr_cap_ = size_t(96) << 20;
-  scr_ = dmalloc<uint8_t>(scr_cap_, owned_);
+  scr_ = dmalloc<uint8_t>(scr_cap_, owned_, device_bytes_);
   stage_cap_ = size_t(8) << 20;
-  d_stage_ = dmalloc<uint8_t>(stage_cap_, owned_);
+  d_stage_ = dmalloc<uint8_t>(stage_cap_, owned_, device_bytes_);
   CUDA_OK(cudaMallocHost(&h_stage_, stage_cap_));
   CUDA_OK(cudaHostAlloc(&h_pub_, 64 * sizeof(F128d), cudaHostAllocMapped));
   CUDA_OK(cudaHostGetDevicePointer(&d_pub_, h_pub_, 0));
@@ -139,9 +168,9 @@ GpuBackend::GpuBackend(const Statement& s) : S(s) {
   CUDA_OK(cudaHostGetDevicePointer(&d_flag_, h_flag_, 0));
   *(volatile uint32_t*)h_flag_ = 0;
   zc_tabs_cap_ = zc_tables_entries(S.m - 7);
-  zc_tabs_ = dmalloc<F128d>(zc_tabs_cap_, owned_);
+  zc_tabs_ = dmalloc<F128d>(zc_tabs_cap_, owned_, device_bytes_);
   CUDA_OK(cudaStreamCreateWithFlags(&pow_st_, cudaStreamNonBlocking));
-  d_pow_ = dmalloc<unsigned long long>(1, owned_);
+  d_pow_ = dmalloc<unsigned long long>(1, owned_, device_bytes_);
   CUDA_OK(cudaMallocHost(&h_pow_, sizeof(unsigned long long)));
   // twiddles of the L0 transform; host tables used by every prove
   tw0_ = twiddles(S.k_code);
@@ -171,6 +200,7 @@ const F128d* GpuBackend::twiddles(uint32_t log_d) {
   auto tw = ntt_twiddles(log_d);
   F128d* d = nullptr;
   CUDA_OK(cudaMalloc(&d, std::max<size_t>(1, tw.size()) * sizeof(F128d)));
+  device_bytes_ += std::max<size_t>(1, tw.size()) * sizeof(F128d);
   CUDA_OK(cudaMemcpy(d, tw.data(), tw.size() * sizeof(F128d), cudaMemcpyHostToDevice));
   tw_[log_d] = d;
   return d;
@@ -740,9 +770,14 @@ void GpuBackend::lg_commit(uint32_t level, uint32_t log_cols, uint32_t log_lanes
   uint64_t block_len = uint64_t(1) << (log_cols + log_rate);
   uint32_t lanes = 1u << log_lanes;
   if (L.block_len != block_len || L.lanes != lanes) {
-    if (L.mat) { cudaFree(L.mat); cudaFree(L.tree); }
+    if (L.mat) {
+      cudaFree(L.mat);
+      cudaFree(L.tree);
+      device_bytes_ -= L.block_len * L.lanes * sizeof(F128d) + 2 * L.block_len * 32;
+    }
     CUDA_OK(cudaMalloc(&L.mat, block_len * lanes * sizeof(F128d)));
     CUDA_OK(cudaMalloc(&L.tree, 2 * block_len * 32));
+    device_bytes_ += block_len * lanes * sizeof(F128d) + 2 * block_len * 32;
     L.block_len = block_len;
     L.lanes = lanes;
   }

@@ -68,6 +68,8 @@ class GpuBackend : public ProverBackend {
   uint64_t d2h_bytes() const { return d2h_; }
 
   cudaStream_t stream() const { return st_; }
+  uint64_t device_bytes() const { return device_bytes_; }
+  static uint64_t estimate_device_bytes(const Statement& S);
   int device() const { return device_; }
   // Device views for tests of single stages.
   const F128d* z() const { return z_; }
@@ -119,6 +121,7 @@ class GpuBackend : public ProverBackend {
   struct Span { int st; cudaEvent_t a, b; uint64_t launches; };
   std::vector<Span> spans_;
   uint64_t h2d_ = 0, d2h_ = 0;
+  uint64_t device_bytes_ = 0;
   const void* d_user_inputs_ = nullptr;
   cudaStream_t st_ = nullptr;
   uint64_t W_ = 0;

@@ -15,9 +15,12 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
+}  // namespace
+
+namespace flock {
 // Statements are shared by every setup of the same (kind, n_blocks): building the
 // matrices and the registry digest is the expensive part of Setup::new.
-std::shared_ptr<Statement> statement_for(HashKind h, uint32_t n) {
+std::shared_ptr<Statement> statement_for_shape(HashKind h, uint32_t n) {
   static std::mutex mu;
   static std::map<std::pair<int, uint32_t>, std::shared_ptr<Statement>> cache;
   std::lock_guard<std::mutex> g(mu);
@@ -29,6 +32,22 @@ std::shared_ptr<Statement> statement_for(HashKind h, uint32_t n) {
   cache[key] = s;
   return s;
 }
+// u64 proof_len | bincode proof | u64 cap_len | cap | ab_value | c_value
+std::vector<uint8_t> make_bundle(const ProveResult& R) {
+  std::vector<uint8_t> pb = proof_bytes(R.proof);
+  std::vector<uint8_t> out;
+  out.reserve(8 + pb.size() + 8 + 32 * R.cap.size() + 32);
+  auto u64 = [&](uint64_t v) { for (int i = 0; i < 8; ++i) out.push_back((uint8_t)(v >> (8 * i))); };
+  u64(pb.size());
+  out.insert(out.end(), pb.begin(), pb.end());
+  u64(R.cap.size());
+  for (auto& h : R.cap) out.insert(out.end(), h.begin(), h.end());
+  for (F128 v : {R.claims.ab_value, R.claims.c_value}) { u64(v.lo); u64(v.hi); }
+  return out;
+}
+}  // namespace flock
+
+namespace {
 
 template <class F>
 int guarded(F&& f) {
@@ -75,7 +94,7 @@ int flock_gb300_setup_new(int hash_kind, uint64_t n_blocks, flock_gb300_setup** 
     return fail(FLOCK_GB300_EINVAL, "n_blocks must be a power of two in [8, 2^24]");
   return guarded([&] {
     auto s = std::make_unique<flock_gb300_setup>();
-    s->stmt = statement_for((HashKind)hash_kind, (uint32_t)n_blocks);
+    s->stmt = statement_for_shape((HashKind)hash_kind, (uint32_t)n_blocks);
     s->backend = std::make_unique<gpu::GpuBackend>(*s->stmt);
     *out = s.release();
     return FLOCK_GB300_OK;
@@ -110,18 +129,11 @@ static int prove_common(flock_gb300_setup* setup, const void* inputs, const void
     setup->backend->begin_prove(d_inputs);
     ProveResult R = prove_fast(*setup->stmt, *setup->backend, static_cast<const uint8_t*>(inputs), domain, domain_len);
     setup->last = R.t;
-    std::vector<uint8_t> pb = proof_bytes(R.proof);
-    size_t len = 8 + pb.size() + 8 + 32 * R.cap.size() + 32;
+    std::vector<uint8_t> bundle = make_bundle(R);
+    size_t len = bundle.size();
     uint8_t* buf = static_cast<uint8_t*>(malloc(len));
     if (!buf) return fail(FLOCK_GB300_EINTERNAL, "out of host memory");
-    size_t o = 0;
-    auto u64 = [&](uint64_t v) { for (int i = 0; i < 8; ++i) buf[o++] = (uint8_t)(v >> (8 * i)); };
-    u64(pb.size());
-    memcpy(buf + o, pb.data(), pb.size());
-    o += pb.size();
-    u64(R.cap.size());
-    for (auto& h : R.cap) { memcpy(buf + o, h.data(), 32); o += 32; }
-    for (F128 v : {R.claims.ab_value, R.claims.c_value}) { u64(v.lo); u64(v.hi); }
+    memcpy(buf, bundle.data(), len);
     *out = buf;
     *out_len = len;
     return FLOCK_GB300_OK;

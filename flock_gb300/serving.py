@@ -1,0 +1,106 @@
+"""Batched and served proving (flock_gb300_prove_batch / flock_gb300_server_*).
+
+Independent proofs run concurrently on the device, each on its own stream and buffers,
+admitted against a device-memory budget; every bundle is byte-identical to the one a
+single ``Setup.prove_fast`` call returns for the same request.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import List, Sequence, Tuple
+
+import numpy as np
+
+from . import _native
+from .bundle import ProofBundle
+from .setups import SETUPS
+
+GiB = 1 << 30
+
+
+@dataclass
+class Outcome:
+    bundle: ProofBundle
+    latency_ms: float
+
+
+def _request(kind: int, recs, domain: bytes, keep: list) -> _native.Request:
+    arr = np.ascontiguousarray(recs)
+    if arr.dtype != SETUPS[kind].DTYPE:
+        raise TypeError(f"inputs for kind {kind} must have dtype {SETUPS[kind].DTYPE}")
+    keep.append(arr)
+    keep.append(domain)
+    return _native.Request(kind, arr.shape[0], arr.ctypes.data, domain, len(domain))
+
+
+def _take(lib, res: _native.Result) -> Outcome:
+    try:
+        blob = ctypes.string_at(res.bundle, res.bundle_len)
+    finally:
+        lib.flock_gb300_free(res.bundle)
+    return Outcome(ProofBundle.parse(blob), res.latency_ms)
+
+
+def prove_batch(requests: Sequence[Tuple[int, np.ndarray, bytes]], workers: int = 8,
+                hbm_budget_bytes: int = 64 * GiB) -> List[Outcome]:
+    """Proves [(kind, records, domain), ...] concurrently; results in request order."""
+    lib = _native.load()
+    keep: list = []
+    n = len(requests)
+    reqs = (_native.Request * n)(*[_request(k, r, d, keep) for k, r, d in requests])
+    results = (_native.Result * n)()
+    rc = lib.flock_gb300_prove_batch(reqs, n, workers, hbm_budget_bytes, results)
+    outs = []
+    for i in range(n):
+        if results[i].status == _native.OK:
+            outs.append(_take(lib, results[i]))
+        else:
+            outs.append(None)
+    _native.check(rc)
+    return outs
+
+
+class ProofServer:
+    """submit() returns a ticket at once; result(ticket) waits for that proof."""
+
+    def __init__(self, hbm_budget_bytes: int = 64 * GiB, workers: int = 8):
+        self._lib = _native.load()
+        h = ctypes.c_void_p()
+        _native.check(self._lib.flock_gb300_server_new(hbm_budget_bytes, workers, ctypes.byref(h)))
+        self._h = h
+
+    def submit(self, kind: int, records: np.ndarray, domain: bytes) -> int:
+        keep: list = []
+        req = _request(kind, records, domain, keep)
+        t = ctypes.c_uint64()
+        _native.check(self._lib.flock_gb300_server_submit(self._h, ctypes.byref(req), ctypes.byref(t)))
+        return t.value
+
+    def result(self, ticket: int, wait_ms: int = -1):
+        """The Outcome of a finished ticket, or None while it runs (wait_ms >= 0)."""
+        res = _native.Result()
+        rc = self._lib.flock_gb300_server_poll(self._h, ticket, wait_ms, ctypes.byref(res))
+        if rc == _native.PENDING:
+            return None
+        _native.check(rc)
+        if res.status != _native.OK:
+            raise _native.FlockError(res.status, self._lib.flock_gb300_last_error().decode())
+        return _take(self._lib, res)
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.flock_gb300_server_free(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass

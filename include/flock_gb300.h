@@ -35,6 +35,7 @@ extern "C" {
 #define FLOCK_GB300_EINVAL 1   /* bad argument: kind, count, sizes, null pointers */
 #define FLOCK_GB300_ECUDA 2    /* a CUDA call failed (message in flock_gb300_last_error) */
 #define FLOCK_GB300_EINTERNAL 3
+#define FLOCK_GB300_PENDING 4  /* flock_gb300_server_poll: not finished yet */
 
 typedef struct flock_gb300_setup flock_gb300_setup;
 
@@ -123,6 +124,42 @@ int flock_gb300_last_phase_ms(const flock_gb300_setup* setup, double out[8]);
  * prove_fast. */
 int flock_gb300_commit_cap_noalloc(int hash_kind, const void* d_inputs, uint64_t n_blocks, uint8_t* cap_out,
                                    size_t cap_out_bytes, size_t* cap_len, void* stream);
+
+/* ---- batched and served proving (no reference counterpart: the reference proves one
+ * statement per call). Independent proofs run concurrently on the device, each on its own
+ * stream and buffers, admitted against a device-memory budget; every bundle is byte-
+ * identical to the one flock_gb300_prove_fast returns for the same request. */
+typedef struct {
+  int hash_kind;
+  uint64_t n_blocks;       /* power of two >= 8 */
+  const void* inputs;      /* n_blocks host records (copied at submission) */
+  const uint8_t* domain;   /* transcript domain bytes */
+  size_t domain_len;
+} flock_gb300_request;
+
+typedef struct {
+  int status;              /* FLOCK_GB300_OK or an error code */
+  uint8_t* bundle;         /* malloc'd proof bundle (release with flock_gb300_free) */
+  size_t bundle_len;
+  double latency_ms;       /* submission to completion */
+} flock_gb300_result;
+
+/* Proves n requests with `workers` concurrent provers within hbm_budget_bytes of device
+ * memory (a request larger than the budget still runs, alone). results[i] answers reqs[i];
+ * returns the first failing status, or 0. */
+int flock_gb300_prove_batch(const flock_gb300_request* reqs, size_t n, int workers, uint64_t hbm_budget_bytes,
+                            flock_gb300_result* results);
+
+/* A serving loop: requests are admitted as workers and memory free up, and proofs that
+ * arrive while others run overlap with them on the device. Provers are cached per
+ * statement shape and evicted least-recently-used when the budget needs room. */
+typedef struct flock_gb300_server flock_gb300_server;
+int flock_gb300_server_new(uint64_t hbm_budget_bytes, int workers, flock_gb300_server** out);
+int flock_gb300_server_submit(flock_gb300_server* server, const flock_gb300_request* req, uint64_t* ticket);
+/* Waits up to wait_ms (< 0: until done) for a ticket. Returns FLOCK_GB300_PENDING while it
+ * runs; once done fills *result (each ticket's result is returned once). */
+int flock_gb300_server_poll(flock_gb300_server* server, uint64_t ticket, int wait_ms, flock_gb300_result* result);
+void flock_gb300_server_free(flock_gb300_server* server);
 
 /* Releases a bundle returned by flock_gb300_prove_fast (cuda-ghash/prove_ffi.cu:417 flock_cuda_free). */
 void flock_gb300_free(uint8_t* p);

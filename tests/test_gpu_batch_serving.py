@@ -1,0 +1,60 @@
+"""Batched and served proving: every bundle equals the one-call prove_fast bundle for the
+same request, alone and in the mix."""
+import random
+
+import pytest
+
+import flock_gb300
+from flock_gb300 import BLAKE3, KECCAK, SHA256, inputs
+
+pytestmark = pytest.mark.gpu
+
+
+def single(kind, n, recs, dom):
+    with flock_gb300.SETUPS[kind](n) as s:
+        return s.prove_fast_bytes(recs, dom)
+
+
+def mixed_requests(count, seed):
+    rng = random.Random(seed)
+    reqs = []
+    for i in range(count):
+        kind = rng.choice([BLAKE3, SHA256, KECCAK])
+        lo = {BLAKE3: 8, SHA256: 7, KECCAK: 6}[kind]
+        n = 1 << rng.randint(lo, lo + 2)
+        reqs.append((kind, inputs.batch(kind, n, 1000 + i), b"mix-%d" % i))
+    return reqs
+
+
+def test_batch_matches_single_proofs():
+    reqs = mixed_requests(10, 7)
+    outs = flock_gb300.prove_batch(reqs, workers=4)
+    for (kind, recs, dom), out in zip(reqs, outs):
+        assert out.bundle.to_bytes() == single(kind, len(recs), recs, dom)
+
+
+def test_batch_under_a_tight_budget_still_matches():
+    reqs = mixed_requests(6, 9)
+    outs = flock_gb300.prove_batch(reqs, workers=3, hbm_budget_bytes=1 << 30)
+    for (kind, recs, dom), out in zip(reqs, outs):
+        assert out.bundle.to_bytes() == single(kind, len(recs), recs, dom)
+
+
+def test_server_results_alone_and_in_the_mix():
+    reqs = mixed_requests(12, 11)
+    with flock_gb300.ProofServer(workers=4) as srv:
+        tickets = [srv.submit(k, r, d) for k, r, d in reqs]
+        outs = [srv.result(t) for t in tickets]
+        # the same request again, alone
+        k, r, d = reqs[3]
+        alone = srv.result(srv.submit(k, r, d))
+    for (kind, recs, dom), out in zip(reqs, outs):
+        assert out.bundle.to_bytes() == single(kind, len(recs), recs, dom)
+        assert out.latency_ms > 0
+    assert alone.bundle.to_bytes() == outs[3].bundle.to_bytes()
+
+
+def test_server_rejects_bad_requests():
+    with flock_gb300.ProofServer(workers=1) as srv:
+        with pytest.raises(flock_gb300.FlockError):
+            srv.submit(BLAKE3, inputs.batch(BLAKE3, 100, 1), b"x")
