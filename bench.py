@@ -363,6 +363,91 @@ def run_gpu(args, world, rank, local):
     return 0
 
 
+def mixed_workload(count: int, seed: int, lo_log: int, hi_log: int):
+    """Seeded mixed requests: hash uniform over the three kinds, batch 2^U(lo..hi) compressions
+    (kept at or above each hash's smallest full-utilisation batch)."""
+    import random
+
+    from flock_gb300 import inputs
+
+    rng = random.Random(seed)
+    out = []
+    floor = {0: 8, 1: 7, 2: 6}
+    for i in range(count):
+        kind = rng.randrange(3)
+        lg = max(floor[kind], int(round(rng.uniform(lo_log, hi_log))))
+        out.append((kind, inputs.batch(kind, 1 << lg, seed * 1000 + i), b"flock-gb300-mixed-%d" % i))
+    return out
+
+
+def run_batched(args):
+    """64 mixed proofs: batched (concurrent provers) against one-proof-at-a-time on the
+    same GPU, identical bundles required."""
+    import flock_gb300
+
+    reqs = mixed_workload(args.count, SEED, 10, args.max_log)
+    hashes = sum(len(r) for _, r, _ in reqs)
+    # plain path: one setup per shape, proofs one after another
+    setups = {}
+    for kind, recs, dom in reqs:
+        setups.setdefault((kind, len(recs)), flock_gb300.SETUPS[kind](len(recs)))
+    for (kind, n), st in setups.items():  # warm-up: device buffers and level twiddles
+        st.prove_fast_bytes(next(r for k, r, _ in reqs if k == kind and len(r) == n), b"warm")
+    t0 = time.perf_counter()
+    plain = [setups[(k, len(r))].prove_fast_bytes(r, d) for k, r, d in reqs]
+    t_plain = time.perf_counter() - t0
+    for st in setups.values():
+        st.close()
+    flock_gb300.prove_batch(reqs[: min(8, len(reqs))], workers=args.workers)  # warm-up
+    t0 = time.perf_counter()
+    outs = flock_gb300.prove_batch(reqs, workers=args.workers)
+    t_batch = time.perf_counter() - t0
+    same = all(o.bundle.to_bytes() == p for o, p in zip(outs, plain))
+    lat = sorted(o.latency_ms for o in outs)
+    line = {"metric": METRIC, "mode": "batched", "value": hashes / t_batch / 1e3, "unit": UNIT,
+            "plain_value": hashes / t_plain / 1e3, "speedup_vs_plain": t_plain / t_batch, "identical_bundles": same,
+            "n_proofs": len(reqs), "hashes": hashes, "workers": args.workers,
+            "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
+            "config": {"workload": f"{len(reqs)} proofs, hash uniform over BLAKE3/SHA-256/Keccak-f, batch 2^U(10..{args.max_log})",
+                       "seed": SEED}, "data": "synthetic (seeded SplitMix64 inputs)", "n_gpus": 1}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_served(args):
+    """Poisson arrivals at --rate proofs/s through the serving loop; p50/p99 latency."""
+    import random
+
+    import flock_gb300
+
+    reqs = mixed_workload(args.count, SEED + 1, 10, args.max_log)
+    rng = random.Random(SEED)
+    hashes = sum(len(r) for _, r, _ in reqs)
+    with flock_gb300.ProofServer(workers=args.workers) as srv:
+        for k, r, d in reqs[:8]:  # warm-up of the provers of the first shapes
+            srv.result(srv.submit(k, r, d))
+        tickets = []
+        t0 = time.perf_counter()
+        t_next = t0
+        for k, r, d in reqs:
+            now = time.perf_counter()
+            if t_next > now:
+                time.sleep(t_next - now)
+            tickets.append(srv.submit(k, r, d))
+            t_next += rng.expovariate(args.rate)
+        outs = [srv.result(t) for t in tickets]
+        t_all = time.perf_counter() - t0
+    lat = sorted(o.latency_ms for o in outs)
+    line = {"metric": METRIC, "mode": "served", "value": hashes / t_all / 1e3, "unit": UNIT,
+            "offered_rate_proofs_per_s": args.rate, "n_proofs": len(reqs), "workers": args.workers,
+            "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                           "max": lat[-1]},
+            "config": {"workload": f"{len(reqs)} Poisson arrivals, hash uniform, batch 2^U(10..{args.max_log})",
+                       "seed": SEED}, "data": "synthetic (seeded SplitMix64 inputs)", "n_gpus": 1}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -372,7 +457,18 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="sha256")
     ap.add_argument("--batch", type=int, default=0, help="override the batch size (parity-test sizes)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", choices=["plain", "batched", "served"], default="plain",
+                    help="plain: the contract line; batched / served: the mixed-workload lines")
+    ap.add_argument("--count", type=int, default=64, help="proofs in the batched / served workload")
+    ap.add_argument("--max-log", type=int, default=16, help="largest batch 2^max_log in the mixed workloads")
+    ap.add_argument("--workers", type=int, default=8)
+    ap.add_argument("--rate", type=float, default=200.0, help="served mode: Poisson arrival rate (proofs/s)")
     args = ap.parse_args()
+    if args.mode != "plain":
+        import __graft_entry__
+
+        __graft_entry__.build()
+        return run_batched(args) if args.mode == "batched" else run_served(args)
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local = dist_init()

@@ -40,6 +40,7 @@ void upload_constants_once() {
     }
     upload_zc_consts(st.ext.data(), reinterpret_cast<const F128d*>(phi8_table().data()), mulk,
                      reinterpret_cast<const F128d*>(wconst));
+    upload_witness_constants();
   });
 }
 
@@ -201,7 +202,10 @@ const F128d* GpuBackend::twiddles(uint32_t log_d) {
   F128d* d = nullptr;
   CUDA_OK(cudaMalloc(&d, std::max<size_t>(1, tw.size()) * sizeof(F128d)));
   device_bytes_ += std::max<size_t>(1, tw.size()) * sizeof(F128d);
-  CUDA_OK(cudaMemcpy(d, tw.data(), tw.size() * sizeof(F128d), cudaMemcpyHostToDevice));
+  // Ordered on this backend's stream: a plain cudaMemcpy from pageable memory may return
+  // before its DMA lands, and kernels on a non-blocking stream are not ordered after it.
+  CUDA_OK(cudaMemcpyAsync(d, tw.data(), tw.size() * sizeof(F128d), cudaMemcpyHostToDevice, st_));
+  CUDA_OK(cudaStreamSynchronize(st_));
   tw_[log_d] = d;
   return d;
 }

@@ -45,6 +45,7 @@ void setup_device(DeviceState& st) {
     CUDA_OK(cudaMemcpy(st.twiddles + (size_t(1) << k), tw.data(), tw.size() * sizeof(F128), cudaMemcpyHostToDevice));
   }
   upload_witness_constants();
+  CUDA_OK(cudaDeviceSynchronize());  // the synchronous copies above may return before their DMA lands
   st.ready = true;
 }
 

@@ -229,6 +229,7 @@ void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t mulk[
   CUDA_OK(cudaMalloc(&d, ZC_CONST_BYTES));
   CUDA_OK(cudaMemset(d, 0, ZC_CONST_BYTES));
   CUDA_OK(cudaMemcpy(d, h, sizeof(ZcConsts), cudaMemcpyHostToDevice));
+  CUDA_OK(cudaDeviceSynchronize());  // complete before any kernel of a non-blocking stream reads it
   delete h;
   g_zc_consts = d;
 }

@@ -10,6 +10,7 @@
 // Per-hash field semantics follow build_group_batch_major:
 //   BLAKE3   blake3.rs:1929-2040      SHA-256  sha2.rs:1743-1850      Keccak  keccak.rs:565-640
 #include "kernels.h"
+#include <mutex>
 #include "../host/r1cs_blake3.h"
 #include "../host/r1cs_sha2.h"
 #include "../host/r1cs_keccak.h"
@@ -346,7 +347,9 @@ __global__ void witness_keccak_kernel(const uint64_t* __restrict__ in, uint32_t 
 
 // ------------------------------------------------------------------------ launchers
 void upload_witness_constants() {
+  static std::mutex mu;
   static bool done = false;
+  std::lock_guard<std::mutex> g(mu);
   if (done) return;
   auto mi = b3r1cs::msg_idx();
   uint8_t idx[7][16];
@@ -361,6 +364,9 @@ void upload_witness_constants() {
   for (int a = 0; a < 5; ++a)
     for (int b = 0; b < 5; ++b) rho[a + 5 * b] = (uint8_t)(kr1cs::RHO[a][b] % 64);
   CUDA_OK(cudaMemcpyToSymbol(KC_RHO, rho, sizeof(rho)));
+  // the copies above may still be in flight when they return; kernels of non-blocking
+  // streams are not ordered after them
+  CUDA_OK(cudaDeviceSynchronize());
   done = true;
 }
 

@@ -58,3 +58,14 @@ def test_server_rejects_bad_requests():
     with flock_gb300.ProofServer(workers=1) as srv:
         with pytest.raises(flock_gb300.FlockError):
             srv.submit(BLAKE3, inputs.batch(BLAKE3, 100, 1), b"x")
+
+
+def test_batch_of_fresh_provers_at_larger_sizes():
+    """Every prover in the batch is new (its first prove allocates and uploads level
+    twiddles while other provers run): the uploads must be ordered on the prover's stream."""
+    reqs = [(SHA256, inputs.batch(SHA256, 1 << 12, 50 + i), b"fresh-%d" % i) for i in range(2)]
+    reqs += [(KECCAK, inputs.batch(KECCAK, 1 << 11, 60 + i), b"fresh-k%d" % i) for i in range(2)]
+    reqs += [(BLAKE3, inputs.batch(BLAKE3, 1 << 12, 70 + i), b"fresh-b%d" % i) for i in range(2)]
+    outs = flock_gb300.prove_batch(reqs, workers=6)
+    for (kind, recs, dom), out in zip(reqs, outs):
+        assert out.bundle.to_bytes() == single(kind, len(recs), recs, dom)
