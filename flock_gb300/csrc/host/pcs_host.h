@@ -243,6 +243,13 @@ inline FrobeniusAssistProof prove_anchor_assist(Transcript& T, const std::vector
     std::vector<std::vector<std::array<F128, 4>>> sfx;   // sfx[l][run] = S_l (state vector), l in 0..L
     std::vector<F128> part;                              // per-run partial weights
     std::array<F128, 4> prefix;
+    // Layers [0, uniform) read the same (c, d) bits for every run (for the aligned layout:
+    // the row bits, all zero). There part[r] = w_r * common and the per-run bucket sum is
+    // common * ws[l], ws[l] = sum_r w_r S_{l+1}(r), precomputed in parallel.
+    int uniform = 0;
+    int ucd = 0;
+    F128 common = F128::one();
+    std::vector<std::array<F128, 4>> ws;
   };
   std::vector<St> S(sts.size());
   for (size_t si = 0; si < sts.size(); ++si) {
@@ -281,6 +288,23 @@ inline FrobeniusAssistProof prove_anchor_assist(Transcript& T, const std::vector
     s.part = a.w;
     s.prefix = {F128(), F128(), F128(), F128()};
     s.prefix[BP_INITIAL] = F128::one();
+    // longest prefix of layers with one (c, d) for every run
+    auto cd_of = [&](size_t r, int l) { return (int)((a.t[r].first >> l) & 1) + 2 * (int)((a.t[r].second >> l) & 1); };
+    while (s.uniform < L && R > 0) {
+      int cd0 = cd_of(0, s.uniform);
+      bool same = true;
+      for (size_t r = 1; r < R && same; ++r) same = cd_of(r, s.uniform) == cd0;
+      if (!same || (s.uniform > 0 && cd0 != s.ucd)) break;
+      s.ucd = cd0;
+      s.uniform++;
+    }
+    s.ws.assign(s.uniform, {F128(), F128(), F128(), F128()});
+    parallel_for((size_t)s.uniform, [&](size_t l) {
+      std::array<F128, 4> acc{};
+      for (size_t r = 0; r < R; ++r)
+        for (int o = 0; o < 4; ++o) acc[o] += a.w[r] * s.sfx[l + 1][r][o];
+      s.ws[l] = acc;
+    });
   }
   FrobeniusAssistProof pf;
   F128 v;
@@ -314,10 +338,14 @@ inline FrobeniusAssistProof prove_anchor_assist(Transcript& T, const std::vector
         B[si][cd] = {F128(), F128(), F128(), F128()};
       }
       const AssistStatement& a = sts[si];
-      for (size_t r = 0; r < a.w.size(); ++r) {
-        int c = (int)((a.t[r].first >> l) & 1), d = (int)((a.t[r].second >> l) & 1);
-        auto& nx = s.sfx[l + 1][r];
-        for (int o = 0; o < 4; ++o) B[si][c + 2 * d][o] += s.part[r] * nx[o];
+      if (l < s.uniform) {
+        for (int o = 0; o < 4; ++o) B[si][s.ucd][o] = s.common * s.ws[l][o];
+      } else {
+        for (size_t r = 0; r < a.w.size(); ++r) {
+          int c = (int)((a.t[r].first >> l) & 1), d = (int)((a.t[r].second >> l) & 1);
+          auto& nx = s.sfx[l + 1][r];
+          for (int o = 0; o < 4; ++o) B[si][c + 2 * d][o] += s.part[r] * nx[o];
+        }
       }
     }
     F128 g1, gi;
@@ -352,9 +380,16 @@ inline FrobeniusAssistProof prove_anchor_assist(Transcript& T, const std::vector
       S[si].prefix = comb4(rd1, folded[si].first, rd, folded[si].second);
       // fold the run partials by the layer's (c, d) bits
       const AssistStatement& a = sts[si];
-      for (size_t r = 0; r < a.w.size(); ++r) {
-        int c = (int)((a.t[r].first >> l) & 1), d = (int)((a.t[r].second >> l) & 1);
-        S[si].part[r] = S[si].part[r] * (c ? rc : rc1) * (d ? rd : rd1);
+      St& s = S[si];
+      if (l < s.uniform) {
+        s.common = s.common * ((s.ucd & 1) ? rc : rc1) * ((s.ucd & 2) ? rd : rd1);
+        if (l + 1 == s.uniform)
+          for (size_t r = 0; r < a.w.size(); ++r) s.part[r] = a.w[r] * s.common;
+      } else {
+        for (size_t r = 0; r < a.w.size(); ++r) {
+          int c = (int)((a.t[r].first >> l) & 1), d = (int)((a.t[r].second >> l) & 1);
+          s.part[r] = s.part[r] * (c ? rc : rc1) * (d ? rd : rd1);
+        }
       }
     }
   }
