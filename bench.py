@@ -76,6 +76,14 @@ def algorithmic_bytes(stage: str, m: int, lanes: int, k_code: int, n: int, kind:
     return table.get(stage)
 
 
+def algorithmic_muls(stage: str, lanes: int, k_code: int) -> float | None:
+    """GF(2^128) products one prove's `stage` must compute (the multiply-bound stages):
+    the additive NTT does one product per butterfly, lanes * 2^(k_code-1) butterflies in
+    each of its k_code - 1 layers (the first layer of the rate-1/2 code is a copy)."""
+    table = {"l0_ntt": lanes * (1 << (k_code - 1)) * (k_code - 1)}
+    return table.get(stage)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
 
@@ -267,8 +275,17 @@ def run_gpu(args, world, rank, local):
     dominant = next((k for k, _ in ranked if algorithmic_bytes(k, setup.m, setup.lanes, setup.log_code_len, n, kind)),
                     ranked[0][0])
 
+    # ---- integer-pipe peak: throughput of the device GF(2^128) product (its own launch)
+    import ctypes
+    mul_peak = ctypes.c_double()
+    flock_gb300._native.check(lib.flock_gb300_f128_mul_rate(256, ctypes.byref(mul_peak)))
+    mul_peak = mul_peak.value
+
     # ---- value: inputs resident in HBM; events only around the roofline stage
     setup.set_stage_timing([dominant])
+    L2_BYTES = 129 << 20
+    working_set = 3 * 16 * (1 << (setup.m - 7))
+    flush = torch.zeros(512 << 18, dtype=torch.int32, device=f"cuda:{local}") if working_set < 2 * L2_BYTES else None
     dom_ms, dom_launches = 0.0, 0
     step_ms = []
     barrier(world)
@@ -279,6 +296,9 @@ def run_gpu(args, world, rank, local):
         ev1 = torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
         for _ in range(args.steps):
+            if flush is not None:  # working set below 2x L2: evict it between steps
+                with torch.cuda.stream(stream):
+                    flush.add_(1)
             s0 = torch.cuda.Event(enable_timing=True)
             s1 = torch.cuda.Event(enable_timing=True)
             s0.record(stream)
@@ -290,11 +310,12 @@ def run_gpu(args, world, rank, local):
             step_ms.append((s0, s1))
         ev1.record(stream)
         torch.cuda.synchronize()
-    launches = lib.flock_gb300_launch_count() - launches0
+    launches = lib.flock_gb300_launch_count() - launches0  # this library's kernels only
     phases = setup.last_phase_ms()
     barrier(world)
-    ms = allmax(world, ev0.elapsed_time(ev1))
     per_step = [a.elapsed_time(b) for a, b in step_ms]
+    # with flushes, the timed region is the sum of the steps (flush kernels excluded)
+    ms = allmax(world, sum(per_step) if flush is not None else ev0.elapsed_time(ev1))
     setup.set_stage_timing(False)
     value = world * n * args.steps / (ms / 1e3) / 1e3
 
@@ -332,6 +353,12 @@ def run_gpu(args, world, rank, local):
                 "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": alg,
                 "launches_per_prove": dom_launches / args.steps, "device_ms_per_prove": per_prove_ms,
                 "peak_source": f"{peak_src} hbm_gbs", "share_of_step": per_prove_ms / (ms / args.steps)}
+        muls = algorithmic_muls(dominant, lanes, setup.log_code_len)
+        if muls:
+            rate = muls / (per_prove_ms / 1e3)
+            roof["mul_pipe"] = {"achieved": rate, "peak": mul_peak, "unit": "F128 mul/s", "frac": rate / mul_peak,
+                                "algorithmic_muls": muls,
+                                "peak_source": "measured live: flock_gb300_f128_mul_rate (chained field.cuh products, full grid)"}
     if rank != 0:
         return 0
 
@@ -345,7 +372,8 @@ def run_gpu(args, world, rank, local):
         "vs_baseline": None, "dtype": "gf2_128", "data": "synthetic (seeded SplitMix64 inputs)",
         "config": {"workload": desc, "hash": wl, "batch": n, "m": m, "lanes": lanes,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "no flush: every step streams z, a, b and the codeword, each larger than L2",
+                   "l2": ("flushed between steps (512 MiB write, outside the step events)" if flush is not None else
+                          "no flush: every step streams z, a, b and the codeword, each larger than L2"),
                    "seed": SEED},
         "latency_ms": {"p50": per_step[len(per_step) // 2], "p99": per_step[min(len(per_step) - 1,
                                                                              int(0.99 * len(per_step)))]},
@@ -398,11 +426,12 @@ def run_batched(args):
     t_plain = time.perf_counter() - t0
     for st in setups.values():
         st.close()
-    flock_gb300.prove_batch(reqs[: min(8, len(reqs))], workers=args.workers)  # warm-up
-    t0 = time.perf_counter()
-    outs = flock_gb300.prove_batch(reqs, workers=args.workers)
-    t_batch = time.perf_counter() - t0
-    same = all(o.bundle.to_bytes() == p for o, p in zip(outs, plain))
+    with flock_gb300.ProofServer(workers=args.workers) as srv:
+        srv.prove_batch(reqs, raw=True)  # warm-up: the server's provers for every shape of the batch
+        t0 = time.perf_counter()
+        outs = srv.prove_batch(reqs, raw=True)
+        t_batch = time.perf_counter() - t0
+    same = all(o.bundle_bytes == p for o, p in zip(outs, plain))
     lat = sorted(o.latency_ms for o in outs)
     line = {"metric": METRIC, "mode": "batched", "value": hashes / t_batch / 1e3, "unit": UNIT,
             "plain_value": hashes / t_plain / 1e3, "speedup_vs_plain": t_plain / t_batch, "identical_bundles": same,

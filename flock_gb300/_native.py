@@ -33,6 +33,8 @@ EXPORTS = (
     "flock_gb300_server_new",
     "flock_gb300_server_submit",
     "flock_gb300_server_poll",
+    "flock_gb300_server_prove_batch",
+    "flock_gb300_f128_mul_rate",
     "flock_gb300_server_free",
     "flock_gb300_free",
     "flock_gb300_device_count",
@@ -125,6 +127,10 @@ def load() -> ctypes.CDLL:
         lib.flock_gb300_server_submit.restype = c.c_int
         lib.flock_gb300_server_poll.argtypes = [c.c_void_p, c.c_uint64, c.c_int, c.POINTER(Result)]
         lib.flock_gb300_server_poll.restype = c.c_int
+        lib.flock_gb300_server_prove_batch.argtypes = [c.c_void_p, c.POINTER(Request), c.c_size_t, c.POINTER(Result)]
+        lib.flock_gb300_server_prove_batch.restype = c.c_int
+        lib.flock_gb300_f128_mul_rate.argtypes = [c.c_int, c.POINTER(c.c_double)]
+        lib.flock_gb300_f128_mul_rate.restype = c.c_int
         lib.flock_gb300_server_free.argtypes = [c.c_void_p]
         lib.flock_gb300_server_free.restype = None
         lib.flock_gb300_free.argtypes = [c.POINTER(c.c_uint8)]

@@ -323,20 +323,23 @@ std::vector<F128> GpuBackend::reduce(uint32_t n_blocks, uint32_t width) {
   d2h_ += width * sizeof(F128d) + sizeof(uint32_t);
   return out;
 }
-// Spin on the published sequence number (the stream keeps running; no synchronisation).
-// A stalled stream is reported after 20 s.
+// Wait for the published sequence number (the stream keeps running; no synchronisation):
+// a short hot spin for the common case of a message a few microseconds away, then a spin
+// that yields the core on every pass, so that concurrent provers' host work (assists,
+// transcripts) is not starved by waiting threads. A stalled stream is reported after 20 s.
 void GpuBackend::wait_published(uint32_t seq) {
   const volatile uint32_t* f = h_flag_;
   uint64_t spins = 0;
   double t0 = 0;
   while (*f != seq) {
-    if ((++spins & 0xFFFF) == 0) {
+    ++spins;
+    if (spins > 2048) std::this_thread::yield();
+    if ((spins & 0x3FFF) == 0) {
       double t = now_ms();
       if (t0 == 0) t0 = t;
       else if (t - t0 > 20000) throw std::runtime_error("device reduction did not publish within 20 s");
       cudaError_t e = cudaStreamQuery(st_);
       if (e != cudaSuccess && e != cudaErrorNotReady) CUDA_OK(e);
-      std::this_thread::yield();
     }
   }
   std::atomic_thread_fence(std::memory_order_acquire);

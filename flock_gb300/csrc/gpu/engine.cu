@@ -248,6 +248,33 @@ void fill_result(const Job& j, flock_gb300_result* out) {
   }
 }
 
+// Submits every request (larger proofs first: the small ones fill in around them) and
+// waits for all; results[i] answers reqs[i].
+int run_batch(Engine& e, const flock_gb300_request* reqs, size_t n, flock_gb300_result* results) {
+  for (size_t i = 0; i < n; ++i)
+    if (check_request(&reqs[i]) != FLOCK_GB300_OK) {
+      set_last_error("invalid request " + std::to_string(i));
+      return FLOCK_GB300_EINVAL;
+    }
+  std::vector<size_t> order(n);
+  for (size_t i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+    return (reqs[x].n_blocks << (2 * reqs[x].hash_kind)) > (reqs[y].n_blocks << (2 * reqs[y].hash_kind));
+  });
+  std::vector<uint64_t> tickets(n);
+  for (size_t i : order) tickets[i] = e.submit(make_job(&reqs[i]));
+  int rc = FLOCK_GB300_OK;
+  for (size_t i = 0; i < n; ++i) {
+    auto j = e.wait(tickets[i], -1);
+    fill_result(*j, &results[i]);
+    if (results[i].status != FLOCK_GB300_OK && rc == FLOCK_GB300_OK) {
+      rc = results[i].status;
+      set_last_error(j->error);
+    }
+  }
+  return rc;
+}
+
 }  // namespace
 
 struct flock_gb300_server {
@@ -259,31 +286,9 @@ extern "C" {
 int flock_gb300_prove_batch(const flock_gb300_request* reqs, size_t n, int workers, uint64_t hbm_budget_bytes,
                             flock_gb300_result* results) {
   if ((!reqs && n) || (!results && n)) return FLOCK_GB300_EINVAL;
-  for (size_t i = 0; i < n; ++i)
-    if (check_request(&reqs[i]) != FLOCK_GB300_OK) {
-      set_last_error("invalid request " + std::to_string(i));
-      return FLOCK_GB300_EINVAL;
-    }
   try {
     Engine e(hbm_budget_bytes, workers);
-    // larger proofs first: the small ones fill in around them
-    std::vector<size_t> order(n);
-    for (size_t i = 0; i < n; ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
-      return (reqs[x].n_blocks << (2 * reqs[x].hash_kind)) > (reqs[y].n_blocks << (2 * reqs[y].hash_kind));
-    });
-    std::vector<uint64_t> tickets(n);
-    for (size_t i : order) tickets[i] = e.submit(make_job(&reqs[i]));
-    int rc = FLOCK_GB300_OK;
-    for (size_t i = 0; i < n; ++i) {
-      auto j = e.wait(tickets[i], -1);
-      fill_result(*j, &results[i]);
-      if (results[i].status != FLOCK_GB300_OK && rc == FLOCK_GB300_OK) {
-        rc = results[i].status;
-        set_last_error(j->error);
-      }
-    }
-    return rc;
+    return run_batch(e, reqs, n, results);
   } catch (const std::exception& ex) {
     set_last_error(ex.what());
     return FLOCK_GB300_ECUDA;
@@ -324,6 +329,17 @@ int flock_gb300_server_poll(flock_gb300_server* s, uint64_t ticket, int wait_ms,
   fill_result(*j, result);
   if (result->status != FLOCK_GB300_OK) set_last_error(j->error);
   return FLOCK_GB300_OK;
+}
+
+int flock_gb300_server_prove_batch(flock_gb300_server* s, const flock_gb300_request* reqs, size_t n,
+                                   flock_gb300_result* results) {
+  if (!s || (!reqs && n) || (!results && n)) return FLOCK_GB300_EINVAL;
+  try {
+    return run_batch(*s->engine, reqs, n, results);
+  } catch (const std::exception& ex) {
+    set_last_error(ex.what());
+    return FLOCK_GB300_ECUDA;
+  }
 }
 
 void flock_gb300_server_free(flock_gb300_server* s) { delete s; }

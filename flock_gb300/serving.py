@@ -25,6 +25,13 @@ class Outcome:
     latency_ms: float
 
 
+@dataclass
+class RawOutcome:
+    """An Outcome whose bundle is left as the wire bytes (no parsing)."""
+    bundle_bytes: bytes
+    latency_ms: float
+
+
 def _request(kind: int, recs, domain: bytes, keep: list) -> _native.Request:
     arr = np.ascontiguousarray(recs)
     if arr.dtype != SETUPS[kind].DTYPE:
@@ -34,31 +41,35 @@ def _request(kind: int, recs, domain: bytes, keep: list) -> _native.Request:
     return _native.Request(kind, arr.shape[0], arr.ctypes.data, domain, len(domain))
 
 
-def _take(lib, res: _native.Result) -> Outcome:
+def _take(lib, res: _native.Result, raw: bool = False):
     try:
         blob = ctypes.string_at(res.bundle, res.bundle_len)
     finally:
         lib.flock_gb300_free(res.bundle)
+    if raw:
+        return RawOutcome(blob, res.latency_ms)
     return Outcome(ProofBundle.parse(blob), res.latency_ms)
 
 
-def prove_batch(requests: Sequence[Tuple[int, np.ndarray, bytes]], workers: int = 8,
-                hbm_budget_bytes: int = 64 * GiB) -> List[Outcome]:
-    """Proves [(kind, records, domain), ...] concurrently; results in request order."""
+def _run_batch(call, requests, raw: bool):
     lib = _native.load()
     keep: list = []
     n = len(requests)
     reqs = (_native.Request * n)(*[_request(k, r, d, keep) for k, r, d in requests])
     results = (_native.Result * n)()
-    rc = lib.flock_gb300_prove_batch(reqs, n, workers, hbm_budget_bytes, results)
-    outs = []
-    for i in range(n):
-        if results[i].status == _native.OK:
-            outs.append(_take(lib, results[i]))
-        else:
-            outs.append(None)
+    rc = call(lib, reqs, n, results)
+    outs = [_take(lib, results[i], raw) if results[i].status == _native.OK else None for i in range(n)]
     _native.check(rc)
     return outs
+
+
+def prove_batch(requests: Sequence[Tuple[int, np.ndarray, bytes]], workers: int = 8,
+                hbm_budget_bytes: int = 64 * GiB, raw: bool = False) -> List[Outcome]:
+    """Proves [(kind, records, domain), ...] concurrently; results in request order. The
+    provers are created for this call and released at its end (ProofServer.prove_batch
+    keeps them)."""
+    return _run_batch(lambda lib, reqs, n, res: lib.flock_gb300_prove_batch(reqs, n, workers, hbm_budget_bytes, res),
+                      requests, raw)
 
 
 class ProofServer:
@@ -87,6 +98,11 @@ class ProofServer:
         if res.status != _native.OK:
             raise _native.FlockError(res.status, self._lib.flock_gb300_last_error().decode())
         return _take(self._lib, res)
+
+    def prove_batch(self, requests: Sequence[Tuple[int, np.ndarray, bytes]], raw: bool = False) -> List[Outcome]:
+        """prove_batch on this server's cached provers."""
+        return _run_batch(lambda lib, reqs, n, res: lib.flock_gb300_server_prove_batch(self._h, reqs, n, res),
+                          requests, raw)
 
     def close(self) -> None:
         if self._h:

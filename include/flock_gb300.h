@@ -159,7 +159,18 @@ int flock_gb300_server_submit(flock_gb300_server* server, const flock_gb300_requ
 /* Waits up to wait_ms (< 0: until done) for a ticket. Returns FLOCK_GB300_PENDING while it
  * runs; once done fills *result (each ticket's result is returned once). */
 int flock_gb300_server_poll(flock_gb300_server* server, uint64_t ticket, int wait_ms, flock_gb300_result* result);
+/* flock_gb300_prove_batch on a server's provers: the provers cached by earlier requests
+ * (device buffers, twiddles, constant tables) are reused, so a steady stream of batches pays
+ * no allocation. May run alongside submit/poll on the same server. */
+int flock_gb300_server_prove_batch(flock_gb300_server* server, const flock_gb300_request* reqs, size_t n,
+                                   flock_gb300_result* results);
 void flock_gb300_server_free(flock_gb300_server* server);
+
+/* Measurement helper (no reference counterpart): products per second of the device
+ * GF(2^128) multiply that the NTT and sumcheck kernels use, from `iters` chained products
+ * per thread on a full grid (about 256 gives a ~10 ms launch). The integer-pipe peak that
+ * the multiply-bound kernels are compared against. Allocates and frees its own buffers. */
+int flock_gb300_f128_mul_rate(int iters, double* muls_per_s);
 
 /* Releases a bundle returned by flock_gb300_prove_fast (cuda-ghash/prove_ffi.cu:417 flock_cuda_free). */
 void flock_gb300_free(uint8_t* p);

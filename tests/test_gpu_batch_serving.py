@@ -69,3 +69,19 @@ def test_batch_of_fresh_provers_at_larger_sizes():
     outs = flock_gb300.prove_batch(reqs, workers=6)
     for (kind, recs, dom), out in zip(reqs, outs):
         assert out.bundle.to_bytes() == single(kind, len(recs), recs, dom)
+
+
+def test_server_batches_reuse_cached_provers():
+    """Two batches on one server: the second runs on the provers the first left cached,
+    alongside a submitted request; every result equals its single prove."""
+    reqs = mixed_requests(8, 13)
+    with flock_gb300.ProofServer(workers=3) as srv:
+        first = srv.prove_batch(reqs, raw=True)
+        k, r, d = reqs[0]
+        ticket = srv.submit(k, r, d)
+        second = srv.prove_batch(reqs[::-1], raw=True)[::-1]
+        extra = srv.result(ticket)
+    for (kind, recs, dom), a, b in zip(reqs, first, second):
+        want = single(kind, len(recs), recs, dom)
+        assert a.bundle_bytes == want and b.bundle_bytes == want
+    assert extra.bundle.to_bytes() == first[0].bundle_bytes
