@@ -31,6 +31,9 @@ def load() -> ctypes.CDLL:
         lib.oracle_registry_digest.restype = c.c_int
         lib.oracle_last_error.restype = c.c_char_p
         lib.oracle_last_phase_ms.argtypes = [c.POINTER(c.c_double)]
+        lib.oracle_verify.argtypes = [c.c_int, c.c_uint64, c.c_char_p, c.c_size_t, c.c_char_p, c.c_size_t,
+                                      c.c_char_p, c.c_size_t]
+        lib.oracle_verify.restype = c.c_int
         _lib = lib
     return _lib
 
@@ -65,3 +68,14 @@ def registry_digest(kind: int, n_blocks: int) -> bytes:
     if lib.oracle_registry_digest(kind, n_blocks, buf) != 0:
         raise RuntimeError(lib.oracle_last_error().decode())
     return buf.raw
+
+
+def verify(kind: int, n_blocks: int, bundle: bytes, domain: bytes) -> tuple:
+    """Replays the transcript of a bundle and checks every relation of the reference
+    verifier (oracle/verifier.h). Returns (accepted, reason)."""
+    lib = load()
+    reason = ctypes.create_string_buffer(256)
+    rc = lib.oracle_verify(kind, n_blocks, bundle, len(bundle), domain, len(domain), reason, 256)
+    if rc == 2:
+        raise RuntimeError(reason.value.decode())
+    return rc == 0, reason.value.decode()

@@ -186,6 +186,26 @@ inline std::vector<F256> fold_ext(const std::vector<F256>& v, F256 r, size_t d) 
   return o;
 }
 
+// Column folds of the lincheck matrices by the row weight eq_inner = skip_w (x) eq(xir)
+// (lincheck.rs:238-281): comb_a = eq_inner^T A_0, comb_b = eq_inner^T B_0 (CSC for
+// BLAKE3 / SHA-256, the walker for Keccak).
+inline void lincheck_combs(const Statement& S, const std::vector<F128>& skip_w, const std::vector<F128>& xir,
+                           std::vector<F128>& comb_a, std::vector<F128>& comb_b) {
+  const uint32_t K = 1u << S.k_log;
+  auto er = build_eq(xir);
+  std::vector<F128> eqi(K);
+  for (uint32_t i = 0; i < K; ++i) eqi[i] = skip_w[i & 63] * er[i >> 6];
+  if (S.hash == HASH_KECCAK) {
+    kr1cs::fold_split(eqi.data(), comb_a, comb_b);
+    return;
+  }
+  comb_a.assign(K, F128()); comb_b.assign(K, F128());
+  for (uint32_t c = 0; c < K; ++c) {
+    for (uint32_t p = S.csc_a->col_ptr[c]; p < S.csc_a->col_ptr[c + 1]; ++p) comb_a[c] += eqi[S.csc_a->rows_flat[p]];
+    for (uint32_t p = S.csc_b->col_ptr[c]; p < S.csc_b->col_ptr[c + 1]; ++p) comb_b[c] += eqi[S.csc_b->rows_flat[p]];
+  }
+}
+
 class CpuBackend : public ProverBackend {
  public:
   explicit CpuBackend(const Statement& s) : S(s) {}
@@ -325,19 +345,7 @@ class CpuBackend : public ProverBackend {
 
   // ---- lincheck
   void lc_comb(const std::vector<F128>& skip_w, const std::vector<F128>& xir) override {
-    const uint32_t K = 1u << S.k_log;
-    auto er = build_eq(xir);
-    std::vector<F128> eqi(K);
-    for (uint32_t i = 0; i < K; ++i) eqi[i] = skip_w[i & 63] * er[i >> 6];
-    if (S.hash == HASH_KECCAK) {
-      kr1cs::fold_split(eqi.data(), comb_a, comb_b);
-      return;
-    }
-    comb_a.assign(K, F128()); comb_b.assign(K, F128());
-    for (uint32_t c = 0; c < K; ++c) {
-      for (uint32_t p = S.csc_a->col_ptr[c]; p < S.csc_a->col_ptr[c + 1]; ++p) comb_a[c] += eqi[S.csc_a->rows_flat[p]];
-      for (uint32_t p = S.csc_b->col_ptr[c]; p < S.csc_b->col_ptr[c + 1]; ++p) comb_b[c] += eqi[S.csc_b->rows_flat[p]];
-    }
+    lincheck_combs(S, skip_w, xir, comb_a, comb_b);
   }
   void lc_zvec(const std::vector<F128>& x_outer) override {
     const uint32_t K = 1u << S.k_log, nu = S.nu;

@@ -6,6 +6,7 @@
 // The bundle format is the one of flock_gb300_prove_fast:
 //   u64 proof_len | bincode proof | u64 cap_len | cap x 32 | ab_value (16) | c_value (16)
 #include "cpu_backend.h"
+#include "verifier.h"
 #include <cstdlib>
 #include <map>
 #include <memory>
@@ -81,6 +82,34 @@ int oracle_prove_fast(int hash_kind, uint64_t n_blocks, const void* inputs, cons
 }
 
 void oracle_free(uint8_t* p) { free(p); }
+
+// Verifies a bundle (the format above) for the statement (hash_kind, n_blocks) and the
+// transcript domain: 0 = accepted, 1 = rejected (the failed check is written to
+// `reason`), 2 = internal error.
+int oracle_verify(int hash_kind, uint64_t n_blocks, const uint8_t* bundle, size_t len, const uint8_t* domain,
+                  size_t domain_len, char* reason, size_t reason_len) {
+  auto say = [&](const std::string& m) {
+    if (reason && reason_len) {
+      size_t n = std::min(reason_len - 1, m.size());
+      memcpy(reason, m.data(), n);
+      reason[n] = 0;
+    }
+  };
+  try {
+    auto s = statement_for(hash_kind, (uint32_t)n_blocks);
+    oracle::Bundle b = oracle::parse_bundle(bundle, len);
+    oracle::verify_bundle(*s, b, domain, domain_len);
+    say("accepted");
+    return 0;
+  } catch (const oracle::Reject& e) {
+    say(e.what());
+    return 1;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    say(std::string("internal error: ") + e.what());
+    return 2;
+  }
+}
 
 // Registry digests of the two small registries pinned by
 // crates/flock-core/src/schedule.rs:1160-1189 (boolean_only_digest_is_byte_identical):
