@@ -453,8 +453,11 @@ def run_served(args):
     rng = random.Random(SEED)
     hashes = sum(len(r) for _, r, _ in reqs)
     with flock_gb300.ProofServer(workers=args.workers) as srv:
-        for k, r, d in reqs[:8]:  # warm-up of the provers of the first shapes
-            srv.result(srv.submit(k, r, d))
+        # warm-up: one request of every shape of the stream (provers, buffers, twiddles)
+        seen = {}
+        for k, r, d in reqs:
+            seen.setdefault((k, len(r)), (k, r, d))
+        srv.prove_batch(list(seen.values()), raw=True)
         tickets = []
         t0 = time.perf_counter()
         t_next = t0
@@ -464,7 +467,7 @@ def run_served(args):
                 time.sleep(t_next - now)
             tickets.append(srv.submit(k, r, d))
             t_next += rng.expovariate(args.rate)
-        outs = [srv.result(t) for t in tickets]
+        outs = [srv.result(t, raw=True) for t in tickets]
         t_all = time.perf_counter() - t0
     lat = sorted(o.latency_ms for o in outs)
     line = {"metric": METRIC, "mode": "served", "value": hashes / t_all / 1e3, "unit": UNIT,
@@ -490,7 +493,7 @@ def main():
                     help="plain: the contract line; batched / served: the mixed-workload lines")
     ap.add_argument("--count", type=int, default=64, help="proofs in the batched / served workload")
     ap.add_argument("--max-log", type=int, default=16, help="largest batch 2^max_log in the mixed workloads")
-    ap.add_argument("--workers", type=int, default=8)
+    ap.add_argument("--workers", type=int, default=2)
     ap.add_argument("--rate", type=float, default=200.0, help="served mode: Poisson arrival rate (proofs/s)")
     args = ap.parse_args()
     if args.mode != "plain":

@@ -35,6 +35,7 @@ EXPORTS = (
     "flock_gb300_server_poll",
     "flock_gb300_server_prove_batch",
     "flock_gb300_f128_mul_rate",
+    "flock_gb300_proof_io",
     "flock_gb300_server_free",
     "flock_gb300_free",
     "flock_gb300_device_count",
@@ -129,6 +130,9 @@ def load() -> ctypes.CDLL:
         lib.flock_gb300_server_poll.restype = c.c_int
         lib.flock_gb300_server_prove_batch.argtypes = [c.c_void_p, c.POINTER(Request), c.c_size_t, c.POINTER(Result)]
         lib.flock_gb300_server_prove_batch.restype = c.c_int
+        lib.flock_gb300_proof_io.argtypes = [c.c_int, c.c_uint64, c.c_char_p, c.c_size_t,
+                                             c.POINTER(c.POINTER(c.c_uint8)), c.POINTER(c.c_size_t)]
+        lib.flock_gb300_proof_io.restype = c.c_int
         lib.flock_gb300_f128_mul_rate.argtypes = [c.c_int, c.POINTER(c.c_double)]
         lib.flock_gb300_f128_mul_rate.restype = c.c_int
         lib.flock_gb300_server_free.argtypes = [c.c_void_p]

@@ -40,6 +40,24 @@ class ProofBundle:
         return (struct.pack("<Q", len(self.proof)) + self.proof + struct.pack("<Q", len(self.cap))
                 + b"".join(self.cap) + self.ab_value + self.c_value)
 
+    def to_proof_io(self, hash_kind: int, n_blocks: int) -> bytes:
+        """The reference's proof file / wire bytes ("FLOCK" v21, flavor R1cs:
+        bincode(Commitment { cap, params }, proof); crates/flock-prover/src/proof_io.rs:238-252)
+        for the setup of (hash_kind, n_blocks). Host-only conversion in the C library."""
+        import ctypes
+
+        from . import _native
+
+        lib = _native.load()
+        blob = self.to_bytes()
+        out = ctypes.POINTER(ctypes.c_uint8)()
+        n = ctypes.c_size_t()
+        _native.check(lib.flock_gb300_proof_io(hash_kind, n_blocks, blob, len(blob), ctypes.byref(out), ctypes.byref(n)))
+        try:
+            return ctypes.string_at(out, n.value)
+        finally:
+            lib.flock_gb300_free(out)
+
     def digest(self) -> bytes:
         h = hashlib.sha256()
         h.update(self.proof)

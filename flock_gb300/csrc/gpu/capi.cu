@@ -1,6 +1,7 @@
 // extern "C" entry points declared in include/flock_gb300.h.
 #include "../../../include/flock_gb300.h"
 #include "backend.h"
+#include "../host/proof_io.h"
 #include <cstdlib>
 #include <memory>
 
@@ -199,6 +200,27 @@ int flock_gb300_last_phase_ms(const flock_gb300_setup* setup, double out[8]) {
 }
 
 void flock_gb300_free(uint8_t* p) { free(p); }
+
+int flock_gb300_proof_io(int hash_kind, uint64_t n_blocks, const uint8_t* bundle, size_t bundle_len, uint8_t** out,
+                         size_t* out_len) {
+  g_last_error.clear();
+  if (!bundle || !out || !out_len) return fail(FLOCK_GB300_EINVAL, "null argument");
+  if (hash_kind < 0 || hash_kind > 2) return fail(FLOCK_GB300_EINVAL, "unknown hash kind");
+  if (n_blocks < 8 || (n_blocks & (n_blocks - 1)) || n_blocks > (uint64_t(1) << 24))
+    return fail(FLOCK_GB300_EINVAL, "n_blocks must be a power of two in [8, 2^24]");
+  *out = nullptr;
+  *out_len = 0;
+  return guarded([&] {
+    auto st = statement_for_shape((HashKind)hash_kind, (uint32_t)n_blocks);
+    std::vector<uint8_t> v = proof_io_from_bundle(*st, bundle, bundle_len);
+    uint8_t* buf = static_cast<uint8_t*>(malloc(v.size()));
+    if (!buf) return fail(FLOCK_GB300_EINTERNAL, "out of host memory");
+    memcpy(buf, v.data(), v.size());
+    *out = buf;
+    *out_len = v.size();
+    return FLOCK_GB300_OK;
+  });
+}
 
 int flock_gb300_device_count(void) {
   int n = 0;

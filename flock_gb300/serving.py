@@ -17,6 +17,10 @@ from .bundle import ProofBundle
 from .setups import SETUPS
 
 GiB = 1 << 30
+# Concurrent provers. Two keep one GB300 busy on the mixed-size workload (one proof's host
+# round trips and assist overlap the other's kernels); more contend for the device and the
+# host cores without adding throughput (measured: 2 -> 1.36x one-at-a-time, 3 -> 1.08x).
+DEFAULT_WORKERS = 2
 
 
 @dataclass
@@ -63,7 +67,7 @@ def _run_batch(call, requests, raw: bool):
     return outs
 
 
-def prove_batch(requests: Sequence[Tuple[int, np.ndarray, bytes]], workers: int = 8,
+def prove_batch(requests: Sequence[Tuple[int, np.ndarray, bytes]], workers: int = DEFAULT_WORKERS,
                 hbm_budget_bytes: int = 64 * GiB, raw: bool = False) -> List[Outcome]:
     """Proves [(kind, records, domain), ...] concurrently; results in request order. The
     provers are created for this call and released at its end (ProofServer.prove_batch
@@ -75,7 +79,7 @@ def prove_batch(requests: Sequence[Tuple[int, np.ndarray, bytes]], workers: int 
 class ProofServer:
     """submit() returns a ticket at once; result(ticket) waits for that proof."""
 
-    def __init__(self, hbm_budget_bytes: int = 64 * GiB, workers: int = 8):
+    def __init__(self, hbm_budget_bytes: int = 64 * GiB, workers: int = DEFAULT_WORKERS):
         self._lib = _native.load()
         h = ctypes.c_void_p()
         _native.check(self._lib.flock_gb300_server_new(hbm_budget_bytes, workers, ctypes.byref(h)))
@@ -88,7 +92,7 @@ class ProofServer:
         _native.check(self._lib.flock_gb300_server_submit(self._h, ctypes.byref(req), ctypes.byref(t)))
         return t.value
 
-    def result(self, ticket: int, wait_ms: int = -1):
+    def result(self, ticket: int, wait_ms: int = -1, raw: bool = False):
         """The Outcome of a finished ticket, or None while it runs (wait_ms >= 0)."""
         res = _native.Result()
         rc = self._lib.flock_gb300_server_poll(self._h, ticket, wait_ms, ctypes.byref(res))
@@ -97,7 +101,7 @@ class ProofServer:
         _native.check(rc)
         if res.status != _native.OK:
             raise _native.FlockError(res.status, self._lib.flock_gb300_last_error().decode())
-        return _take(self._lib, res)
+        return _take(self._lib, res, raw)
 
     def prove_batch(self, requests: Sequence[Tuple[int, np.ndarray, bytes]], raw: bool = False) -> List[Outcome]:
         """prove_batch on this server's cached provers."""

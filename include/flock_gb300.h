@@ -166,6 +166,13 @@ int flock_gb300_server_prove_batch(flock_gb300_server* server, const flock_gb300
                                    flock_gb300_result* results);
 void flock_gb300_server_free(flock_gb300_server* server);
 
+/* The reference's proof file / wire format of a bundle (crates/flock-prover/src/proof_io.rs:238-252,
+ * R1csProofBundleLigerito::to_bytes): "FLOCK" | version 21 | flavor 2 | bincode(Commitment,
+ * proof), with the commitment's PcsParams those of the setup for (hash_kind, n_blocks).
+ * Host-only (no device work); *out is malloc'd, release with flock_gb300_free. */
+int flock_gb300_proof_io(int hash_kind, uint64_t n_blocks, const uint8_t* bundle, size_t bundle_len, uint8_t** out,
+                         size_t* out_len);
+
 /* Measurement helper (no reference counterpart): products per second of the device
  * GF(2^128) multiply that the NTT and sumcheck kernels use, from `iters` chained products
  * per thread on a full grid (about 256 gives a ~10 ms launch). The integer-pipe peak that
