@@ -402,7 +402,7 @@ uint32_t launch_zc_fold2(const F128d* a, const F128d* b, const F128d* w64, F128d
 // and, unless `msg` is false, emit the pair message over the folded vectors:
 //   g1 = sum_j eq(j) A1 B1, ginf = sum_j eq(j) (A0 + A1)(B0 + B1), (A0, A1) = out[2j..2j+2).
 // eq_lo == nullptr means eq = 1. n_pairs = output length / 2 (>= 1).
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
 pair_fold_kernel(const F128d* __restrict__ ain, const F128d* __restrict__ bin, uint64_t n_pairs, F128d r,
                  const F128d* __restrict__ r_dev, const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F128d* __restrict__ eq_hi,
                  F128d* __restrict__ aout, F128d* __restrict__ bout, F128d* __restrict__ part, int msg) {
