@@ -33,28 +33,27 @@ struct F128 {
 };
 static_assert(sizeof(F128) == 16, "F128 is two little-endian u64 words");
 
-// 64x64 -> 128 carry-less product, 4-bit window (software; ~100 integer ops).
+// 32x32 -> 64 carry-less product from sixteen 64-bit integer products of operands thinned
+// to every fourth bit: within one residue class mod 4 a product column collects at most 8
+// partial products, so no carry reaches the next bit of the same class, and the class bits
+// of the integer products are the GF(2) sums. Portable (plain 64-bit multiplies).
+inline uint64_t clmul32(uint32_t x, uint32_t y) {
+  const uint32_t m0 = 0x11111111u, m1 = 0x22222222u, m2 = 0x44444444u, m3 = 0x88888888u;
+  const uint64_t x0 = x & m0, x1 = x & m1, x2 = x & m2, x3 = x & m3;
+  const uint64_t y0 = y & m0, y1 = y & m1, y2 = y & m2, y3 = y & m3;
+  const uint64_t z0 = (x0 * y0) ^ (x1 * y3) ^ (x2 * y2) ^ (x3 * y1);
+  const uint64_t z1 = (x0 * y1) ^ (x1 * y0) ^ (x2 * y3) ^ (x3 * y2);
+  const uint64_t z2 = (x0 * y2) ^ (x1 * y1) ^ (x2 * y0) ^ (x3 * y3);
+  const uint64_t z3 = (x0 * y3) ^ (x1 * y2) ^ (x2 * y1) ^ (x3 * y0);
+  return (z0 & 0x1111111111111111ull) | (z1 & 0x2222222222222222ull) | (z2 & 0x4444444444444444ull) |
+         (z3 & 0x8888888888888888ull);
+}
+// 64x64 -> 128 carry-less product (Karatsuba over 32-bit halves).
 inline void clmul64(uint64_t a, uint64_t b, uint64_t& rlo, uint64_t& rhi) {
-  uint64_t tl[16], th[16];
-  tl[0] = 0; th[0] = 0;
-  tl[1] = a; th[1] = 0;
-  for (int i = 2; i < 16; i += 2) {
-    // even: shift of i/2 by one
-    tl[i] = tl[i >> 1] << 1;
-    th[i] = (th[i >> 1] << 1) | (tl[i >> 1] >> 63);
-    tl[i + 1] = tl[i] ^ a;
-    th[i + 1] = th[i];
-  }
-  uint64_t lo = 0, hi = 0;
-  for (int s = 60; s >= 0; s -= 4) {
-    // shift accumulator left by 4 then add table entry
-    hi = (hi << 4) | (lo >> 60);
-    lo <<= 4;
-    unsigned nib = (unsigned)((b >> s) & 15u);
-    lo ^= tl[nib];
-    hi ^= th[nib];
-  }
-  rlo = lo; rhi = hi;
+  const uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32), b0 = (uint32_t)b, b1 = (uint32_t)(b >> 32);
+  const uint64_t l = clmul32(a0, b0), h = clmul32(a1, b1), m = clmul32(a0 ^ a1, b0 ^ b1) ^ l ^ h;
+  rlo = l ^ (m << 32);
+  rhi = h ^ (m >> 32);
 }
 
 // Reduce a 256-bit product (r0 lowest) modulo x^128 + x^7 + x^2 + x + 1.
