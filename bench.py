@@ -346,11 +346,13 @@ def run_gpu(args, world, rank, local):
         tf = os.path.join(ROOT, "profiles", "traffic.json")
         if os.path.exists(tf):
             try:
-                traffic = json.load(open(tf)).get(wl, {}).get(dominant)
+                traffic = json.load(open(tf)).get(wl, {}).get(dominant) if not args.batch else None
             except Exception:
                 traffic = None
         roof = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": alg,
+                "frac": achieved / peak, "traffic": traffic,
+                "traffic_scope": "DRAM bytes per launch (profiles/traffic.json)" if traffic else None,
+                "algorithmic_bytes_per_launch": alg / max(1.0, dom_launches / args.steps), "algorithmic_bytes": alg,
                 "launches_per_prove": dom_launches / args.steps, "device_ms_per_prove": per_prove_ms,
                 "peak_source": f"{peak_src} hbm_gbs", "share_of_step": per_prove_ms / (ms / args.steps)}
         muls = algorithmic_muls(dominant, lanes, setup.log_code_len)

@@ -177,15 +177,14 @@ struct AlignedJagged {
 };
 
 // sum over boolean c < used of prod_b f_b(c_b), with f_b given as (f_b(0), f_b(1)).
-inline F128 prefix_product_sum(const std::vector<std::pair<F128, F128>>& f, uint64_t used) {
-  int k = (int)f.size();
+inline F128 prefix_product_sum(const std::pair<F128, F128>* f, int k, uint64_t used) {
   if (used >= (uint64_t(1) << k)) {
     F128 p = F128::one();
-    for (auto& q : f) p = p * (q.first + q.second);
+    for (int b = 0; b < k; ++b) p = p * (f[b].first + f[b].second);
     return p;
   }
   // suffix totals of the free low bits
-  std::vector<F128> low_total(k + 1);
+  F128 low_total[65];
   low_total[0] = F128::one();
   for (int b = 0; b < k; ++b) low_total[b + 1] = low_total[b] * (f[b].first + f[b].second);
   F128 acc, high = F128::one();
@@ -198,6 +197,9 @@ inline F128 prefix_product_sum(const std::vector<std::pair<F128, F128>>& f, uint
     }
   }
   return acc;
+}
+inline F128 prefix_product_sum(const std::vector<std::pair<F128, F128>>& f, uint64_t used) {
+  return prefix_product_sum(f.data(), (int)f.size(), used);
 }
 // eq(a, b) for boolean b as field value: (1 + a) or a.
 inline std::pair<F128, F128> eq_pair(F128 a) { return {a + F128::one(), a}; }
@@ -501,7 +503,7 @@ inline MultipointTwistedProof prove_multipoint(Transcript& T, const AlignedJagge
         size_t i = ij / 128, j = ij % 128;
         {
           // column weights: u < b bound to s, u = b the round variable, u > b summed against rho_j
-          std::vector<std::pair<F128, F128>> f0(k), f1(k);
+          std::pair<F128, F128> f0[64], f1[64];
           for (uint32_t u = 0; u < k; ++u) {
             auto ez = eq_pair(claims[i].z_col[u]);
             std::pair<F128, F128> w;
@@ -510,7 +512,7 @@ inline MultipointTwistedProof prove_multipoint(Transcript& T, const AlignedJagge
             if (u == b) { f0[u] = {ez.first, F128()}; f1[u] = {F128(), ez.second}; }
             else { f0[u] = f1[u] = {ez.first * w.first, ez.second * w.second}; }
           }
-          F128 l20 = prefix_product_sum(f0, J.used), l21 = prefix_product_sum(f1, J.used);
+          F128 l20 = prefix_product_sum(f0, (int)k, J.used), l21 = prefix_product_sum(f1, (int)k, J.used);
           F128 c = P[i][j];  // row factors and bound column factors of g already folded in
           c1v[ij] = c * rp[j][n + b] * l21;
           civ[ij] = c * (l20 + l21);

@@ -14,6 +14,7 @@
 //   inner eq-basis open            pcs.rs:214-560
 //   Ligerito F256 ladder           pcs/ligerito/extension.rs:1636-2290
 #pragma once
+#include <future>
 #include "pcs_host.h"
 #include <chrono>
 #include <cstdio>
@@ -310,6 +311,11 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
   F128 g_ab = pg.second[0], g_c = pg.second[1];
   for (auto& v : rs_ab.table) v = v * g_ab;
   for (auto& v : rs_c.table) v = v * g_c;
+  // The assist's linearised fold coefficients depend only on the scaled tables: compute
+  // them on another host thread while the merged sumcheck runs on the backend.
+  auto coeffs = std::async(std::launch::async, [&rs_ab, &rs_c] {
+    return std::make_pair(linearized_coefficients(rs_ab.table), linearized_coefficients(rs_c.table));
+  });
   F128 target = g_ab * rs_ab.sumcheck_claim + g_c * rs_c.sumcheck_claim;
   mo.ring_switches = {rs_ab.proof, rs_c.proof};
   const uint32_t dense_log = S.geo.dense_m - 7;
@@ -338,8 +344,13 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
   }
   // Frobenius multipoint assist on a forked chain, concurrent with the inner open.
   std::vector<RsClaimPoint> fcl(2);
-  fcl[0].z_row = wc[0].z_row; fcl[0].z_col = wc[0].z_col; fcl[0].coeffs = linearized_coefficients(rs_ab.table);
-  fcl[1].z_row = wc[1].z_row; fcl[1].z_col = wc[1].z_col; fcl[1].coeffs = linearized_coefficients(rs_c.table);
+  {
+    auto cf = coeffs.get();
+    fcl[0].coeffs = std::move(cf.first);
+    fcl[1].coeffs = std::move(cf.second);
+  }
+  fcl[0].z_row = wc[0].z_row; fcl[0].z_col = wc[0].z_col;
+  fcl[1].z_row = wc[1].z_row; fcl[1].z_col = wc[1].z_col;
   Transcript ch_a = T.fork("flock-par-assist-v1");
   double assist_ms = 0;
   std::thread assist([&] {
