@@ -125,7 +125,7 @@ __device__ __forceinline__ uint32_t gf8_mul4(uint32_t a, uint32_t b) {
 // after the constants are staged. Per row x = 8M + K the team extends the a and b rows
 // (8 byte-table lookups each), multiplies pointwise in GF(2^8) and accumulates e_K * p
 // into g_M; then F = sum_M x^M phi8(g_M) (Horner) and acc += eq_o(xo) * F.
-constexpr int ZC_TEAMS = 24;  // teams per block (384 threads)
+constexpr int ZC_TEAMS = 32;  // teams per block (512 threads)
 __global__ void __launch_bounds__(16 * ZC_TEAMS, 1)
 zc_round1_ab_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, uint64_t n_xo,
                     const ZcConsts* __restrict__ gconst, const F128d* __restrict__ eq_lo, uint32_t lo_bits,
@@ -187,34 +187,58 @@ zc_round1_ab_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, ui
   for (int k = 0; k < 4; ++k) part[row * 64 + 4 * lane + k] = acc[k];
 }
 
-// s_hat_v_c: per xo the 64 word weights eq_o(xo) * x^M * phi8(e2[K2]) (one multiply each),
-// then thread t XORs the weights of the words whose bit t is set.
+// s_hat_v_c[t] = sum_xo eq_o(xo) sum_w wconst[w] bit_t(z[64 xo + w]). The word constants
+// and the eq_hi factor are applied once per eq_hi chunk, not per xo:
+//   part[t] = sum_chunks eq_hi(chunk) * sum_{w in group} wconst[w] * U[w][t],
+//   U[w][t] = sum_{xo in chunk} eq_lo(xo) bit_t(z[64 xo + w]),
+// so the inner loop is a masked XOR per (xo, word, bit) and no multiply. Block = 128
+// threads (one per bit t) x one group of 8 words (blockIdx.y) x a run of xo_per_block
+// consecutive xo (blockIdx.x); runs and chunks are powers of two.
+constexpr uint32_t SVC_WORDS = 8;
+constexpr uint32_t SVC_TILE = 32;  // xo staged in shared memory per step
 __global__ void __launch_bounds__(128)
-zc_svc_kernel(const F128d* __restrict__ z, uint64_t n_xo, const ZcConsts* __restrict__ gconst,
+zc_svc_kernel(const F128d* __restrict__ z, uint64_t xo_per_block, const ZcConsts* __restrict__ gconst,
               const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F128d* __restrict__ eq_hi,
               F128d* __restrict__ part) {
-  __shared__ F128d wc[64], wt[64];
-  __shared__ F128d wz[64];
-  const uint32_t t = threadIdx.x;
-  if (t < 64) wc[t] = gconst->wconst[t];
+  __shared__ uint4 zt[SVC_TILE * SVC_WORDS];
+  __shared__ F128d et[SVC_TILE];
+  const uint32_t t = threadIdx.x, limb = t >> 5, sh = 31 - (t & 31);
+  const uint32_t g = blockIdx.y;
+  const uint64_t xo0 = (uint64_t)blockIdx.x * xo_per_block;
+  const uint64_t chunk = 1ull << lo_bits;
+  const uint64_t seg = xo_per_block < chunk ? xo_per_block : chunk;
+  const uint32_t tile = seg < SVC_TILE ? (uint32_t)seg : SVC_TILE;
+  const F128d* wc = gconst->wconst + g * SVC_WORDS;
+  const uint4* z4 = reinterpret_cast<const uint4*>(z);
   F128d acc = f128_zero();
-  const uint32_t limb = t >> 6, sh = t & 63;
-  for (uint64_t xo = blockIdx.x; xo < n_xo; xo += gridDim.x) {
-    __syncthreads();
-    if (t < 64) {
-      wt[t] = eq_at(eq_lo, lo_bits, eq_hi, xo) * wc[t];
-      wz[t] = z[xo * 64 + t];
+  for (uint64_t s0 = xo0; s0 < xo0 + xo_per_block; s0 += seg) {
+    F128d U[SVC_WORDS];
+#pragma unroll
+    for (uint32_t w = 0; w < SVC_WORDS; ++w) U[w] = f128_zero();
+    for (uint64_t xt = s0; xt < s0 + seg; xt += tile) {
+      __syncthreads();
+      for (uint32_t i = t; i < tile * SVC_WORDS; i += blockDim.x)
+        zt[i] = z4[(xt + (i / SVC_WORDS)) * 64 + g * SVC_WORDS + (i % SVC_WORDS)];
+      if (t < tile) et[t] = eq_lo[(xt + t) & (chunk - 1)];
+      __syncthreads();
+      for (uint32_t x = 0; x < tile; ++x) {
+        const F128d e = et[x];
+        const uint32_t* row = reinterpret_cast<const uint32_t*>(zt + x * SVC_WORDS);
+#pragma unroll
+        for (uint32_t w = 0; w < SVC_WORDS; ++w) {
+          const uint32_t word = row[4 * w + limb];
+          const uint64_t m = (uint64_t)(int64_t)((int32_t)(word << sh) >> 31);  // all ones iff bit t is set
+          U[w].lo ^= e.lo & m;
+          U[w].hi ^= e.hi & m;
+        }
+      }
     }
-    __syncthreads();
-#pragma unroll 8
-    for (int w = 0; w < 64; ++w) {
-      uint64_t bits = limb ? wz[w].hi : wz[w].lo;
-      uint64_t m = 0ull - ((bits >> sh) & 1);
-      acc.lo ^= wt[w].lo & m;
-      acc.hi ^= wt[w].hi & m;
-    }
+    F128d v = f128_zero();
+#pragma unroll
+    for (uint32_t w = 0; w < SVC_WORDS; ++w) v += wc[w] * U[w];
+    acc += eq_hi ? eq_hi[s0 >> lo_bits] * v : v;
   }
-  part[(uint64_t)blockIdx.x * 128 + t] = acc;
+  part[((uint64_t)blockIdx.y * gridDim.x + blockIdx.x) * 128 + t] = acc;
 }
 
 static ZcConsts* g_zc_consts = nullptr;
@@ -249,10 +273,13 @@ void launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32_t m
   zc_round1_ab_kernel<<<blocks, 16 * ZC_TEAMS, smem, s>>>(a, b, n_xo, g_zc_consts, eq_lo, lo_bits, eq_hi, part_ab);
   LAUNCH_OK();
   *nrows_ab = blocks * ZC_TEAMS;
-  uint32_t sblocks = (uint32_t)std::min<uint64_t>(n_xo, (uint64_t)sm_count() * 8);
-  zc_svc_kernel<<<sblocks, 128, 0, s>>>(z, n_xo, g_zc_consts, eq_lo, lo_bits, eq_hi, part_svc);
+  // at most 256 runs of xo per word group (n_xo and the chunks are powers of two)
+  const uint64_t runs = std::min<uint64_t>(n_xo, 256);
+  const uint64_t run = n_xo / runs;
+  zc_svc_kernel<<<dim3((uint32_t)runs, 64 / SVC_WORDS), 128, 0, s>>>(z, run, g_zc_consts, eq_lo, lo_bits, eq_hi,
+                                                                   part_svc);
   LAUNCH_OK();
-  *nrows_svc = sblocks;
+  *nrows_svc = (uint32_t)(runs * (64 / SVC_WORDS));
 }
 
 // ------------------------------------------------------------------ zerocheck skip fold
