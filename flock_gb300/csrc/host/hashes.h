@@ -76,21 +76,23 @@ struct Sha256 {
     if (n) { memcpy(buf, p, n); blen = (uint32_t)n; }
   }
 
-  // Finalize a COPY (the state stays usable).
+  // Finalize a COPY (the state stays usable): 0x80, zeros to 56 mod 64, the bit length.
   std::array<uint8_t, 32> digest() const {
-    Sha256 c = *this;
-    uint64_t bits = c.total * 8;
-    uint8_t pad = 0x80;
-    c.update(&pad, 1);
-    uint8_t z = 0;
-    while (c.blen != 56) c.update(&z, 1);
-    uint8_t L[8];
-    for (int i = 0; i < 8; ++i) L[i] = (uint8_t)(bits >> (56 - 8 * i));
-    c.update(L, 8);
+    uint32_t st[8];
+    memcpy(st, h, sizeof(st));
+    uint8_t blk[128];
+    memcpy(blk, buf, blen);
+    const uint32_t end = blen < 56 ? 64 : 128;
+    memset(blk + blen, 0, end - blen);
+    blk[blen] = 0x80;
+    const uint64_t bits = total * 8;
+    for (int i = 0; i < 8; ++i) blk[end - 8 + i] = (uint8_t)(bits >> (56 - 8 * i));
+    compress(st, blk);
+    if (end == 128) compress(st, blk + 64);
     std::array<uint8_t, 32> out;
     for (int i = 0; i < 8; ++i) {
-      out[4 * i] = (uint8_t)(c.h[i] >> 24); out[4 * i + 1] = (uint8_t)(c.h[i] >> 16);
-      out[4 * i + 2] = (uint8_t)(c.h[i] >> 8); out[4 * i + 3] = (uint8_t)c.h[i];
+      out[4 * i] = (uint8_t)(st[i] >> 24); out[4 * i + 1] = (uint8_t)(st[i] >> 16);
+      out[4 * i + 2] = (uint8_t)(st[i] >> 8); out[4 * i + 3] = (uint8_t)st[i];
     }
     return out;
   }

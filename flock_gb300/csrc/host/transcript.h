@@ -49,14 +49,36 @@ inline bool has_leading_zero_bits(const uint8_t* h, uint32_t bits) {
 // default is a sequential host scan. The contract is the SMALLEST satisfying nonce.
 using PowSearchFn = std::function<uint64_t(const std::array<uint8_t, 32>& digest, uint32_t bits)>;
 
-inline uint64_t pow_search_host(const std::array<uint8_t, 32>& digest, uint32_t bits) {
-  uint8_t pre[40];
-  memcpy(pre, digest.data(), 32);
-  for (uint64_t nonce = 0;; ++nonce) {
-    for (int i = 0; i < 8; ++i) pre[32 + i] = (uint8_t)(nonce >> (8 * i));
-    auto h = Sha256::hash(pre, 40);
-    if (has_leading_zero_bits(h.data(), bits)) return nonce;
+// SHA256(digest || nonce_le) is one padded 64-byte block: build it once, then per nonce
+// rewrite the 8 nonce bytes and run a single compression.
+struct PowBlock {
+  uint8_t blk[64];
+  explicit PowBlock(const std::array<uint8_t, 32>& digest) {
+    memcpy(blk, digest.data(), 32);
+    memset(blk + 32, 0, 32);
+    blk[40] = 0x80;
+    blk[62] = 0x01;  // 320 bits, big-endian
+    blk[63] = 0x40;
   }
+  // leading-zero test of SHA256(digest || nonce) on the big-endian state words
+  bool meets(uint64_t nonce, uint32_t bits) {
+    for (int i = 0; i < 8; ++i) blk[32 + i] = (uint8_t)(nonce >> (8 * i));
+    uint32_t st[8];
+    memcpy(st, Sha256::IV, sizeof(st));
+    Sha256::compress(st, blk);
+    for (uint32_t w = 0; bits; ++w) {
+      const uint32_t take = bits < 32 ? bits : 32;
+      if (st[w] >> (32 - take)) return false;
+      bits -= take;
+    }
+    return true;
+  }
+};
+
+inline uint64_t pow_search_host(const std::array<uint8_t, 32>& digest, uint32_t bits) {
+  PowBlock pb(digest);
+  for (uint64_t nonce = 0;; ++nonce)
+    if (pb.meets(nonce, bits)) return nonce;
 }
 
 class Transcript {
@@ -135,11 +157,7 @@ class Transcript {
     if (bits == 0) {
       ok = nonce == 0;
     } else {
-      uint8_t pre[40];
-      memcpy(pre, digest.data(), 32);
-      for (int i = 0; i < 8; ++i) pre[32 + i] = (uint8_t)(nonce >> (8 * i));
-      auto h = Sha256::hash(pre, 40);
-      ok = has_leading_zero_bits(h.data(), bits);
+      ok = bits <= 256 && PowBlock(digest).meets(nonce, bits);
     }
     uint8_t le[8];
     for (int i = 0; i < 8; ++i) le[i] = (uint8_t)(nonce >> (8 * i));
