@@ -168,6 +168,8 @@ GpuBackend::GpuBackend(const Statement& s) : S(s) {
   CUDA_OK(cudaHostAlloc(&h_flag_, 64, cudaHostAllocMapped));
   CUDA_OK(cudaHostGetDevicePointer(&d_flag_, h_flag_, 0));
   *(volatile uint32_t*)h_flag_ = 0;
+  pub_counter_ = dmalloc<uint32_t>(1, owned_, device_bytes_);
+  CUDA_OK(cudaMemsetAsync(pub_counter_, 0, sizeof(uint32_t), st_));
   zc_tabs_cap_ = zc_tables_entries(S.m - 7);
   zc_tabs_ = dmalloc<F128d>(zc_tabs_cap_, owned_, device_bytes_);
   CUDA_OK(cudaStreamCreateWithFlags(&pow_st_, cudaStreamNonBlocking));
@@ -316,6 +318,9 @@ std::vector<F128> GpuBackend::reduce(uint32_t n_blocks, uint32_t width) {
   // round messages: one block reduces and publishes into mapped host memory
   uint32_t seq = ++seq_;
   launch_reduce_publish(part_, n_blocks, width, d_pub_, d_flag_, seq, st_);
+  return read_published(seq, width);
+}
+std::vector<F128> GpuBackend::read_published(uint32_t seq, uint32_t width) {
   wait_published(seq);
   std::vector<F128> out(width);
   const volatile F128d* p = h_pub_;
@@ -525,7 +530,7 @@ void GpuBackend::zc_fold(F128 rho, const std::vector<F128>& eq_point, F128& g1, 
   // round 0 writes W words per vector into zc2; later rounds alternate zc1 <-> zc2
   F128d* oa = (zc_round_ == 0 || zc_cur_a_ == zc1a_) ? zc2a_ : zc1a_;
   F128d* ob = (zc_round_ == 0 || zc_cur_a_ == zc1a_) ? zc2b_ : zc1b_;
-  uint32_t nb;
+  uint32_t nb, pub_seq = 0;
   {
     Mark mk(this, ST_ZC_FOLDS);
     if (zc_round_ == 0) {
@@ -533,11 +538,14 @@ void GpuBackend::zc_fold(F128 rho, const std::vector<F128>& eq_point, F128& g1, 
       nb = launch_zc_fold2(a_, b_, zc_w64_, dev(rho), tabs, n_pairs, zc_tabs_ + lo.out_off, lo.n, zc_tabs_ + hi.out_off,
                            oa, ob, part_, st_);
     } else {
-      nb = launch_pair_fold(zc_cur_a_, zc_cur_b_, n_pairs, dev(rho), nullptr, zc_tabs_ + lo.out_off, lo.n,
-                            zc_tabs_ + hi.out_off, oa, ob, part_, true, st_);
+      FusedPublish fp = fused_publish();
+      launch_pair_fold(zc_cur_a_, zc_cur_b_, n_pairs, dev(rho), nullptr, zc_tabs_ + lo.out_off, lo.n,
+                       zc_tabs_ + hi.out_off, oa, ob, part_, true, st_, fp);
+      nb = 0;
+      pub_seq = fp.seq;
     }
   }
-  auto v = reduce(nb, 2);
+  auto v = pub_seq ? read_published(pub_seq, 2) : reduce(nb, 2);
   g1 = v[0];
   gi = v[1];
   zc_cur_a_ = oa;
@@ -677,16 +685,17 @@ void GpuBackend::mo_round(F128 r, bool last, F128& g1, F128& gi) {
   F128d* ow = (mo_q_ == moAq_) ? moBw_ : moAw_;
   uint64_t n_pairs = mo_len_ / 4;
   uint32_t chunk_bits = std::min<uint32_t>(10, ceil_log2(n_pairs));  // chunking only sets the work split
-  uint32_t nb;
+  FusedPublish fp;
+  if (!last) fp = fused_publish();
   {
     Mark mk(this, ST_MO_ROUNDS);
-    nb = launch_pair_fold(mo_q_, mo_w_, n_pairs, dev(r), nullptr, nullptr, chunk_bits, nullptr, oq, ow, part_, !last, st_);
+    launch_pair_fold(mo_q_, mo_w_, n_pairs, dev(r), nullptr, nullptr, chunk_bits, nullptr, oq, ow, part_, !last, st_, fp);
   }
   mo_q_ = oq;
   mo_w_ = ow;
   mo_len_ /= 2;
   if (!last) {
-    auto v = reduce(nb, 2);
+    auto v = read_published(fp.seq, 2);
     g1 = v[0];
     gi = v[1];
   }

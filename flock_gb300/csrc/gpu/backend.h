@@ -172,6 +172,9 @@ class GpuBackend : public ProverBackend {
   uint32_t* d_flag_ = nullptr;
   uint32_t seq_ = 0;
   void wait_published(uint32_t seq);
+  std::vector<F128> read_published(uint32_t seq, uint32_t width);
+  uint32_t* pub_counter_ = nullptr;  // ticket counter of in-kernel publication (device)
+  FusedPublish fused_publish() { FusedPublish p; p.out = d_pub_; p.flag = d_flag_; p.counter = pub_counter_; p.seq = ++seq_; return p; }
   // eq tables of every zerocheck fold round, built once from the skip-fold point
   F128d* zc_tabs_ = nullptr;
   uint64_t zc_tabs_cap_ = 0;

@@ -66,10 +66,20 @@ uint32_t launch_zc_fold_skip(const F128d* a, const F128d* b, const F128d* w64, u
 uint32_t launch_zc_fold2(const F128d* a, const F128d* b, const F128d* w64, F128d rho, F128d* tabs, uint64_t n_pairs,
                          const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* aout, F128d* bout, F128d* part,
                          cudaStream_t s);                                                              // width 2
+// In-kernel publication of a round message: the last block to finish (a device-wide
+// ticket counter) XOR-reduces every block's partials, writes the message to mapped host
+// memory and then the sequence number, as launch_reduce_publish does in a launch of its
+// own. counter must be zero before the launch; the last block resets it.
+struct FusedPublish {
+  F128d* out = nullptr;        // mapped host memory (null: no publication)
+  uint32_t* flag = nullptr;    // mapped host memory
+  uint32_t* counter = nullptr; // device memory
+  uint32_t seq = 0;
+};
 // r_dev (when not null) is the device address of the challenge, read by the kernel.
 uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, F128d r, const F128d* r_dev,
                           const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* aout, F128d* bout,
-                          F128d* part, bool msg, cudaStream_t s);                                      // width 2
+                          F128d* part, bool msg, cudaStream_t s, FusedPublish pub = FusedPublish());  // width 2
 
 void launch_lc_eq_inner(const F128d* w64, const F128d* er, uint32_t K, F128d* eqi, cudaStream_t s);
 void launch_csc_fold(const uint32_t* col_ptr, const uint32_t* rows, uint32_t K, const F128d* eqi, F128d* out,

@@ -424,6 +424,40 @@ uint32_t launch_zc_fold2(const F128d* a, const F128d* b, const F128d* w64, F128d
   return blocks;
 }
 
+// ------------------------------------------------------------------ fused publication
+// Called by every block after thread 0 stored its `width` partials at part[block * width]:
+// the block takes a ticket; the block that takes the last one reduces all partials (the
+// other blocks' stores are visible to it after their fences and the atomic), writes the
+// message to mapped memory, then the sequence number, and resets the counter.
+__device__ void publish_if_last(const F128d* part, uint32_t width, const FusedPublish& pub, F128d* sh) {
+  __shared__ uint32_t ticket;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    ticket = atomicAdd(pub.counter, 1u);
+  }
+  __syncthreads();
+  if (ticket != gridDim.x - 1) return;
+  __threadfence();
+  for (uint32_t j = 0; j < width; ++j) {
+    F128d acc = f128_zero();
+    for (uint32_t b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+      const F128d* p = part + (uint64_t)b * width + j;
+      acc += f128(__ldcg(&p->lo), __ldcg(&p->hi));
+    }
+    acc = block_xor(acc, sh);
+    if (threadIdx.x == 0) {
+      volatile F128d* o = pub.out;
+      o[j].lo = acc.lo;
+      o[j].hi = acc.hi;
+    }
+  }
+  if (threadIdx.x == 0) {
+    *pub.counter = 0;
+    __threadfence_system();
+    *(volatile uint32_t*)pub.flag = pub.seq;
+  }
+}
+
 // ------------------------------------------------------------------ pair fold + message
 // Fold the low variable of two vectors at r (out[i] = in[2i] + r (in[2i+1] + in[2i]))
 // and, unless `msg` is false, emit the pair message over the folded vectors:
@@ -432,7 +466,7 @@ uint32_t launch_zc_fold2(const F128d* a, const F128d* b, const F128d* w64, F128d
 __global__ void __launch_bounds__(256, 2)
 pair_fold_kernel(const F128d* __restrict__ ain, const F128d* __restrict__ bin, uint64_t n_pairs, F128d r,
                  const F128d* __restrict__ r_dev, const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F128d* __restrict__ eq_hi,
-                 F128d* __restrict__ aout, F128d* __restrict__ bout, F128d* __restrict__ part, int msg) {
+                 F128d* __restrict__ aout, F128d* __restrict__ bout, F128d* __restrict__ part, int msg, FusedPublish pub) {
   __shared__ F128d sh[32];
   if (r_dev) r = *r_dev;
   const uint64_t chunk = 1ull << lo_bits;
@@ -470,14 +504,15 @@ pair_fold_kernel(const F128d* __restrict__ ain, const F128d* __restrict__ bin, u
     }
   }
   if (msg && threadIdx.x == 0) { part[blockIdx.x * 2] = G1; part[blockIdx.x * 2 + 1] = GI; }
+  if (msg && pub.out) publish_if_last(part, 2, pub, sh);
 }
 uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, F128d r, const F128d* r_dev,
                           const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* aout, F128d* bout,
-                          F128d* part, bool msg, cudaStream_t s) {
+                          F128d* part, bool msg, cudaStream_t s, FusedPublish pub) {
   uint64_t n_chunks = (n_pairs + (1ull << lo_bits) - 1) >> lo_bits;
   uint32_t blocks = (uint32_t)std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 8);
   pair_fold_kernel<<<blocks, 256, 0, s>>>(ain, bin, n_pairs, r, r_dev, eq_lo, lo_bits, eq_hi, aout, bout, part,
-                                          msg ? 1 : 0);
+                                          msg ? 1 : 0, pub);
   LAUNCH_OK();
   return blocks;
 }
