@@ -14,9 +14,17 @@ namespace gpu {
 
 namespace {
 
-std::once_flag g_consts_once;
+// Constant tables are per device (module constants and cudaMalloc'd tables live in each
+// device's context); a process may drive several devices.
+std::mutex g_consts_mu;
+bool g_consts_done[MAX_DEVICES] = {};
 void upload_constants_once() {
-  std::call_once(g_consts_once, [] {
+  int dev = 0;
+  CUDA_OK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= MAX_DEVICES) throw std::runtime_error("device index out of range");
+  std::lock_guard<std::mutex> g(g_consts_mu);
+  if (g_consts_done[dev]) return;
+  [] {
     const SkipTables& st = skip_tables();
     // eq factor of the three small zerocheck constants (bit j of K selects c_j or 1 + c_j)
     const uint8_t c[3] = {0xF7, 0x53, 0xB5};
@@ -41,7 +49,8 @@ void upload_constants_once() {
     upload_zc_consts(st.ext.data(), reinterpret_cast<const F128d*>(phi8_table().data()), mulk,
                      reinterpret_cast<const F128d*>(wconst));
     upload_witness_constants();
-  });
+  }();
+  g_consts_done[dev] = true;
 }
 
 inline F128d dev(F128 v) { F128d r; r.lo = v.lo; r.hi = v.hi; return r; }

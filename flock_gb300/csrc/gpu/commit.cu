@@ -123,12 +123,7 @@ void launch_ntt(F128d* data, uint32_t lanes, uint32_t log_d, uint32_t start_laye
       uint64_t n_groups = 1ull << (log_d - NL);
       uint64_t lane_tiles = (lanes + lane_tile - 1) / lane_tile;
       size_t smem = (size_t)(1u << NL) * lane_tile * sizeof(F128d);
-      static bool attr = false;
-      if (!attr) {
-        CUDA_OK(cudaFuncSetAttribute(ntt_fused_kernel<NL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)((1u << NL) * 64 * sizeof(F128d))));
-        attr = true;
-      }
+      set_dynamic_smem((const void*)ntt_fused_kernel<NL>, (int)((1u << NL) * 64 * sizeof(F128d)));
       ntt_fused_kernel<NL><<<(unsigned)(n_groups * lane_tiles), 256, smem, s>>>(data, lanes, log_d, layer, tw,
                                                                                  lane_tile);
       LAUNCH_OK();

@@ -24,6 +24,10 @@ namespace gpu {
 // Kernel launches made by this library (all threads); read through flock_gb300_launch_count.
 uint64_t launch_count();
 void note_launch();
+constexpr int MAX_DEVICES = 64;
+// Raises `kernel`'s dynamic shared-memory limit to `bytes` on the current device, once per
+// (kernel, device, size); thread-safe (provers on several threads launch the same kernels).
+void set_dynamic_smem(const void* kernel, int bytes);
 #define LAUNCH_OK()                    \
   do {                                 \
     CUDA_OK(cudaGetLastError());       \

@@ -30,7 +30,6 @@ struct DeviceState {
   uint8_t* scratch = nullptr;
   F128d* twiddles = nullptr;
 };
-constexpr int MAX_DEVICES = 64;
 DeviceState g_state[MAX_DEVICES];
 std::mutex g_mu[MAX_DEVICES];
 

@@ -10,6 +10,9 @@
 // consecutive indices, summing lo-weighted terms and multiplying by hi once per chunk.
 #include "kernels.h"
 #include <atomic>
+#include <mutex>
+#include <set>
+#include <tuple>
 
 namespace flock {
 namespace gpu {
@@ -69,14 +72,30 @@ static std::atomic<uint64_t> g_launches{0};
 uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
-static int g_sm_count = 0;
+static int current_device() {
+  int dev = 0;
+  CUDA_OK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= MAX_DEVICES) throw std::runtime_error("device index out of range");
+  return dev;
+}
 int sm_count() {
-  if (!g_sm_count) {
-    int dev = 0;
-    CUDA_OK(cudaGetDevice(&dev));
-    CUDA_OK(cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev));
+  static std::atomic<int> cache[MAX_DEVICES];
+  const int dev = current_device();
+  int n = cache[dev].load(std::memory_order_relaxed);
+  if (!n) {
+    CUDA_OK(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+    cache[dev].store(n, std::memory_order_relaxed);
   }
-  return g_sm_count;
+  return n;
+}
+void set_dynamic_smem(const void* kernel, int bytes) {
+  static std::mutex mu;
+  static std::set<std::tuple<const void*, int, int>> done;
+  const auto key = std::make_tuple(kernel, current_device(), bytes);
+  std::lock_guard<std::mutex> g(mu);
+  if (done.count(key)) return;
+  CUDA_OK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  done.insert(key);
 }
 
 // ------------------------------------------------------------------ zerocheck round 1
@@ -241,9 +260,11 @@ zc_svc_kernel(const F128d* __restrict__ z, uint64_t xo_per_block, const ZcConsts
   part[((uint64_t)blockIdx.y * gridDim.x + blockIdx.x) * 128 + t] = acc;
 }
 
-static ZcConsts* g_zc_consts = nullptr;
+static ZcConsts* g_zc_consts_dev[MAX_DEVICES] = {};  // written under the caller's lock, before any prover launches
+static ZcConsts* zc_consts() { return g_zc_consts_dev[current_device()]; }
 void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t mulk[8][256], const F128d* wconst) {
-  if (g_zc_consts) return;
+  const int dev = current_device();
+  if (g_zc_consts_dev[dev]) return;
   ZcConsts* h = new ZcConsts();
   memcpy(h->ext, ext, sizeof(h->ext));
   memcpy(h->phi8, phi8, sizeof(h->phi8));
@@ -255,20 +276,17 @@ void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t mulk[
   CUDA_OK(cudaMemcpy(d, h, sizeof(ZcConsts), cudaMemcpyHostToDevice));
   CUDA_OK(cudaDeviceSynchronize());  // complete before any kernel of a non-blocking stream reads it
   delete h;
-  g_zc_consts = d;
+  g_zc_consts_dev[dev] = d;
 }
 
 void launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32_t m, const F128d* eq_lo, uint32_t lo_bits,
                       const F128d* eq_hi, F128d* part_ab, uint32_t* nrows_ab, F128d* part_svc, uint32_t* nrows_svc,
                       cudaStream_t s) {
+  ZcConsts* g_zc_consts = zc_consts();
   if (!g_zc_consts) throw std::runtime_error("zerocheck constants not uploaded");
   uint64_t n_xo = 1ull << (m - 13);
   size_t smem = ZC_CONST_BYTES;
-  static bool attr = false;
-  if (!attr) {
-    CUDA_OK(cudaFuncSetAttribute(zc_round1_ab_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  set_dynamic_smem((const void*)zc_round1_ab_kernel, (int)smem);
   uint32_t blocks = (uint32_t)std::min<uint64_t>((n_xo + ZC_TEAMS - 1) / ZC_TEAMS, (uint64_t)sm_count());
   zc_round1_ab_kernel<<<blocks, 16 * ZC_TEAMS, smem, s>>>(a, b, n_xo, g_zc_consts, eq_lo, lo_bits, eq_hi, part_ab);
   LAUNCH_OK();
@@ -412,11 +430,7 @@ uint32_t launch_zc_fold2(const F128d* a, const F128d* b, const F128d* w64, F128d
                          cudaStream_t s) {
   zc_scaled_tables_kernel<<<16, 256, 0, s>>>(w64, rho, tabs);
   LAUNCH_OK();
-  static bool attr = false;
-  if (!attr) {
-    CUDA_OK(cudaFuncSetAttribute(zc_fold2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 4096 * 16));
-    attr = true;
-  }
+  set_dynamic_smem((const void*)zc_fold2_kernel, 4096 * 16);
   uint64_t n_chunks = (n_pairs + (1ull << lo_bits) - 1) >> lo_bits;
   uint32_t blocks = (uint32_t)std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 3);
   zc_fold2_kernel<<<blocks, 256, 4096 * 16, s>>>(a, b, tabs, n_pairs, eq_lo, lo_bits, eq_hi, aout, bout, part);
@@ -747,11 +761,7 @@ uint32_t launch_mo_build_w(const F128d* q, const F128d* er0, const F128d* ec0, c
                            const F128d* tables, uint32_t nu, uint64_t area, uint64_t n, F128d* w, F128d* part,
                            cudaStream_t s) {
   size_t smem = 2 * 16 * 256 * sizeof(F128d);
-  static bool attr = false;
-  if (!attr) {
-    CUDA_OK(cudaFuncSetAttribute(mo_build_w_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  set_dynamic_smem((const void*)mo_build_w_kernel, (int)smem);
   uint32_t blocks = (uint32_t)std::min<uint64_t>((n / 2 + 511) / 512, (uint64_t)sm_count());
   mo_build_w_kernel<<<blocks, 512, smem, s>>>(q, er0, ec0, er1, ec1, tables, nu, area, n, w, part);
   LAUNCH_OK();

@@ -347,10 +347,14 @@ __global__ void witness_keccak_kernel(const uint64_t* __restrict__ in, uint32_t 
 
 // ------------------------------------------------------------------------ launchers
 void upload_witness_constants() {
+  // module constants are per device
   static std::mutex mu;
-  static bool done = false;
+  static bool done[MAX_DEVICES] = {};
+  int dev = 0;
+  CUDA_OK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= MAX_DEVICES) throw std::runtime_error("device index out of range");
   std::lock_guard<std::mutex> g(mu);
-  if (done) return;
+  if (done[dev]) return;
   auto mi = b3r1cs::msg_idx();
   uint8_t idx[7][16];
   for (int r = 0; r < 7; ++r)
@@ -367,7 +371,7 @@ void upload_witness_constants() {
   // the copies above may still be in flight when they return; kernels of non-blocking
   // streams are not ordered after them
   CUDA_OK(cudaDeviceSynchronize());
-  done = true;
+  done[dev] = true;
 }
 
 void launch_witness(int hash, const void* d_inputs, uint32_t n_inst, uint32_t nu, F128d* z, F128d* a, F128d* b,
