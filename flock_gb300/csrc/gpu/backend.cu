@@ -253,6 +253,7 @@ GpuBackend::Mark::~Mark() {
   }
 }
 void GpuBackend::begin_prove(const void* d_inputs) {
+  lg_pend_fold_.active = false;
   d_user_inputs_ = d_inputs;
   h2d_ = d2h_ = 0;
   spans_.clear();
@@ -717,6 +718,7 @@ F128 GpuBackend::mo_q_eval() {
 
 // ------------------------------------------------------------------ Ligerito
 void GpuBackend::lg_basis_eq(F128 gamma, const std::vector<F128>& rho) {
+  lg_flush_fold();
   scr_off_ = 0;
   if ((uint64_t(1) << rho.size()) != W_) throw std::runtime_error("Ligerito basis size mismatch");
   EqSplit e = eq_split(rho, gamma, 10);
@@ -727,6 +729,7 @@ void GpuBackend::lg_basis_eq(F128 gamma, const std::vector<F128>& rho) {
 }
 
 F128 GpuBackend::lg_eval_eq(const std::vector<F128>& zp) {
+  lg_flush_fold();
   scr_off_ = 0;
   if (!lg_base_) throw std::runtime_error("OOD evaluation expects the committed base vector");
   EqSplit e = eq_split(zp, F128::one(), 10);
@@ -736,6 +739,7 @@ F128 GpuBackend::lg_eval_eq(const std::vector<F128>& zp) {
 }
 
 void GpuBackend::lg_add_eq(F128 beta, const std::vector<F128>& zp) {
+  lg_flush_fold();
   scr_off_ = 0;
   if (!lg_base_) throw std::runtime_error("basis update expects the base stage");
   EqSplit e = eq_split(zp, beta, 10);
@@ -743,6 +747,26 @@ void GpuBackend::lg_add_eq(F128 beta, const std::vector<F128>& zp) {
 }
 
 Msg256 GpuBackend::lg_message(size_t d) {
+  if (lg_pend_fold_.active) {
+    // fold and message in one pass over the F256 vectors
+    const uint64_t n_out = lg_n_ / 2;
+    const size_t dm = (d == 1 || n_out == d) ? 1 : d;
+    const int nx = lg_cur_ ^ 1;
+    uint32_t nb;
+    {
+      Mark mk(this, ST_LIGERITO);
+      nb = launch_lg_fold_msg256(lf_[lg_cur_], lb_[lg_cur_], n_out, dev(lg_pend_fold_.r), lg_pend_fold_.d, dm, lf_[nx],
+                                 lb_[nx], part_, st_);
+    }
+    lg_pend_fold_.active = false;
+    lg_cur_ = nx;
+    lg_n_ = n_out;
+    auto v = reduce(nb, 4);
+    Msg256 m;
+    m.u0 = F256(v[0], v[1]);
+    m.u2 = F256(v[2], v[3]);
+    return m;
+  }
   uint64_t n = lg_n_;
   if (d == 1 || n == d) d = 1;
   Msg256 m;
@@ -762,7 +786,28 @@ Msg256 GpuBackend::lg_message(size_t d) {
   return m;
 }
 
+void GpuBackend::lg_flush_fold() {
+  if (!lg_pend_fold_.active) return;
+  lg_pend_fold_.active = false;
+  const uint64_t n_out = lg_n_ / 2;
+  const int nx = lg_cur_ ^ 1;
+  {
+    Mark mk(this, ST_LIGERITO);
+    launch_lg_fold256(lf_[lg_cur_], lb_[lg_cur_], n_out, dev(lg_pend_fold_.r), nullptr, lg_pend_fold_.d, lf_[nx], lb_[nx],
+                      st_);
+  }
+  lg_cur_ = nx;
+  lg_n_ = n_out;
+}
+
 void GpuBackend::lg_fold(F256 r, size_t d) {
+  lg_flush_fold();
+  if (!lg_base_) {
+    lg_pend_fold_.active = true;
+    lg_pend_fold_.r = r;
+    lg_pend_fold_.d = d;
+    return;
+  }
   uint64_t n_out = lg_n_ / 2;
   Mark mk(this, ST_LIGERITO);
   if (lg_base_) {
@@ -778,6 +823,7 @@ void GpuBackend::lg_fold(F256 r, size_t d) {
 }
 
 void GpuBackend::lg_code_switch() {
+  lg_flush_fold();
   if (lg_base_) throw std::runtime_error("code switch before the first fold");
   if (2 * lg_n_ > W_ / 2) throw std::runtime_error("code switch exceeds the Ligerito buffers");
   int nx = lg_cur_ ^ 1;
@@ -789,6 +835,7 @@ void GpuBackend::lg_code_switch() {
 
 void GpuBackend::lg_commit(uint32_t level, uint32_t log_cols, uint32_t log_lanes, uint32_t log_rate,
                            uint32_t cap_depth, std::vector<Hash>& cap) {
+  lg_flush_fold();
   if (lg_n_ != (uint64_t(1) << (log_cols + log_lanes))) throw std::runtime_error("Ligerito commit size mismatch");
   if (levels_.size() < level + 1) levels_.resize(level + 1);
   Level& L = levels_[level];
@@ -814,6 +861,7 @@ void GpuBackend::lg_commit(uint32_t level, uint32_t log_cols, uint32_t log_lanes
 }
 
 Msg256 GpuBackend::lg_introduce_eq(const std::vector<F128>& zp, F128& answer) {
+  lg_flush_fold();
   scr_off_ = 0;
   if ((uint64_t(1) << zp.size()) != lg_n_) throw std::runtime_error("OOD point size mismatch");
   EqSplit e = eq_split(zp, F128::one(), 10);
@@ -831,6 +879,7 @@ Msg256 GpuBackend::lg_introduce_eq(const std::vector<F128>& zp, F128& answer) {
 
 Msg256 GpuBackend::lg_introduce_induced(uint32_t ln, uint32_t log_rate, const std::vector<uint64_t>& pos,
                                         const std::vector<F128>& w, const std::vector<std::vector<F128>>&) {
+  lg_flush_fold();
   scr_off_ = 0;
   if ((uint64_t(2) << ln) != lg_n_) throw std::runtime_error("induced basis size mismatch");
   if (pos.size() != w.size()) throw std::runtime_error("induced basis: one weight per position");
@@ -857,12 +906,14 @@ Msg256 GpuBackend::lg_introduce_induced(uint32_t ln, uint32_t log_rate, const st
 }
 
 void GpuBackend::lg_glue(F128 beta) {
+  lg_flush_fold();
   Mark mk(this, ST_LIGERITO);
   launch_lg_glue(lb_[lg_cur_], pend_, dev(beta), pend_n_, pend_induced_, st_);
 }
 
 void GpuBackend::lg_open(uint32_t level, const std::vector<uint64_t>& pos, uint32_t cap_depth,
                          std::vector<std::vector<F128>>& rows, std::vector<Hash>& paths) {
+  lg_flush_fold();
   scr_off_ = 0;
   const F128d* mat;
   const uint8_t* tree;
@@ -895,6 +946,7 @@ void GpuBackend::lg_open(uint32_t level, const std::vector<uint64_t>& pos, uint3
 }
 
 std::vector<F256> GpuBackend::lg_residual() {
+  lg_flush_fold();
   std::vector<F256> out(lg_n_);
   CUDA_OK(cudaMemcpyAsync(out.data(), lf_[lg_cur_], lg_n_ * sizeof(F256d), cudaMemcpyDeviceToHost, st_));
   d2h_ += lg_n_ * sizeof(F256d);

@@ -159,6 +159,15 @@ class GpuBackend : public ProverBackend {
   F256d* lb_[2] = {nullptr, nullptr};
   int lg_cur_ = 0;
   bool lg_base_ = true;
+  // An F256 fold is held back until the next call: a message over the folded vectors then
+  // runs fused with it (one pass); any other call first performs it on its own.
+  struct PendingFold {
+    bool active = false;
+    F256 r;
+    size_t d = 0;
+  };
+  PendingFold lg_pend_fold_;
+  void lg_flush_fold();
   uint64_t lg_n_ = 0;
   F128d* pend_ = nullptr;
   bool pend_induced_ = false;

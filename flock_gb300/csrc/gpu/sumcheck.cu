@@ -887,6 +887,51 @@ void launch_lg_fold256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, 
   lg_fold256_kernel<<<(unsigned)((n_out + 255) / 256), 256, 0, s>>>(f, b, n_out, r, r_dev, d, fo, bo);
   LAUNCH_OK();
 }
+// One round's fold (at r, pairs d_fold apart) fused with the next round's message over the
+// folded vectors (pairs d_msg apart): each thread folds the two outputs of one message pair,
+// stores them, and accumulates u0 = sum f0 b0, u2 = sum (f0 + f1)(b0 + b1) over them. Same
+// index maps as lg_fold256_kernel and lg_message256_kernel; one pass instead of two.
+// An out-of-line F256 product: the fused kernel holds six of them per iteration, and
+// inlining them all exhausts the register file.
+__device__ __noinline__ F256d f256_mul_call(F256d a, F256d b) { return a * b; }
+__device__ __forceinline__ void lg_fold_at(const F256d* __restrict__ f, const F256d* __restrict__ b, F256d r, uint64_t d,
+                                        uint64_t i, F256d& fi, F256d& bi) {
+  const uint64_t blk = i / d, k = i - blk * d, lo = 2 * blk * d + k, hi = lo + d;
+  const F256d f0 = f[lo], b0 = b[lo];
+  fi = f0 + f256_mul_call(r, f[hi] + f0);
+  bi = b0 + f256_mul_call(r, b[hi] + b0);
+}
+__global__ void __launch_bounds__(256)
+lg_fold_msg256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n_out, F256d r,
+                      uint64_t d_fold, uint64_t d_msg, F256d* __restrict__ fo, F256d* __restrict__ bo,
+                      F128d* __restrict__ part) {
+  __shared__ F128d sh[32];
+  F256d u0 = f256(f128_zero(), f128_zero()), u2 = u0;
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_out / 2; p += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t mb = p / d_msg, mk = p - mb * d_msg, olo = 2 * mb * d_msg + mk, ohi = olo + d_msg;
+    F256d fl, bl, fh, bh;
+    lg_fold_at(f, b, r, d_fold, olo, fl, bl);
+    fo[olo] = fl;
+    bo[olo] = bl;
+    u0 += f256_mul_call(fl, bl);
+    lg_fold_at(f, b, r, d_fold, ohi, fh, bh);
+    fo[ohi] = fh;
+    bo[ohi] = bh;
+    u2 += f256_mul_call(fl + fh, bl + bh);
+  }
+  F128d r0 = block_xor(u0.c0, sh), r1 = block_xor(u0.c1, sh), r2 = block_xor(u2.c0, sh), r3 = block_xor(u2.c1, sh);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x * 4] = r0; part[blockIdx.x * 4 + 1] = r1;
+    part[blockIdx.x * 4 + 2] = r2; part[blockIdx.x * 4 + 3] = r3;
+  }
+}
+uint32_t launch_lg_fold_msg256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, uint64_t d_fold, uint64_t d_msg,
+                               F256d* fo, F256d* bo, F128d* part, cudaStream_t s) {
+  uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n_out / 2 + 255) / 256, (uint64_t)sm_count() * 8));
+  lg_fold_msg256_kernel<<<blocks, 256, 0, s>>>(f, b, n_out, r, d_fold, d_msg, fo, bo, part);
+  LAUNCH_OK();
+  return blocks;
+}
 // f' = (f.c0, f.c1) interleaved as base values; b' = (b, u b).
 __global__ void lg_code_switch_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n,
                                       F256d* __restrict__ fo, F256d* __restrict__ bo) {
