@@ -71,6 +71,10 @@ __device__ __forceinline__ F128d mul(F128d a, F128d b) {
   return ghash_reduce(l0, l1 ^ m0, h0 ^ m1, h1);
 }
 __device__ __forceinline__ F128d operator*(F128d a, F128d b) { return mul(a, b); }
+// The same product out of line: kernels that hold several products in flight per
+// iteration (the sumcheck folds) spill or lose occupancy when every product is inlined;
+// a call keeps one product's temporaries live at a time.
+__device__ __noinline__ static F128d mul_call(F128d a, F128d b) { return mul(a, b); }
 
 __device__ __forceinline__ F128d mul_by_x(F128d z) {
   uint64_t mask = 0ull - (z.hi >> 63);
@@ -91,6 +95,8 @@ __device__ __forceinline__ F256d operator*(F256d a, F256d b) {
   return f256(p0 + mul_by_x_inv(p1), p2 + p0);
 }
 __device__ __forceinline__ F256d operator*(F256d a, F128d b) { return f256(a.c0 * b, a.c1 * b); }
+// Out-of-line F256 product (see mul_call).
+__device__ __noinline__ static F256d f256_mul_call(F256d a, F256d b) { return a * b; }
 
 // ---- warp / block XOR reductions
 __device__ __forceinline__ F128d warp_xor(F128d v) {

@@ -198,7 +198,7 @@ zc_round1_ab_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, ui
       F128d F = f128_zero();
 #pragma unroll
       for (int M = 15; M >= 0; --M) F = mul_by_x(F) + C.phi8[(G[M] >> (8 * k)) & 255];
-      acc[k] += e * F;
+      acc[k] += mul_call(e, F);
     }
   }
   uint64_t row = (uint64_t)blockIdx.x * ZC_TEAMS + team;
@@ -336,8 +336,8 @@ zc_fold_skip_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, co
         b1 += T[c][(bv.hi >> (8 * c)) & 255];
       }
       F128d e = eq_lo[wi & (chunk - 1)];
-      g1 += e * (a1 * b1);
-      gi += e * ((a0 + a1) * (b0 + b1));
+      g1 += mul_call(e, mul_call(a1, b1));
+      gi += mul_call(e, mul_call(a0 + a1, b0 + b1));
     }
     g1 = block_xor(g1, sh);
     gi = block_xor(gi, sh);
@@ -412,8 +412,8 @@ zc_fold2_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, const 
       aout[2 * j] = A[0]; aout[2 * j + 1] = A[1];
       bout[2 * j] = B[0]; bout[2 * j + 1] = B[1];
       F128d e = eq_lo[j & (chunk - 1)];
-      g1 += e * (A[1] * B[1]);
-      gi += e * ((A[0] + A[1]) * (B[0] + B[1]));
+      g1 += mul_call(e, mul_call(A[1], B[1]));
+      gi += mul_call(e, mul_call(A[0] + A[1], B[0] + B[1]));
     }
     g1 = block_xor(g1, sh);
     gi = block_xor(gi, sh);
@@ -492,16 +492,16 @@ pair_fold_kernel(const F128d* __restrict__ ain, const F128d* __restrict__ bin, u
     for (uint64_t j = ch * chunk + threadIdx.x; j < end; j += blockDim.x) {
       F128d x0 = ain[4 * j], x1 = ain[4 * j + 1], x2 = ain[4 * j + 2], x3 = ain[4 * j + 3];
       F128d y0 = bin[4 * j], y1 = bin[4 * j + 1], y2 = bin[4 * j + 2], y3 = bin[4 * j + 3];
-      F128d A0 = x0 + r * (x1 + x0), A1 = x2 + r * (x3 + x2);
-      F128d B0 = y0 + r * (y1 + y0), B1 = y2 + r * (y3 + y2);
+      F128d A0 = x0 + mul_call(r, x1 + x0), A1 = x2 + mul_call(r, x3 + x2);
+      F128d B0 = y0 + mul_call(r, y1 + y0), B1 = y2 + mul_call(r, y3 + y2);
       aout[2 * j] = A0; aout[2 * j + 1] = A1;
       bout[2 * j] = B0; bout[2 * j + 1] = B1;
       if (msg) {
-        F128d t1 = A1 * B1, ti = (A0 + A1) * (B0 + B1);
+        F128d t1 = mul_call(A1, B1), ti = mul_call(A0 + A1, B0 + B1);
         if (eq_lo) {
           F128d e = eq_lo[j & (chunk - 1)];
-          t1 = e * t1;
-          ti = e * ti;
+          t1 = mul_call(e, t1);
+          ti = mul_call(e, ti);
         }
         g1 += t1;
         gi += ti;
@@ -744,14 +744,14 @@ mo_build_w_kernel(const F128d* __restrict__ q, const F128d* __restrict__ er0, co
       F128d acc = f128_zero();
       if (d < area) {
         uint64_t row = d & rmask, col = d >> nu;
-        acc = fold_slot(er0[row] * ec0[col], tab) + fold_slot(er1[row] * ec1[col], tab + 16 * 256);
+        acc = fold_slot(mul_call(er0[row], ec0[col]), tab) + fold_slot(mul_call(er1[row], ec1[col]), tab + 16 * 256);
       }
       W[k] = acc;
       w[d] = acc;
     }
     F128d q0 = q[2 * i], q1 = q[2 * i + 1];
-    u0 += q0 * W[0];
-    u2 += (q0 + q1) * (W[0] + W[1]);
+    u0 += mul_call(q0, W[0]);
+    u2 += mul_call(q0 + q1, W[0] + W[1]);
   }
   u0 = block_xor(u0, sh);
   u2 = block_xor(u2, sh);
@@ -839,8 +839,8 @@ __global__ void lg_message256_kernel(const F256d* __restrict__ f, const F256d* _
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n / 2; p += (uint64_t)gridDim.x * blockDim.x) {
     uint64_t blk = p / d, k = p - blk * d, lo = 2 * blk * d + k, hi = lo + d;
     F256d f0 = f[lo], f1 = f[hi], b0 = b[lo], b1 = b[hi];
-    u0 += f0 * b0;
-    u2 += (f0 + f1) * (b0 + b1);
+    u0 += f256_mul_call(f0, b0);
+    u2 += f256_mul_call(f0 + f1, b0 + b1);
   }
   F128d r0 = block_xor(u0.c0, sh), r1 = block_xor(u0.c1, sh), r2 = block_xor(u2.c0, sh), r3 = block_xor(u2.c1, sh);
   if (threadIdx.x == 0) {
@@ -863,8 +863,8 @@ __global__ void lg_fold128_kernel(const F128d* __restrict__ f, const F128d* __re
   if (r_dev) r = *r_dev;
   uint64_t blk = i / d, k = i - blk * d, lo = 2 * blk * d + k, hi = lo + d;
   F128d f0 = f[lo], df = f[hi] + f0, b0 = b[lo], db = b[hi] + b0;
-  fo[i] = f256(f0 + r.c0 * df, r.c1 * df);
-  bo[i] = f256(b0 + r.c0 * db, r.c1 * db);
+  fo[i] = f256(f0 + mul_call(r.c0, df), mul_call(r.c1, df));
+  bo[i] = f256(b0 + mul_call(r.c0, db), mul_call(r.c1, db));
 }
 void launch_lg_fold128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, const F256d* r_dev, uint64_t d,
                        F256d* fo, F256d* bo, cudaStream_t s) {
@@ -891,9 +891,6 @@ void launch_lg_fold256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, 
 // folded vectors (pairs d_msg apart): each thread folds the two outputs of one message pair,
 // stores them, and accumulates u0 = sum f0 b0, u2 = sum (f0 + f1)(b0 + b1) over them. Same
 // index maps as lg_fold256_kernel and lg_message256_kernel; one pass instead of two.
-// An out-of-line F256 product: the fused kernel holds six of them per iteration, and
-// inlining them all exhausts the register file.
-__device__ __noinline__ F256d f256_mul_call(F256d a, F256d b) { return a * b; }
 __device__ __forceinline__ void lg_fold_at(const F256d* __restrict__ f, const F256d* __restrict__ b, F256d r, uint64_t d,
                                         uint64_t i, F256d& fi, F256d& bi) {
   const uint64_t blk = i / d, k = i - blk * d, lo = 2 * blk * d + k, hi = lo + d;
