@@ -58,7 +58,7 @@ __global__ void ntt_layer_kernel(F128d* __restrict__ data, uint32_t lanes, uint3
   uint64_t i0 = (block << (sh + 1)) + within, i1 = i0 + (1ull << sh);
   F128d t = tw[(1ull << layer) - 1 + block];
   F128d u = data[i0 * lanes + l], v = data[i1 * lanes + l];
-  F128d nu = u + v * t;
+  F128d nu = block == 0 ? u : u + v * t;  // the first block's twiddle is zero in every layer
   data[i0 * lanes + l] = nu;
   data[i1 * lanes + l] = v + nu;
 }
@@ -101,7 +101,7 @@ __global__ void ntt_fused_kernel(F128d* __restrict__ data, uint32_t lanes, uint3
       uint64_t gblock = gpos >> (log_d - L);
       F128d t = tw[(1ull << L) - 1 + gblock];
       F128d u = sm[i0 * lane_tile + l], v = sm[i1 * lane_tile + l];
-      F128d nu = u + v * t;
+      F128d nu = gblock == 0 ? u : u + v * t;  // the first block's twiddle is zero in every layer
       sm[i0 * lane_tile + l] = nu;
       sm[i1 * lane_tile + l] = v + nu;
     }

@@ -1005,7 +1005,7 @@ __global__ void ntt_t_layer_kernel(F128d* __restrict__ y, uint32_t log_d, uint32
   F128d t = tw[(1ull << layer) - 1 + blk];
   F128d u = y[i0], v = y[i1], sum = u + v;
   y[i0] = sum;
-  y[i1] = v + t * sum;
+  y[i1] = blk == 0 ? v : v + t * sum;  // the first block's twiddle is zero in every layer
 }
 // basis[i] = sum_rep y[rep * n + i]; with the split f (length 2n):
 // a = sum f[2i] basis[i], s = sum (f[2i] + f[2i+1]) basis[i].
