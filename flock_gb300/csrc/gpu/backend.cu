@@ -752,16 +752,16 @@ Msg256 GpuBackend::lg_message(size_t d) {
     const uint64_t n_out = lg_n_ / 2;
     const size_t dm = (d == 1 || n_out == d) ? 1 : d;
     const int nx = lg_cur_ ^ 1;
-    uint32_t nb;
+    FusedPublish fp = fused_publish();
     {
       Mark mk(this, ST_LIGERITO);
-      nb = launch_lg_fold_msg256(lf_[lg_cur_], lb_[lg_cur_], n_out, dev(lg_pend_fold_.r), lg_pend_fold_.d, dm, lf_[nx],
-                                 lb_[nx], part_, st_);
+      launch_lg_fold_msg256(lf_[lg_cur_], lb_[lg_cur_], n_out, dev(lg_pend_fold_.r), lg_pend_fold_.d, dm, lf_[nx],
+                            lb_[nx], part_, st_, fp);
     }
     lg_pend_fold_.active = false;
     lg_cur_ = nx;
     lg_n_ = n_out;
-    auto v = reduce(nb, 4);
+    auto v = read_published(fp.seq, 4);
     Msg256 m;
     m.u0 = F256(v[0], v[1]);
     m.u2 = F256(v[2], v[3]);

@@ -110,7 +110,8 @@ uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64
 void launch_lg_fold128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, const F256d* r_dev, uint64_t d,
                        F256d* fo, F256d* bo, cudaStream_t s);
 uint32_t launch_lg_fold_msg256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, uint64_t d_fold, uint64_t d_msg,
-                               F256d* fo, F256d* bo, F128d* part, cudaStream_t s);                  // width 4
+                               F256d* fo, F256d* bo, F128d* part, cudaStream_t s,
+                               FusedPublish pub = FusedPublish());                                  // width 4
 void launch_lg_fold256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, const F256d* r_dev, uint64_t d,
                        F256d* fo, F256d* bo, cudaStream_t s);
 void launch_lg_code_switch(const F256d* f, const F256d* b, uint64_t n, F256d* fo, F256d* bo, cudaStream_t s);

@@ -898,10 +898,10 @@ __device__ __forceinline__ void lg_fold_at(const F256d* __restrict__ f, const F2
   fi = f0 + f256_mul_call(r, f[hi] + f0);
   bi = b0 + f256_mul_call(r, b[hi] + b0);
 }
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
 lg_fold_msg256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n_out, F256d r,
                       uint64_t d_fold, uint64_t d_msg, F256d* __restrict__ fo, F256d* __restrict__ bo,
-                      F128d* __restrict__ part) {
+                      F128d* __restrict__ part, FusedPublish pub) {
   __shared__ F128d sh[32];
   F256d u0 = f256(f128_zero(), f128_zero()), u2 = u0;
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_out / 2; p += (uint64_t)gridDim.x * blockDim.x) {
@@ -921,11 +921,12 @@ lg_fold_msg256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, 
     part[blockIdx.x * 4] = r0; part[blockIdx.x * 4 + 1] = r1;
     part[blockIdx.x * 4 + 2] = r2; part[blockIdx.x * 4 + 3] = r3;
   }
+  if (pub.out) publish_if_last(part, 4, pub, sh);
 }
 uint32_t launch_lg_fold_msg256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, uint64_t d_fold, uint64_t d_msg,
-                               F256d* fo, F256d* bo, F128d* part, cudaStream_t s) {
+                               F256d* fo, F256d* bo, F128d* part, cudaStream_t s, FusedPublish pub) {
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n_out / 2 + 255) / 256, (uint64_t)sm_count() * 8));
-  lg_fold_msg256_kernel<<<blocks, 256, 0, s>>>(f, b, n_out, r, d_fold, d_msg, fo, bo, part);
+  lg_fold_msg256_kernel<<<blocks, 256, 0, s>>>(f, b, n_out, r, d_fold, d_msg, fo, bo, part, pub);
   LAUNCH_OK();
   return blocks;
 }
