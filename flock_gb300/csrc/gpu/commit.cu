@@ -9,6 +9,7 @@
 // one position's `lanes` words. Trees are flat: leaves [0, N), then each level, root last.
 #include "kernels.h"
 #include "sha256.cuh"
+#include <atomic>
 
 namespace flock {
 namespace gpu {
@@ -66,12 +67,14 @@ __global__ void ntt_layer_kernel(F128d* __restrict__ data, uint32_t lanes, uint3
 // Several consecutive layers [layer, layer + nl) fused through shared memory. A block
 // owns 2^nl positions spaced 2^(log_d - layer - nl) apart (one residue class inside a
 // block of the first fused layer) for a slice of lanes; each fused layer pairs positions
-// within that set.
+// within that set. Fused layer k meets 2^k twiddles; the block stages all 2^nl - 1 of them
+// once, already split for mul_split, after the positions' data.
 template <int NL>
 __global__ void ntt_fused_kernel(F128d* __restrict__ data, uint32_t lanes, uint32_t log_d, uint32_t layer,
                                  const F128d* __restrict__ tw, uint32_t lane_tile) {
-  extern __shared__ F128d sm[];  // [2^NL][lane_tile]
+  extern __shared__ F128d sm[];  // [2^NL][lane_tile], then F128split[2^NL - 1]
   const uint32_t P = 1u << NL;
+  F128split* tws = reinterpret_cast<F128split*>(sm + P * lane_tile);
   uint32_t stride_log = log_d - layer - NL;  // spacing of the positions in this group
   uint64_t n_groups = 1ull << (log_d - NL);
   uint64_t lane_tiles = (lanes + lane_tile - 1) / lane_tile;
@@ -83,27 +86,37 @@ __global__ void ntt_fused_kernel(F128d* __restrict__ data, uint32_t lanes, uint3
   uint64_t base = (outer << (stride_log + NL)) + resid;
   uint32_t l0 = lt * lane_tile;
   uint32_t nl_here = min(lane_tile, lanes - l0);
+  // twiddle (k, blk) at tws[2^k - 1 + blk]: its global block at layer + k is (outer << k) + blk
+  for (uint32_t t = threadIdx.x; t < P - 1; t += blockDim.x) {
+    const uint32_t k = 31 - __clz(t + 1), blk = t + 1 - (1u << k);
+    tws[t] = split_factor(tw[(1ull << (layer + k)) - 1 + (outer << k) + blk]);
+  }
   for (uint32_t i = threadIdx.x; i < P * nl_here; i += blockDim.x) {
     uint32_t pos = i / nl_here, l = i - pos * nl_here;
     sm[pos * lane_tile + l] = data[(base + ((uint64_t)pos << stride_log)) * lanes + l0 + l];
   }
   __syncthreads();
+  // (pair, lane) of this thread's first butterfly and the step between its butterflies
+  const uint32_t pr0 = threadIdx.x / nl_here, ln0 = threadIdx.x - pr0 * nl_here;
+  const uint32_t dpr = blockDim.x / nl_here, dln = blockDim.x - dpr * nl_here;
 #pragma unroll
   for (int k = 0; k < NL; ++k) {
-    uint32_t L = layer + k;
-    uint32_t half = P >> (k + 1);  // pairing distance inside the group (in group positions)
+    const uint32_t half = P >> (k + 1);  // pairing distance inside the group (in group positions)
+    uint32_t pr = pr0, l = ln0;
     for (uint32_t i = threadIdx.x; i < (P / 2) * nl_here; i += blockDim.x) {
-      uint32_t pr = i / nl_here, l = i - pr * nl_here;
       uint32_t blk = pr / half, w = pr - blk * half;
       uint32_t i0 = blk * 2 * half + w, i1 = i0 + half;
-      // global block index at layer L of position i0
-      uint64_t gpos = base + ((uint64_t)i0 << stride_log);
-      uint64_t gblock = gpos >> (log_d - L);
-      F128d t = tw[(1ull << L) - 1 + gblock];
       F128d u = sm[i0 * lane_tile + l], v = sm[i1 * lane_tile + l];
-      F128d nu = gblock == 0 ? u : u + v * t;  // the first block's twiddle is zero in every layer
+      // the first block's twiddle is zero in every layer
+      F128d nu = (outer == 0 && blk == 0) ? u : u + mul_split(v, tws[(1u << k) - 1 + blk]);
       sm[i0 * lane_tile + l] = nu;
       sm[i1 * lane_tile + l] = v + nu;
+      pr += dpr;
+      l += dln;
+      if (l >= nl_here) {
+        l -= nl_here;
+        ++pr;
+      }
     }
     __syncthreads();
   }
@@ -113,19 +126,48 @@ __global__ void ntt_fused_kernel(F128d* __restrict__ data, uint32_t lanes, uint3
   }
 }
 
+// Threads per fused-NTT block for a lane tile: among the multiples of 32 in [192, 384], the
+// one with the most busy resident warps per SM (resident warps, capped at 32, times the
+// fraction of threads with a butterfly in a layer's passes). Cached per device and tile.
+template <int NL>
+static uint32_t ntt_block_threads(uint32_t lane_tile, size_t smem) {
+  static std::atomic<uint32_t> cache[MAX_DEVICES][65];
+  int dev = 0;
+  CUDA_OK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= MAX_DEVICES || lane_tile > 64) throw std::runtime_error("fused NTT: bad device or lane tile");
+  uint32_t best = cache[dev][lane_tile].load(std::memory_order_relaxed);
+  if (best) return best;
+  const uint32_t butterflies = (1u << (NL - 1)) * lane_tile;
+  double best_score = -1.0;
+  for (uint32_t t = 192; t <= 384; t += 32) {
+    int blocks = 0;
+    CUDA_OK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, ntt_fused_kernel<NL>, (int)t, smem));
+    const uint32_t passes = (butterflies + t - 1) / t;
+    const double score = std::min(blocks * t / 32.0, 32.0) * butterflies / (double)(passes * t);
+    if (score > best_score + 1e-9) {
+      best_score = score;
+      best = t;
+    }
+  }
+  cache[dev][lane_tile].store(best, std::memory_order_relaxed);
+  return best;
+}
+
 void launch_ntt(F128d* data, uint32_t lanes, uint32_t log_d, uint32_t start_layer, const F128d* tw, cudaStream_t s) {
   const int NL = 6;  // layers fused per pass
   uint32_t layer = start_layer;
   uint32_t lane_tile = lanes < 64 ? lanes : 64;
+  const size_t tw_bytes = ((1u << NL) - 1) * sizeof(F128split);
   while (layer < log_d) {
     uint32_t remaining = log_d - layer;
     if (remaining >= (uint32_t)NL) {
       uint64_t n_groups = 1ull << (log_d - NL);
       uint64_t lane_tiles = (lanes + lane_tile - 1) / lane_tile;
-      size_t smem = (size_t)(1u << NL) * lane_tile * sizeof(F128d);
-      set_dynamic_smem((const void*)ntt_fused_kernel<NL>, (int)((1u << NL) * 64 * sizeof(F128d)));
-      ntt_fused_kernel<NL><<<(unsigned)(n_groups * lane_tiles), 256, smem, s>>>(data, lanes, log_d, layer, tw,
-                                                                                 lane_tile);
+      size_t smem = (size_t)(1u << NL) * lane_tile * sizeof(F128d) + tw_bytes;
+      set_dynamic_smem((const void*)ntt_fused_kernel<NL>, (int)((1u << NL) * 64 * sizeof(F128d) + tw_bytes));
+      const uint32_t threads = ntt_block_threads<NL>(lane_tile, smem);
+      ntt_fused_kernel<NL><<<(unsigned)(n_groups * lane_tiles), threads, smem, s>>>(data, lanes, log_d, layer, tw,
+                                                                                     lane_tile);
       LAUNCH_OK();
       layer += NL;
     } else {

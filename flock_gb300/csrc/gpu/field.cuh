@@ -76,6 +76,60 @@ __device__ __forceinline__ F128d operator*(F128d a, F128d b) { return mul(a, b);
 // a call keeps one product's temporaries live at a time.
 __device__ __noinline__ static F128d mul_call(F128d a, F128d b) { return mul(a, b); }
 
+// One factor of mul() in the form clmul32 consumes it: the nine Karatsuba words (for each
+// of b.lo, b.hi and b.lo ^ b.hi: its low half, its high half and their sum), each thinned
+// to its four residue classes. Multiplying many values by one constant (an NTT twiddle, a
+// fold challenge) from this form skips the constant's 41 splitting and pre-add operations
+// per product; the products are bit-identical to mul().
+struct __align__(16) F128split {
+  uint32_t w[9][4];
+};
+__device__ __forceinline__ void split_classes(uint32_t y, uint32_t* o) {
+  o[0] = y & 0x11111111u;
+  o[1] = y & 0x22222222u;
+  o[2] = y & 0x44444444u;
+  o[3] = y & 0x88888888u;
+}
+__device__ __forceinline__ F128split split_factor(F128d b) {
+  F128split s;
+  const uint64_t hl[3] = {b.lo, b.hi, b.lo ^ b.hi};
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const uint32_t y0 = (uint32_t)hl[q], y1 = (uint32_t)(hl[q] >> 32);
+    split_classes(y0, s.w[3 * q]);
+    split_classes(y1, s.w[3 * q + 1]);
+    split_classes(y0 ^ y1, s.w[3 * q + 2]);
+  }
+  return s;
+}
+__device__ __forceinline__ uint64_t clmul32_split(uint32_t x, const uint32_t* y) {
+  const uint32_t x0 = x & 0x11111111u, x1 = x & 0x22222222u, x2 = x & 0x44444444u, x3 = x & 0x88888888u;
+  const uint32_t y0 = y[0], y1 = y[1], y2 = y[2], y3 = y[3];
+  uint64_t z0 = mulw(x0, y0) ^ mulw(x1, y3) ^ mulw(x2, y2) ^ mulw(x3, y1);
+  uint64_t z1 = mulw(x0, y1) ^ mulw(x1, y0) ^ mulw(x2, y3) ^ mulw(x3, y2);
+  uint64_t z2 = mulw(x0, y2) ^ mulw(x1, y1) ^ mulw(x2, y0) ^ mulw(x3, y3);
+  uint64_t z3 = mulw(x0, y3) ^ mulw(x1, y2) ^ mulw(x2, y1) ^ mulw(x3, y0);
+  const uint64_t M0 = 0x1111111111111111ull, M1 = 0x2222222222222222ull, M2 = 0x4444444444444444ull,
+                 M3 = 0x8888888888888888ull;
+  return (z0 & M0) | (z1 & M1) | (z2 & M2) | (z3 & M3);
+}
+__device__ __forceinline__ void clmul64_split(uint64_t a, const uint32_t (*y)[4], uint64_t& lo, uint64_t& hi) {
+  const uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32);
+  uint64_t l = clmul32_split(a0, y[0]), h = clmul32_split(a1, y[1]), m = clmul32_split(a0 ^ a1, y[2]) ^ l ^ h;
+  lo = l ^ (m << 32);
+  hi = h ^ (m >> 32);
+}
+// a * b with b given as split_factor(b).
+__device__ __forceinline__ F128d mul_split(F128d a, const F128split& b) {
+  uint64_t l0, l1, h0, h1, m0, m1;
+  clmul64_split(a.lo, b.w, l0, l1);
+  clmul64_split(a.hi, b.w + 3, h0, h1);
+  clmul64_split(a.lo ^ a.hi, b.w + 6, m0, m1);
+  m0 ^= l0 ^ h0;
+  m1 ^= l1 ^ h1;
+  return ghash_reduce(l0, l1 ^ m0, h0 ^ m1, h1);
+}
+
 __device__ __forceinline__ F128d mul_by_x(F128d z) {
   uint64_t mask = 0ull - (z.hi >> 63);
   return f128((z.lo << 1) ^ (0x87ull & mask), (z.hi << 1) | (z.lo >> 63));

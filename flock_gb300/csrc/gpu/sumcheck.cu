@@ -115,35 +115,18 @@ struct ZcConsts {
   F128d phi8[256];
   uint8_t mulk[8][256];        // e_K * v
   F128d wconst[64];            // word weights within an xo: x^M * phi8(e2[K2]) for word 4M + K2
+  uint8_t gmul[256 * 256];     // GF(2^8) products: gmul[256 a + b] = a * b
 };
 constexpr size_t ZC_CONST_BYTES = (sizeof(ZcConsts) + 15) & ~size_t(15);
 
-// Byte b of a word (zero-extended) and every byte of v set to 0xFF where its bit 7 is set:
-// one byte-permute each.
+// Byte b of a word, zero-extended: one byte-permute.
 __device__ __forceinline__ uint32_t byte_of(uint32_t v, int b) { return __byte_perm(v, 0, 0x4440 | b); }
-// prmt with the sign-replicate bit set in each selector nibble (not expressible through
-// __byte_perm, which ignores that bit)
-__device__ __forceinline__ uint32_t msb_spread(uint32_t v) {
-  uint32_t r;
-  asm("prmt.b32 %0, %1, %2, 0xBA98;" : "=r"(r) : "r"(v), "r"(0u));
-  return r;
-}
-
-// Four GF(2^8) products (AES polynomial) of packed bytes, shift-and-add in registers.
-__device__ __forceinline__ uint32_t gf8_mul4(uint32_t a, uint32_t b) {
-  uint32_t r = 0;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    r ^= a & msb_spread(b << (7 - k));  // bit k of each byte of b selects a * x^k
-    if (k < 7) a = ((a << 1) & 0xFEFEFEFEu) ^ (msb_spread(a) & 0x1B1B1B1Bu);
-  }
-  return r;
-}
 
 // P_ab: one team of 16 threads per xo, thread = four Lambda points; no block barriers
 // after the constants are staged. Per row x = 8M + K the team extends the a and b rows
-// (8 byte-table lookups each), multiplies pointwise in GF(2^8) and accumulates e_K * p
-// into g_M; then F = sum_M x^M phi8(g_M) (Horner) and acc += eq_o(xo) * F.
+// (8 byte-table lookups each), multiplies pointwise in GF(2^8) through the 64 KB product
+// table and accumulates e_K * p into g_M; then F = sum_M x^M phi8(g_M) (Horner) and
+// acc += eq_o(xo) * F. Tables: about 199 KB of shared memory, one block per SM.
 constexpr int ZC_TEAMS = 32;  // teams per block (512 threads)
 __global__ void __launch_bounds__(16 * ZC_TEAMS, 1)
 zc_round1_ab_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, uint64_t n_xo,
@@ -184,10 +167,12 @@ zc_round1_ab_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, ui
             eb ^= *reinterpret_cast<const uint32_t*>(extb + c * 16384 + (byte_of(b0, c) << 6)) ^
                   *reinterpret_cast<const uint32_t*>(extb + (c + 4) * 16384 + (byte_of(b1, c) << 6));
           }
-          uint32_t p = gf8_mul4(ea, eb);
+          // four GF(2^8) products by table (shared memory; the table is symmetric, so the
+          // index may put either operand high), each scaled by e_K through its mulk table
+          const uint32_t i01 = __byte_perm(ea, eb, 0x5140), i23 = __byte_perm(ea, eb, 0x7362);
           const uint8_t* mk = C.mulk[2 * kk + h];
-          g ^= (uint32_t)mk[byte_of(p, 0)] | ((uint32_t)mk[byte_of(p, 1)] << 8) | ((uint32_t)mk[byte_of(p, 2)] << 16) |
-               ((uint32_t)mk[byte_of(p, 3)] << 24);
+          g ^= (uint32_t)mk[C.gmul[i01 & 0xFFFF]] | ((uint32_t)mk[C.gmul[i01 >> 16]] << 8) |
+               ((uint32_t)mk[C.gmul[i23 & 0xFFFF]] << 16) | ((uint32_t)mk[C.gmul[i23 >> 16]] << 24);
         }
       }
       G[M] = g;
@@ -270,6 +255,15 @@ void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t mulk[
   memcpy(h->phi8, phi8, sizeof(h->phi8));
   memcpy(h->mulk, mulk, sizeof(h->mulk));
   memcpy(h->wconst, wconst, sizeof(h->wconst));
+  for (uint32_t a = 0; a < 256; ++a)
+    for (uint32_t b = 0; b < 256; ++b) {
+      uint32_t p = 0, x = a;  // shift-and-add modulo the AES polynomial x^8 + x^4 + x^3 + x + 1
+      for (int k = 0; k < 8; ++k) {
+        if ((b >> k) & 1) p ^= x;
+        x = (x << 1) ^ ((x & 0x80) ? 0x11B : 0);
+      }
+      h->gmul[256 * a + b] = (uint8_t)p;
+    }
   ZcConsts* d = nullptr;
   CUDA_OK(cudaMalloc(&d, ZC_CONST_BYTES));
   CUDA_OK(cudaMemset(d, 0, ZC_CONST_BYTES));
