@@ -130,6 +130,10 @@ __device__ __forceinline__ F128d mul_split(F128d a, const F128split& b) {
   return ghash_reduce(l0, l1 ^ m0, h0 ^ m1, h1);
 }
 
+// Out-of-line mul_split (see mul_call); b is typically staged once per block in shared
+// memory.
+__device__ __noinline__ static F128d mul_split_call(F128d a, const F128split* b) { return mul_split(a, *b); }
+
 __device__ __forceinline__ F128d mul_by_x(F128d z) {
   uint64_t mask = 0ull - (z.hi >> 63);
   return f128((z.lo << 1) ^ (0x87ull & mask), (z.hi << 1) | (z.lo >> 63));

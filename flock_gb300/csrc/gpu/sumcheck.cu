@@ -476,7 +476,9 @@ pair_fold_kernel(const F128d* __restrict__ ain, const F128d* __restrict__ bin, u
                  const F128d* __restrict__ r_dev, const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F128d* __restrict__ eq_hi,
                  F128d* __restrict__ aout, F128d* __restrict__ bout, F128d* __restrict__ part, int msg, FusedPublish pub) {
   __shared__ F128d sh[32];
-  if (r_dev) r = *r_dev;
+  __shared__ F128split rs;  // the fold challenge, split once
+  if (threadIdx.x == 0) rs = split_factor(r_dev ? *r_dev : r);
+  __syncthreads();
   const uint64_t chunk = 1ull << lo_bits;
   const uint64_t n_chunks = (n_pairs + chunk - 1) / chunk;
   F128d G1 = f128_zero(), GI = f128_zero();
@@ -486,8 +488,8 @@ pair_fold_kernel(const F128d* __restrict__ ain, const F128d* __restrict__ bin, u
     for (uint64_t j = ch * chunk + threadIdx.x; j < end; j += blockDim.x) {
       F128d x0 = ain[4 * j], x1 = ain[4 * j + 1], x2 = ain[4 * j + 2], x3 = ain[4 * j + 3];
       F128d y0 = bin[4 * j], y1 = bin[4 * j + 1], y2 = bin[4 * j + 2], y3 = bin[4 * j + 3];
-      F128d A0 = x0 + mul_call(r, x1 + x0), A1 = x2 + mul_call(r, x3 + x2);
-      F128d B0 = y0 + mul_call(r, y1 + y0), B1 = y2 + mul_call(r, y3 + y2);
+      F128d A0 = x0 + mul_split_call(x1 + x0, &rs), A1 = x2 + mul_split_call(x3 + x2, &rs);
+      F128d B0 = y0 + mul_split_call(y1 + y0, &rs), B1 = y2 + mul_split_call(y3 + y2, &rs);
       aout[2 * j] = A0; aout[2 * j + 1] = A1;
       bout[2 * j] = B0; bout[2 * j + 1] = B1;
       if (msg) {
@@ -806,12 +808,22 @@ uint32_t launch_lg_dot_eq(const F128d* f, uint32_t stride, const F128d* eq_lo, u
 // Round message with block pairing d: pairs (lo, lo + d), lo = 2 d blk + k.
 //   u0 = sum f[lo] b[lo], u2 = sum (f[lo] + f[hi]) (b[lo] + b[hi]).
 // F128 (base) variant: outputs 2 words per block; F256 variant: 4 words (u0.c0, u0.c1, u2.c0, u2.c1).
-__global__ void lg_message128_kernel(const F128d* __restrict__ f, const F128d* __restrict__ b, uint64_t n, uint64_t d,
+// The pairing distances are powers of two (the kernels take log2 d).
+static uint32_t log2_distance(uint64_t d) {
+  if (d == 0 || (d & (d - 1))) throw std::runtime_error("Ligerito pair distance must be a power of two");
+  uint32_t l = 0;
+  while ((uint64_t(1) << l) < d) ++l;
+  return l;
+}
+__device__ __forceinline__ uint64_t pair_lo(uint64_t i, uint32_t d_log) {
+  return ((i >> d_log) << (d_log + 1)) | (i & ((1ull << d_log) - 1));
+}
+__global__ void lg_message128_kernel(const F128d* __restrict__ f, const F128d* __restrict__ b, uint64_t n, uint32_t d_log,
                                      F128d* __restrict__ part) {
   __shared__ F128d sh[32];
   F128d u0 = f128_zero(), u2 = f128_zero();
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n / 2; p += (uint64_t)gridDim.x * blockDim.x) {
-    uint64_t blk = p / d, k = p - blk * d, lo = 2 * blk * d + k, hi = lo + d;
+    const uint64_t lo = pair_lo(p, d_log), hi = lo + (1ull << d_log);
     F128d f0 = f[lo], f1 = f[hi], b0 = b[lo], b1 = b[hi];
     u0 += f0 * b0;
     u2 += (f0 + f1) * (b0 + b1);
@@ -822,16 +834,16 @@ __global__ void lg_message128_kernel(const F128d* __restrict__ f, const F128d* _
 }
 uint32_t launch_lg_message128(const F128d* f, const F128d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s) {
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n / 2 + 255) / 256, (uint64_t)sm_count() * 8));
-  lg_message128_kernel<<<blocks, 256, 0, s>>>(f, b, n, d, part);
+  lg_message128_kernel<<<blocks, 256, 0, s>>>(f, b, n, log2_distance(d), part);
   LAUNCH_OK();
   return blocks;
 }
-__global__ void lg_message256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n, uint64_t d,
+__global__ void lg_message256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n, uint32_t d_log,
                                      F128d* __restrict__ part) {
   __shared__ F128d sh[32];
   F256d u0 = f256(f128_zero(), f128_zero()), u2 = u0;
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n / 2; p += (uint64_t)gridDim.x * blockDim.x) {
-    uint64_t blk = p / d, k = p - blk * d, lo = 2 * blk * d + k, hi = lo + d;
+    const uint64_t lo = pair_lo(p, d_log), hi = lo + (1ull << d_log);
     F256d f0 = f[lo], f1 = f[hi], b0 = b[lo], b1 = b[hi];
     u0 += f256_mul_call(f0, b0);
     u2 += f256_mul_call(f0 + f1, b0 + b1);
@@ -844,68 +856,68 @@ __global__ void lg_message256_kernel(const F256d* __restrict__ f, const F256d* _
 }
 uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s) {
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n / 2 + 255) / 256, (uint64_t)sm_count() * 8));
-  lg_message256_kernel<<<blocks, 256, 0, s>>>(f, b, n, d, part);
+  lg_message256_kernel<<<blocks, 256, 0, s>>>(f, b, n, log2_distance(d), part);
   LAUNCH_OK();
   return blocks;
 }
 // o[i] = v[lo] + r (v[hi] + v[lo]), i = blk d + k, lo = 2 d blk + k.
 __global__ void lg_fold128_kernel(const F128d* __restrict__ f, const F128d* __restrict__ b, uint64_t n_out, F256d r,
-                                  const F256d* __restrict__ r_dev, uint64_t d, F256d* __restrict__ fo,
+                                  const F256d* __restrict__ r_dev, uint32_t d_log, F256d* __restrict__ fo,
                                   F256d* __restrict__ bo) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_out) return;
-  if (r_dev) r = *r_dev;
-  uint64_t blk = i / d, k = i - blk * d, lo = 2 * blk * d + k, hi = lo + d;
+  const uint64_t lo = pair_lo(i, d_log), hi = lo + (1ull << d_log);
   F128d f0 = f[lo], df = f[hi] + f0, b0 = b[lo], db = b[hi] + b0;
-  fo[i] = f256(f0 + mul_call(r.c0, df), mul_call(r.c1, df));
-  bo[i] = f256(b0 + mul_call(r.c0, db), mul_call(r.c1, db));
+  const F256d rv = r_dev ? *r_dev : r;
+  fo[i] = f256(f0 + mul_call(rv.c0, df), mul_call(rv.c1, df));
+  bo[i] = f256(b0 + mul_call(rv.c0, db), mul_call(rv.c1, db));
 }
 void launch_lg_fold128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, const F256d* r_dev, uint64_t d,
                        F256d* fo, F256d* bo, cudaStream_t s) {
-  lg_fold128_kernel<<<(unsigned)((n_out + 255) / 256), 256, 0, s>>>(f, b, n_out, r, r_dev, d, fo, bo);
+  lg_fold128_kernel<<<(unsigned)((n_out + 255) / 256), 256, 0, s>>>(f, b, n_out, r, r_dev, log2_distance(d), fo, bo);
   LAUNCH_OK();
 }
 __global__ void lg_fold256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n_out, F256d r,
-                                  const F256d* __restrict__ r_dev, uint64_t d, F256d* __restrict__ fo,
+                                  const F256d* __restrict__ r_dev, uint32_t d_log, F256d* __restrict__ fo,
                                   F256d* __restrict__ bo) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_out) return;
-  if (r_dev) r = *r_dev;
-  uint64_t blk = i / d, k = i - blk * d, lo = 2 * blk * d + k, hi = lo + d;
+  const uint64_t lo = pair_lo(i, d_log), hi = lo + (1ull << d_log);
   F256d f0 = f[lo], b0 = b[lo];
-  fo[i] = f0 + r * (f[hi] + f0);
-  bo[i] = b0 + r * (b[hi] + b0);
+  const F256d rv = r_dev ? *r_dev : r;
+  fo[i] = f0 + f256_mul_call(rv, f[hi] + f0);
+  bo[i] = b0 + f256_mul_call(rv, b[hi] + b0);
 }
 void launch_lg_fold256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, const F256d* r_dev, uint64_t d,
                        F256d* fo, F256d* bo, cudaStream_t s) {
-  lg_fold256_kernel<<<(unsigned)((n_out + 255) / 256), 256, 0, s>>>(f, b, n_out, r, r_dev, d, fo, bo);
+  lg_fold256_kernel<<<(unsigned)((n_out + 255) / 256), 256, 0, s>>>(f, b, n_out, r, r_dev, log2_distance(d), fo, bo);
   LAUNCH_OK();
 }
 // One round's fold (at r, pairs d_fold apart) fused with the next round's message over the
 // folded vectors (pairs d_msg apart): each thread folds the two outputs of one message pair,
 // stores them, and accumulates u0 = sum f0 b0, u2 = sum (f0 + f1)(b0 + b1) over them. Same
 // index maps as lg_fold256_kernel and lg_message256_kernel; one pass instead of two.
-__device__ __forceinline__ void lg_fold_at(const F256d* __restrict__ f, const F256d* __restrict__ b, F256d r, uint64_t d,
-                                        uint64_t i, F256d& fi, F256d& bi) {
-  const uint64_t blk = i / d, k = i - blk * d, lo = 2 * blk * d + k, hi = lo + d;
+__device__ __forceinline__ void lg_fold_at(const F256d* __restrict__ f, const F256d* __restrict__ b, F256d r,
+                                        uint32_t d_log, uint64_t i, F256d& fi, F256d& bi) {
+  const uint64_t lo = pair_lo(i, d_log), hi = lo + (1ull << d_log);
   const F256d f0 = f[lo], b0 = b[lo];
   fi = f0 + f256_mul_call(r, f[hi] + f0);
   bi = b0 + f256_mul_call(r, b[hi] + b0);
 }
 __global__ void __launch_bounds__(256, 2)
 lg_fold_msg256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n_out, F256d r,
-                      uint64_t d_fold, uint64_t d_msg, F256d* __restrict__ fo, F256d* __restrict__ bo,
+                      uint32_t dlog_fold, uint32_t dlog_msg, F256d* __restrict__ fo, F256d* __restrict__ bo,
                       F128d* __restrict__ part, FusedPublish pub) {
   __shared__ F128d sh[32];
   F256d u0 = f256(f128_zero(), f128_zero()), u2 = u0;
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_out / 2; p += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t mb = p / d_msg, mk = p - mb * d_msg, olo = 2 * mb * d_msg + mk, ohi = olo + d_msg;
+    const uint64_t olo = pair_lo(p, dlog_msg), ohi = olo + (1ull << dlog_msg);
     F256d fl, bl, fh, bh;
-    lg_fold_at(f, b, r, d_fold, olo, fl, bl);
+    lg_fold_at(f, b, r, dlog_fold, olo, fl, bl);
     fo[olo] = fl;
     bo[olo] = bl;
     u0 += f256_mul_call(fl, bl);
-    lg_fold_at(f, b, r, d_fold, ohi, fh, bh);
+    lg_fold_at(f, b, r, dlog_fold, ohi, fh, bh);
     fo[ohi] = fh;
     bo[ohi] = bh;
     u2 += f256_mul_call(fl + fh, bl + bh);
@@ -920,7 +932,8 @@ lg_fold_msg256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, 
 uint32_t launch_lg_fold_msg256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, uint64_t d_fold, uint64_t d_msg,
                                F256d* fo, F256d* bo, F128d* part, cudaStream_t s, FusedPublish pub) {
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n_out / 2 + 255) / 256, (uint64_t)sm_count() * 8));
-  lg_fold_msg256_kernel<<<blocks, 256, 0, s>>>(f, b, n_out, r, d_fold, d_msg, fo, bo, part, pub);
+  lg_fold_msg256_kernel<<<blocks, 256, 0, s>>>(f, b, n_out, r, log2_distance(d_fold), log2_distance(d_msg), fo, bo,
+                                               part, pub);
   LAUNCH_OK();
   return blocks;
 }
