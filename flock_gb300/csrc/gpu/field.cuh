@@ -6,8 +6,9 @@
 // formed from sixteen 32x32 -> 64 integer multiplies of operands thinned to every
 // fourth bit ("holes"): within one residue class mod 4 each product column receives at
 // most 8 partial products, so no carry reaches the next bit of the same class and the
-// class bits of the integer product are the GF(2) sums. The four classes are masked and
-// merged. Two Karatsuba levels build the 128 x 128 product from nine such products,
+// class bits of the integer product are the GF(2) sums (pairs of products whose columns
+// stay below 16 are summed as integers, clmul32_classes). The four classes are masked
+// and merged. Two Karatsuba levels build the 128 x 128 product from nine such products,
 // followed by the shift-and-fold reduction.
 #pragma once
 #include <cstdint>
@@ -29,20 +30,44 @@ __host__ __device__ __forceinline__ F128d operator+(F128d a, F128d b) { return f
 __host__ __device__ __forceinline__ F128d& operator+=(F128d& a, F128d b) { a.lo ^= b.lo; a.hi ^= b.hi; return a; }
 __host__ __device__ __forceinline__ bool is_zero(F128d a) { return (a.lo | a.hi) == 0; }
 
-__device__ __forceinline__ uint64_t mulw(uint32_t a, uint32_t b) { return (uint64_t)a * (uint64_t)b; }
+// 32 x 32 -> 64 integer product, and the same plus a 64-bit addend. Written as PTX
+// mul.wide / mad.wide: the C++ form (uint64_t)a * (uint64_t)b compiles to a wide multiply
+// plus an extra add on the same multiply pipe, which costs the GF(2^128) product ~14%.
+__device__ __forceinline__ uint64_t mulw(uint32_t a, uint32_t b) {
+  uint64_t r;
+  asm("mul.wide.u32 %0, %1, %2;" : "=l"(r) : "r"(a), "r"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t madw(uint32_t a, uint32_t b, uint64_t c) {
+  uint64_t r;
+  asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(r) : "r"(a), "r"(b), "l"(c));
+  return r;
+}
+
+// The carry-less product from the operands' residue classes: class c of the result
+// collects the four products x_i y_j with i + j = c (mod 4). A product's column p holds
+// g(u) = #{s + t = u : 0 <= s, t <= 7} partial products, u = (p - i - j) / 4, at most 8.
+// Two products of one class whose index sums differ by 4 peak one column apart, so their
+// integer sum holds at most g(u) + g(u - 1) <= 15 per column: still no carry into the
+// next column of the class. Such pairs are added (in the multiply's addend) instead of
+// XORed, which moves work from the logic pipe to the multiply pipe.
+__device__ __forceinline__ uint64_t clmul32_classes(uint32_t x0, uint32_t x1, uint32_t x2, uint32_t x3, uint32_t y0,
+                                                    uint32_t y1, uint32_t y2, uint32_t y3) {
+  const uint64_t z0 = madw(x0, y0, mulw(x1, y3)) ^ mulw(x2, y2) ^ mulw(x3, y1);
+  const uint64_t z1 = madw(x0, y1, mulw(x2, y3)) ^ madw(x1, y0, mulw(x3, y2));
+  const uint64_t z2 = madw(x0, y2, mulw(x3, y3)) ^ mulw(x1, y1) ^ mulw(x2, y0);
+  const uint64_t z3 = mulw(x0, y3) ^ mulw(x1, y2) ^ mulw(x2, y1) ^ mulw(x3, y0);
+  const uint64_t M0 = 0x1111111111111111ull, M1 = 0x2222222222222222ull, M2 = 0x4444444444444444ull,
+                 M3 = 0x8888888888888888ull;
+  return (z0 & M0) | (z1 & M1) | (z2 & M2) | (z3 & M3);
+}
 
 // 32 x 32 -> 64 carry-less product.
 __device__ __forceinline__ uint64_t clmul32(uint32_t x, uint32_t y) {
   const uint32_t m0 = 0x11111111u, m1 = 0x22222222u, m2 = 0x44444444u, m3 = 0x88888888u;
   uint32_t x0 = x & m0, x1 = x & m1, x2 = x & m2, x3 = x & m3;
   uint32_t y0 = y & m0, y1 = y & m1, y2 = y & m2, y3 = y & m3;
-  uint64_t z0 = mulw(x0, y0) ^ mulw(x1, y3) ^ mulw(x2, y2) ^ mulw(x3, y1);
-  uint64_t z1 = mulw(x0, y1) ^ mulw(x1, y0) ^ mulw(x2, y3) ^ mulw(x3, y2);
-  uint64_t z2 = mulw(x0, y2) ^ mulw(x1, y1) ^ mulw(x2, y0) ^ mulw(x3, y3);
-  uint64_t z3 = mulw(x0, y3) ^ mulw(x1, y2) ^ mulw(x2, y1) ^ mulw(x3, y0);
-  const uint64_t M0 = 0x1111111111111111ull, M1 = 0x2222222222222222ull, M2 = 0x4444444444444444ull,
-                 M3 = 0x8888888888888888ull;
-  return (z0 & M0) | (z1 & M1) | (z2 & M2) | (z3 & M3);
+  return clmul32_classes(x0, x1, x2, x3, y0, y1, y2, y3);
 }
 
 // 64 x 64 -> 128 carry-less product (Karatsuba over 32-bit halves).
@@ -104,14 +129,7 @@ __device__ __forceinline__ F128split split_factor(F128d b) {
 }
 __device__ __forceinline__ uint64_t clmul32_split(uint32_t x, const uint32_t* y) {
   const uint32_t x0 = x & 0x11111111u, x1 = x & 0x22222222u, x2 = x & 0x44444444u, x3 = x & 0x88888888u;
-  const uint32_t y0 = y[0], y1 = y[1], y2 = y[2], y3 = y[3];
-  uint64_t z0 = mulw(x0, y0) ^ mulw(x1, y3) ^ mulw(x2, y2) ^ mulw(x3, y1);
-  uint64_t z1 = mulw(x0, y1) ^ mulw(x1, y0) ^ mulw(x2, y3) ^ mulw(x3, y2);
-  uint64_t z2 = mulw(x0, y2) ^ mulw(x1, y1) ^ mulw(x2, y0) ^ mulw(x3, y3);
-  uint64_t z3 = mulw(x0, y3) ^ mulw(x1, y2) ^ mulw(x2, y1) ^ mulw(x3, y0);
-  const uint64_t M0 = 0x1111111111111111ull, M1 = 0x2222222222222222ull, M2 = 0x4444444444444444ull,
-                 M3 = 0x8888888888888888ull;
-  return (z0 & M0) | (z1 & M1) | (z2 & M2) | (z3 & M3);
+  return clmul32_classes(x0, x1, x2, x3, y[0], y[1], y[2], y[3]);
 }
 __device__ __forceinline__ void clmul64_split(uint64_t a, const uint32_t (*y)[4], uint64_t& lo, uint64_t& hi) {
   const uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32);
