@@ -121,12 +121,30 @@ constexpr size_t ZC_CONST_BYTES = (sizeof(ZcConsts) + 15) & ~size_t(15);
 
 // Byte b of a word, zero-extended: one byte-permute.
 __device__ __forceinline__ uint32_t byte_of(uint32_t v, int b) { return __byte_perm(v, 0, 0x4440 | b); }
+// Every byte of v set to 0xFF where its bit 7 is set (prmt with the sign-replicate bit
+// set in each selector nibble, which __byte_perm does not expose).
+__device__ __forceinline__ uint32_t msb_spread(uint32_t v) {
+  uint32_t r;
+  asm("prmt.b32 %0, %1, %2, 0xBA98;" : "=r"(r) : "r"(v), "r"(0u));
+  return r;
+}
+// Four GF(2^8) products (AES polynomial) of packed bytes, shift-and-add in registers.
+__device__ __forceinline__ uint32_t gf8_mul4(uint32_t a, uint32_t b) {
+  uint32_t r = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    r ^= a & msb_spread(b << (7 - k));  // bit k of each byte of b selects a * x^k
+    if (k < 7) a = ((a << 1) & 0xFEFEFEFEu) ^ (msb_spread(a) & 0x1B1B1B1Bu);
+  }
+  return r;
+}
 
 // P_ab: one team of 16 threads per xo, thread = four Lambda points; no block barriers
 // after the constants are staged. Per row x = 8M + K the team extends the a and b rows
-// (8 byte-table lookups each), multiplies pointwise in GF(2^8) through the 64 KB product
-// table and accumulates e_K * p into g_M; then F = sum_M x^M phi8(g_M) (Horner) and
-// acc += eq_o(xo) * F. Tables: about 199 KB of shared memory, one block per SM.
+// (8 byte-table lookups each), multiplies pointwise in GF(2^8) (the 64 KB product table is
+// symmetric, so its index may put either factor high) and accumulates e_K * p into g_M;
+// then F = sum_M x^M phi8(g_M) (Horner) and acc += eq_o(xo) * F. Tables: about 199 KB of
+// shared memory, one block per SM.
 constexpr int ZC_TEAMS = 32;  // teams per block (512 threads)
 __global__ void __launch_bounds__(16 * ZC_TEAMS, 1)
 zc_round1_ab_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, uint64_t n_xo,
@@ -167,12 +185,19 @@ zc_round1_ab_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, ui
             eb ^= *reinterpret_cast<const uint32_t*>(extb + c * 16384 + (byte_of(b0, c) << 6)) ^
                   *reinterpret_cast<const uint32_t*>(extb + (c + 4) * 16384 + (byte_of(b1, c) << 6));
           }
-          // four GF(2^8) products by table (shared memory; the table is symmetric, so the
-          // index may put either operand high), each scaled by e_K through its mulk table
-          const uint32_t i01 = __byte_perm(ea, eb, 0x5140), i23 = __byte_perm(ea, eb, 0x7362);
+          // the four GF(2^8) products, then e_K times each (mulk table): half of the rows take
+          // the products from the 64 KB product table (shared-memory pipe), half compute them
+          // in registers (logic pipe), which balances the two pipes
           const uint8_t* mk = C.mulk[2 * kk + h];
-          g ^= (uint32_t)mk[C.gmul[i01 & 0xFFFF]] | ((uint32_t)mk[C.gmul[i01 >> 16]] << 8) |
-               ((uint32_t)mk[C.gmul[i23 & 0xFFFF]] << 16) | ((uint32_t)mk[C.gmul[i23 >> 16]] << 24);
+          if (h == 0) {
+            const uint32_t i01 = __byte_perm(ea, eb, 0x5140), i23 = __byte_perm(ea, eb, 0x7362);
+            g ^= (uint32_t)mk[C.gmul[i01 & 0xFFFF]] | ((uint32_t)mk[C.gmul[i01 >> 16]] << 8) |
+                 ((uint32_t)mk[C.gmul[i23 & 0xFFFF]] << 16) | ((uint32_t)mk[C.gmul[i23 >> 16]] << 24);
+          } else {
+            const uint32_t p = gf8_mul4(ea, eb);
+            g ^= (uint32_t)mk[byte_of(p, 0)] | ((uint32_t)mk[byte_of(p, 1)] << 8) | ((uint32_t)mk[byte_of(p, 2)] << 16) |
+                 ((uint32_t)mk[byte_of(p, 3)] << 24);
+          }
         }
       }
       G[M] = g;
