@@ -69,8 +69,9 @@ __global__ void ntt_layer_kernel(F128d* __restrict__ data, uint32_t lanes, uint3
 // block of the first fused layer) for a slice of lanes; each fused layer pairs positions
 // within that set. Fused layer k meets 2^k twiddles; the block stages all 2^nl - 1 of them
 // once, already split for mul_split, after the positions' data.
+constexpr uint32_t NTT_MAX_THREADS = 320;  // with 3 blocks per SM: at most 64 registers a thread
 template <int NL>
-__global__ void ntt_fused_kernel(F128d* __restrict__ data, uint32_t lanes, uint32_t log_d, uint32_t layer,
+__global__ void __launch_bounds__(NTT_MAX_THREADS, 3) ntt_fused_kernel(F128d* __restrict__ data, uint32_t lanes, uint32_t log_d, uint32_t layer,
                                  const F128d* __restrict__ tw, uint32_t lane_tile) {
   extern __shared__ F128d sm[];  // [2^NL][lane_tile], then F128split[2^NL - 1]
   const uint32_t P = 1u << NL;
@@ -89,7 +90,15 @@ __global__ void ntt_fused_kernel(F128d* __restrict__ data, uint32_t lanes, uint3
   // twiddle (k, blk) at tws[2^k - 1 + blk]: its global block at layer + k is (outer << k) + blk
   for (uint32_t t = threadIdx.x; t < P - 1; t += blockDim.x) {
     const uint32_t k = 31 - __clz(t + 1), blk = t + 1 - (1u << k);
-    tws[t] = split_factor(tw[(1ull << (layer + k)) - 1 + (outer << k) + blk]);
+    const F128d v = tw[(1ull << (layer + k)) - 1 + (outer << k) + blk];
+    const uint64_t hl[3] = {v.lo, v.hi, v.lo ^ v.hi};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {  // split_factor(v), stored as it is formed
+      const uint32_t y0 = (uint32_t)hl[q], y1 = (uint32_t)(hl[q] >> 32);
+      split_classes(y0, tws[t].w[3 * q]);
+      split_classes(y1, tws[t].w[3 * q + 1]);
+      split_classes(y0 ^ y1, tws[t].w[3 * q + 2]);
+    }
   }
   for (uint32_t i = threadIdx.x; i < P * nl_here; i += blockDim.x) {
     uint32_t pos = i / nl_here, l = i - pos * nl_here;
@@ -126,7 +135,7 @@ __global__ void ntt_fused_kernel(F128d* __restrict__ data, uint32_t lanes, uint3
   }
 }
 
-// Threads per fused-NTT block for a lane tile: among the multiples of 32 in [192, 384], the
+// Threads per fused-NTT block for a lane tile: among the multiples of 32 in [192, 320], the
 // one with the most busy resident warps per SM (resident warps, capped at 32, times the
 // fraction of threads with a butterfly in a layer's passes). Cached per device and tile.
 template <int NL>
@@ -139,7 +148,7 @@ static uint32_t ntt_block_threads(uint32_t lane_tile, size_t smem) {
   if (best) return best;
   const uint32_t butterflies = (1u << (NL - 1)) * lane_tile;
   double best_score = -1.0;
-  for (uint32_t t = 192; t <= 384; t += 32) {
+  for (uint32_t t = 192; t <= NTT_MAX_THREADS; t += 32) {
     int blocks = 0;
     CUDA_OK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, ntt_fused_kernel<NL>, (int)t, smem));
     const uint32_t passes = (butterflies + t - 1) / t;
