@@ -17,15 +17,6 @@
 
 namespace flock {
 
-// Plain copy of a streaming SHA-256 state (same meaning on host and device).
-struct ShaState {
-  uint32_t h[8];
-  uint8_t buf[64];
-  uint64_t total;  // bytes absorbed
-  uint32_t blen;   // bytes pending in buf
-  uint32_t pad;
-};
-
 enum : uint8_t { OP_DOMAIN = 1, OP_LABEL = 2, OP_OBSERVE = 3, OP_SQUEEZE = 4, OP_BYTES = 5 };
 enum : uint8_t { KIND_NONE = 0, KIND_SCALAR = 1, KIND_SLICE = 2 };
 
@@ -182,24 +173,6 @@ class Transcript {
   }
 
   std::array<uint8_t, 32> state_digest() const { return state_.digest(); }
-
-  // The running SHA-256 state, for continuing the same transcript elsewhere (the
-  // device-resident round loops) and resuming it here afterwards.
-  ShaState export_state() const {
-    ShaState s;
-    memcpy(s.h, state_.h, sizeof(s.h));
-    memcpy(s.buf, state_.buf, sizeof(s.buf));
-    s.total = state_.total;
-    s.blen = state_.blen;
-    s.pad = 0;
-    return s;
-  }
-  void import_state(const ShaState& s) {
-    memcpy(state_.h, s.h, sizeof(s.h));
-    memcpy(state_.buf, s.buf, sizeof(s.buf));
-    state_.total = s.total;
-    state_.blen = s.blen;
-  }
 
  private:
   Sha256 state_;
