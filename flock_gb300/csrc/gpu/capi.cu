@@ -35,16 +35,14 @@ std::shared_ptr<Statement> statement_for_shape(HashKind h, uint32_t n) {
 }
 // u64 proof_len | bincode proof | u64 cap_len | cap | ab_value | c_value
 std::vector<uint8_t> make_bundle(const ProveResult& R) {
-  std::vector<uint8_t> pb = proof_bytes(R.proof);
-  std::vector<uint8_t> out;
-  out.reserve(8 + pb.size() + 8 + 32 * R.cap.size() + 32);
-  auto u64 = [&](uint64_t v) { for (int i = 0; i < 8; ++i) out.push_back((uint8_t)(v >> (8 * i))); };
-  u64(pb.size());
-  out.insert(out.end(), pb.begin(), pb.end());
-  u64(R.cap.size());
-  for (auto& h : R.cap) out.insert(out.end(), h.begin(), h.end());
-  for (F128 v : {R.claims.ab_value, R.claims.c_value}) { u64(v.lo); u64(v.hi); }
-  return out;
+  Bincode bc;
+  bc.u64(0);  // proof length, patched below
+  bc.merged(R.proof);
+  Bincode::put64(bc.out.data(), bc.out.size() - 8);
+  bc.vh(R.cap);
+  bc.f128(R.claims.ab_value);
+  bc.f128(R.claims.c_value);
+  return std::move(bc.out);
 }
 }  // namespace flock
 

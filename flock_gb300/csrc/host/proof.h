@@ -15,6 +15,7 @@
 #pragma once
 #include "field.h"
 #include <array>
+#include <cstring>
 #include <vector>
 
 namespace flock {
@@ -101,16 +102,48 @@ struct ProofClaims {
 };
 
 // ---- bincode writer --------------------------------------------------------------
+// Writes grow the buffer once per value or per vector (a proof is hundreds of KB; a
+// byte-at-a-time writer spent about a millisecond of host time per proof here).
 struct Bincode {
   std::vector<uint8_t> out;
-  void u64(uint64_t v) { for (int i = 0; i < 8; ++i) out.push_back((uint8_t)(v >> (8 * i))); }
-  void f128(const F128& v) { u64(v.lo); u64(v.hi); }
-  void f256(const F256& v) { f128(v.c0); f128(v.c1); }
-  void hash(const Hash& h) { out.insert(out.end(), h.begin(), h.end()); }
-  void vf(const std::vector<F128>& v) { u64(v.size()); for (auto& x : v) f128(x); }
-  void vu(const std::vector<uint64_t>& v) { u64(v.size()); for (auto x : v) u64(x); }
-  void vp(const std::vector<Pair128>& v) { u64(v.size()); for (auto& p : v) { f128(p.first); f128(p.second); } }
-  void vh(const std::vector<Hash>& v) { u64(v.size()); for (auto& h : v) hash(h); }
+  Bincode() { out.reserve(size_t(1) << 20); }
+  uint8_t* grow(size_t n) {
+    const size_t at = out.size();
+    out.resize(at + n);
+    return out.data() + at;
+  }
+  static void put64(uint8_t* p, uint64_t v) {
+    for (int i = 0; i < 8; ++i) p[i] = (uint8_t)(v >> (8 * i));
+  }
+  static uint8_t* put128(uint8_t* p, const F128& v) {
+    put64(p, v.lo);
+    put64(p + 8, v.hi);
+    return p + 16;
+  }
+  void u64(uint64_t v) { put64(grow(8), v); }
+  void f128(const F128& v) { put128(grow(16), v); }
+  void f256(const F256& v) { put128(put128(grow(32), v.c0), v.c1); }
+  void hash(const Hash& h) { memcpy(grow(32), h.data(), 32); }
+  void vf(const std::vector<F128>& v) {
+    u64(v.size());
+    uint8_t* p = grow(16 * v.size());
+    for (auto& x : v) p = put128(p, x);
+  }
+  void vu(const std::vector<uint64_t>& v) {
+    u64(v.size());
+    uint8_t* p = grow(8 * v.size());
+    for (auto x : v) { put64(p, x); p += 8; }
+  }
+  void vp(const std::vector<Pair128>& v) {
+    u64(v.size());
+    uint8_t* p = grow(32 * v.size());
+    for (auto& q : v) p = put128(put128(p, q.first), q.second);
+  }
+  void vh(const std::vector<Hash>& v) {
+    u64(v.size());
+    uint8_t* p = grow(32 * v.size());
+    for (auto& h : v) { memcpy(p, h.data(), 32); p += 32; }
+  }
   void vvf(const std::vector<std::vector<F128>>& v) { u64(v.size()); for (auto& x : v) vf(x); }
 
   void zc(const ZerocheckProof& p) {
