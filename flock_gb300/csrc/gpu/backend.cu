@@ -183,7 +183,14 @@ GpuBackend::GpuBackend(const Statement& s) : S(s) {
   zc_tabs_ = dmalloc<F128d>(zc_tabs_cap_, owned_, device_bytes_);
   CUDA_OK(cudaStreamCreateWithFlags(&pow_st_, cudaStreamNonBlocking));
   d_pow_ = dmalloc<unsigned long long>(1, owned_, device_bytes_);
-  CUDA_OK(cudaMallocHost(&h_pow_, sizeof(unsigned long long)));
+  CUDA_OK(cudaMemset(d_pow_, 0xFF, sizeof(unsigned long long)));
+  pow_counter_ = dmalloc<uint32_t>(1, owned_, device_bytes_);
+  CUDA_OK(cudaMemset(pow_counter_, 0, sizeof(uint32_t)));
+  CUDA_OK(cudaHostAlloc(&h_pow_, sizeof(unsigned long long), cudaHostAllocMapped));
+  CUDA_OK(cudaHostGetDevicePointer(&d_pow_out_, h_pow_, 0));
+  CUDA_OK(cudaHostAlloc(&h_pow_flag_, 64, cudaHostAllocMapped));
+  CUDA_OK(cudaHostGetDevicePointer(&d_pow_flag_, h_pow_flag_, 0));
+  *(volatile uint32_t*)h_pow_flag_ = 0;
   // twiddles of the L0 transform; host tables used by every prove
   tw0_ = twiddles(S.k_code);
   (void)moore_inverse();
@@ -200,6 +207,7 @@ GpuBackend::~GpuBackend() {
   cudaFreeHost(h_red_);
   cudaFreeHost(h_stage_);
   cudaFreeHost(h_pow_);
+  cudaFreeHost(h_pow_flag_);
   cudaFreeHost(h_pub_);
   cudaFreeHost(h_flag_);
   cudaStreamDestroy(pow_st_);
@@ -279,11 +287,11 @@ uint64_t GpuBackend::gpu_pow(const std::array<uint8_t, 32>& digest, uint32_t bit
   // ~e^-16 chance that a window of 16 * 2^bits nonces holds no solution; then the next one
   const uint64_t window = uint64_t(16) << bits;
   for (uint64_t start = 0;; start += window) {
-    CUDA_OK(cudaMemsetAsync(d_pow_, 0xFF, sizeof(unsigned long long), pow_st_));
-    launch_pow(words, bits, start, window, d_pow_, pow_st_);
-    CUDA_OK(cudaMemcpyAsync(h_pow_, d_pow_, sizeof(unsigned long long), cudaMemcpyDeviceToHost, pow_st_));
-    CUDA_OK(cudaStreamSynchronize(pow_st_));
-    if (*h_pow_ != ~0ull) return *h_pow_;
+    const uint32_t seq = ++pow_seq_;
+    launch_pow(words, bits, start, window, d_pow_, pow_counter_, d_pow_out_, d_pow_flag_, seq, pow_st_);
+    wait_flag(h_pow_flag_, seq, pow_st_);
+    const unsigned long long v = *(volatile unsigned long long*)h_pow_;
+    if (v != ~0ull) return v;
   }
 }
 PowSearchFn GpuBackend::pow_search() {
@@ -342,8 +350,9 @@ std::vector<F128> GpuBackend::read_published(uint32_t seq, uint32_t width) {
 // a short hot spin for the common case of a message a few microseconds away, then a spin
 // that yields the core on every pass, so that concurrent provers' host work (assists,
 // transcripts) is not starved by waiting threads. A stalled stream is reported after 20 s.
-void GpuBackend::wait_published(uint32_t seq) {
-  const volatile uint32_t* f = h_flag_;
+void GpuBackend::wait_published(uint32_t seq) { wait_flag(h_flag_, seq, st_); }
+void GpuBackend::wait_flag(const uint32_t* flag, uint32_t seq, cudaStream_t stream) {
+  const volatile uint32_t* f = flag;
   uint64_t spins = 0;
   double t0 = 0;
   while (*f != seq) {
@@ -352,8 +361,8 @@ void GpuBackend::wait_published(uint32_t seq) {
     if ((spins & 0x3FFF) == 0) {
       double t = now_ms();
       if (t0 == 0) t0 = t;
-      else if (t - t0 > 20000) throw std::runtime_error("device reduction did not publish within 20 s");
-      cudaError_t e = cudaStreamQuery(st_);
+      else if (t - t0 > 20000) throw std::runtime_error("device result not published within 20 s");
+      cudaError_t e = cudaStreamQuery(stream);
       if (e != cudaSuccess && e != cudaErrorNotReady) CUDA_OK(e);
     }
   }

@@ -181,6 +181,9 @@ class GpuBackend : public ProverBackend {
   uint32_t* d_flag_ = nullptr;
   uint32_t seq_ = 0;
   void wait_published(uint32_t seq);
+  // Spin until the mapped flag holds seq (bounded: an error after 20 s, stream errors
+  // reported as they occur).
+  void wait_flag(const uint32_t* flag, uint32_t seq, cudaStream_t stream);
   std::vector<F128> read_published(uint32_t seq, uint32_t width);
   uint32_t* pub_counter_ = nullptr;  // ticket counter of in-kernel publication (device)
   FusedPublish fused_publish() { FusedPublish p; p.out = d_pub_; p.flag = d_flag_; p.counter = pub_counter_; p.seq = ++seq_; return p; }
@@ -191,8 +194,13 @@ class GpuBackend : public ProverBackend {
 
   std::mutex pow_mu_;
   cudaStream_t pow_st_ = nullptr;
-  unsigned long long* d_pow_ = nullptr;
-  unsigned long long* h_pow_ = nullptr;
+  unsigned long long* d_pow_ = nullptr;      // running minimum of the current search (device)
+  uint32_t* pow_counter_ = nullptr;          // ticket counter of the current search (device)
+  unsigned long long* h_pow_ = nullptr;      // result, mapped host memory
+  unsigned long long* d_pow_out_ = nullptr;  // its device alias
+  uint32_t* h_pow_flag_ = nullptr;           // sequence number of the last finished search (mapped)
+  uint32_t* d_pow_flag_ = nullptr;
+  uint32_t pow_seq_ = 0;
   uint64_t gpu_pow(const std::array<uint8_t, 32>& digest, uint32_t bits);
 
   F128d* part_ = nullptr;

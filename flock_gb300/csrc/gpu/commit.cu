@@ -245,39 +245,64 @@ void launch_merkle(const F128d* rows, uint32_t lanes, uint64_t n_leaves, uint8_t
   }
 }
 
-// ---- transcript proof of work: the smallest nonce in [start, start + count) whose
-// SHA256(digest || nonce_le) has `bits` leading zero bits (challenger.rs:1100-1140)
-__global__ void pow_kernel(uint4 dlo, uint4 dhi, uint32_t bits, uint64_t start, uint64_t count,
-                           unsigned long long* result) {
-  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= count) return;
-  uint64_t nonce = start + i;
-  uint32_t w[16];
-  w[0] = bswap32(dlo.x); w[1] = bswap32(dlo.y); w[2] = bswap32(dlo.z); w[3] = bswap32(dlo.w);
-  w[4] = bswap32(dhi.x); w[5] = bswap32(dhi.y); w[6] = bswap32(dhi.z); w[7] = bswap32(dhi.w);
-  w[8] = bswap32((uint32_t)nonce);
-  w[9] = bswap32((uint32_t)(nonce >> 32));
-  w[10] = 0x80000000u;
+// ---- transcript proof of work (challenger.rs:1100-1140): the smallest nonce in
+// [start, start + count) whose SHA256(digest || nonce_le) has `bits` leading zero bits,
+// or ~0. Each block folds its minimum into *dmin; the last block to
+// finish (ticket counter) reads and resets *dmin, writes the result to mapped host memory,
+// then the sequence number, and resets the counter: one launch per search, no copies.
+__global__ void __launch_bounds__(256) pow_kernel(uint4 dlo, uint4 dhi, uint32_t bits, uint64_t start, uint64_t count,
+                                                  unsigned long long* dmin, uint32_t* counter, unsigned long long* out,
+                                                  uint32_t* flag, uint32_t seq) {
+  __shared__ unsigned long long bmin;
+  __shared__ uint32_t ticket;
+  if (threadIdx.x == 0) bmin = ~0ull;
+  __syncthreads();
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) {
+    const uint64_t nonce = start + i;
+    uint32_t w[16];
+    w[0] = bswap32(dlo.x); w[1] = bswap32(dlo.y); w[2] = bswap32(dlo.z); w[3] = bswap32(dlo.w);
+    w[4] = bswap32(dhi.x); w[5] = bswap32(dhi.y); w[6] = bswap32(dhi.z); w[7] = bswap32(dhi.w);
+    w[8] = bswap32((uint32_t)nonce);
+    w[9] = bswap32((uint32_t)(nonce >> 32));
+    w[10] = 0x80000000u;
 #pragma unroll
-  for (int k = 11; k < 15; ++k) w[k] = 0;
-  w[15] = 320;
-  uint32_t st[8];
-  sha256_init(st);
-  sha256_compress(st, w);
-  bool ok = true;
-  uint32_t need = bits;
+    for (int k = 11; k < 15; ++k) w[k] = 0;
+    w[15] = 320;
+    uint32_t st[8];
+    sha256_init(st);
+    sha256_compress(st, w);
+    bool ok = true;
+    uint32_t need = bits;
 #pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    if (need >= 32) { ok &= st[k] == 0; need -= 32; }
-    else if (need > 0) { ok &= (st[k] >> (32 - need)) == 0; need = 0; }
+    for (int k = 0; k < 8; ++k) {
+      if (need >= 32) { ok &= st[k] == 0; need -= 32; }
+      else if (need > 0) { ok &= (st[k] >> (32 - need)) == 0; need = 0; }
+    }
+    if (ok) atomicMin(&bmin, (unsigned long long)nonce);
   }
-  if (ok) atomicMin(result, (unsigned long long)nonce);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (bmin != ~0ull) atomicMin(dmin, bmin);
+    __threadfence();
+    ticket = atomicAdd(counter, 1u);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && ticket == gridDim.x - 1) {
+    __threadfence();
+    const unsigned long long m = atomicExch(dmin, ~0ull);
+    *counter = 0;
+    *(volatile unsigned long long*)out = m;
+    __threadfence_system();
+    *(volatile uint32_t*)flag = seq;
+  }
 }
-void launch_pow(const uint32_t digest_le[8], uint32_t bits, uint64_t start, uint64_t count,
-                unsigned long long* d_result, cudaStream_t s) {
+void launch_pow(const uint32_t digest_le[8], uint32_t bits, uint64_t start, uint64_t count, unsigned long long* d_min,
+                uint32_t* d_counter, unsigned long long* out, uint32_t* flag, uint32_t seq, cudaStream_t s) {
   uint4 lo = make_uint4(digest_le[0], digest_le[1], digest_le[2], digest_le[3]);
   uint4 hi = make_uint4(digest_le[4], digest_le[5], digest_le[6], digest_le[7]);
-  pow_kernel<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(lo, hi, bits, start, count, d_result);
+  pow_kernel<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(lo, hi, bits, start, count, d_min, d_counter, out, flag,
+                                                             seq);
   LAUNCH_OK();
 }
 
