@@ -324,9 +324,50 @@ inline FrobeniusAssistProof prove_anchor_assist(Transcript& T, const std::vector
   auto comb4 = [](F128 x, const std::array<F128, 4>& a, F128 y, const std::array<F128, 4>& b) {
     return std::array<F128, 4>{x * a[0] + y * b[0], x * a[1] + y * b[1], x * a[2] + y * b[2], x * a[3] + y * b[3]};
   };
+  // Per-run work of layer l in one parallel pass over (statement, run chunk): first fold
+  // the run partials by layer l - 1's bits and challenges (rc_prev, rd_prev), then add
+  // part * S_{l+1} into the chunk's (c, d) buckets for layer l. Chunk buckets are summed
+  // (XOR) afterwards, so the result does not depend on the split.
+  constexpr size_t NCH = 32;
+  using Bucket = std::array<std::array<F128, 4>, 4>;
+  std::vector<Bucket> chunk_b(S.size() * NCH);
+  std::vector<Bucket> B(S.size());
+  auto run_pass = [&](int l, F128 rc_prev, F128 rd_prev) {
+    parallel_for(S.size() * NCH, [&](size_t task) {
+      const size_t si = task / NCH, ch = task % NCH;
+      const AssistStatement& a = sts[si];
+      St& s = S[si];
+      const size_t R = a.w.size(), r0 = R * ch / NCH, r1 = R * (ch + 1) / NCH;
+      Bucket bk{};
+      const bool fold = l > 0 && l - 1 >= s.uniform, seed = l > 0 && l == s.uniform;
+      const bool bucket = l < L && l >= s.uniform;
+      const F128 rc1 = rc_prev + F128::one(), rd1 = rd_prev + F128::one();
+      for (size_t r = r0; r < r1; ++r) {
+        if (seed) s.part[r] = a.w[r] * s.common;
+        if (fold) {
+          int c = (int)((a.t[r].first >> (l - 1)) & 1), d = (int)((a.t[r].second >> (l - 1)) & 1);
+          s.part[r] = s.part[r] * (c ? rc_prev : rc1) * (d ? rd_prev : rd1);
+        }
+        if (bucket) {
+          int c = (int)((a.t[r].first >> l) & 1), d = (int)((a.t[r].second >> l) & 1);
+          const auto& nx = s.sfx[l + 1][r];
+          for (int o = 0; o < 4; ++o) bk[c + 2 * d][o] += s.part[r] * nx[o];
+        }
+      }
+      chunk_b[task] = bk;
+    });
+    for (size_t si = 0; si < S.size(); ++si) {
+      Bucket acc{};
+      for (size_t ch = 0; ch < NCH; ++ch)
+        for (int cd = 0; cd < 4; ++cd)
+          for (int o = 0; o < 4; ++o) acc[cd][o] += chunk_b[si * NCH + ch][cd][o];
+      B[si] = acc;
+    }
+  };
+  run_pass(0, F128(), F128());
   for (int l = 0; l < L; ++l) {
     // per statement: u[cd] = prefix * M_l(c, d); bucket[cd] = sum over runs with bits (c,d) of part * S_{l+1}
-    std::vector<std::array<std::array<F128, 4>, 4>> U(S.size()), B(S.size());
+    std::vector<std::array<std::array<F128, 4>, 4>> U(S.size());
     for (size_t si = 0; si < S.size(); ++si) {
       St& s = S[si];
       for (int cd = 0; cd < 4; ++cd) {
@@ -337,17 +378,10 @@ inline FrobeniusAssistProof prove_anchor_assist(Transcript& T, const std::vector
           for (int st = 0; st < 4; ++st) acc += s.prefix[st] * M[st][o];
           U[si][cd][o] = acc;
         }
-        B[si][cd] = {F128(), F128(), F128(), F128()};
       }
-      const AssistStatement& a = sts[si];
-      if (l < s.uniform) {
+      if (l < s.uniform) {  // every run has the bits ucd here: one bucket, from the precomputed sums
+        for (int cd = 0; cd < 4; ++cd) B[si][cd] = {F128(), F128(), F128(), F128()};
         for (int o = 0; o < 4; ++o) B[si][s.ucd][o] = s.common * s.ws[l][o];
-      } else {
-        for (size_t r = 0; r < a.w.size(); ++r) {
-          int c = (int)((a.t[r].first >> l) & 1), d = (int)((a.t[r].second >> l) & 1);
-          auto& nx = s.sfx[l + 1][r];
-          for (int o = 0; o < 4; ++o) B[si][c + 2 * d][o] += s.part[r] * nx[o];
-        }
       }
     }
     F128 g1, gi;
@@ -380,20 +414,12 @@ inline FrobeniusAssistProof prove_anchor_assist(Transcript& T, const std::vector
     F128 rd1 = rd + F128::one();
     for (size_t si = 0; si < S.size(); ++si) {
       S[si].prefix = comb4(rd1, folded[si].first, rd, folded[si].second);
-      // fold the run partials by the layer's (c, d) bits
-      const AssistStatement& a = sts[si];
       St& s = S[si];
-      if (l < s.uniform) {
-        s.common = s.common * ((s.ucd & 1) ? rc : rc1) * ((s.ucd & 2) ? rd : rd1);
-        if (l + 1 == s.uniform)
-          for (size_t r = 0; r < a.w.size(); ++r) s.part[r] = a.w[r] * s.common;
-      } else {
-        for (size_t r = 0; r < a.w.size(); ++r) {
-          int c = (int)((a.t[r].first >> l) & 1), d = (int)((a.t[r].second >> l) & 1);
-          s.part[r] = s.part[r] * (c ? rc : rc1) * (d ? rd : rd1);
-        }
-      }
+      if (l < s.uniform) s.common = s.common * ((s.ucd & 1) ? rc : rc1) * ((s.ucd & 2) ? rd : rd1);
     }
+    // the run partials fold by this layer's bits in the next layer's pass (not needed after
+    // the last layer)
+    if (l + 1 < L) run_pass(l + 1, rc, rd);
   }
   return pf;
 }
@@ -487,10 +513,20 @@ inline MultipointTwistedProof prove_multipoint(Transcript& T, const AlignedJagge
   });
   std::vector<F128> s;  // bound challenges
   std::vector<F128> c1v(R * 128), civ(R * 128);
-  auto message = [&](uint32_t t, F128& g1, F128& gi) {
+  // absorb the variable bound in round t (challenge r) into the prefix products
+  auto absorb = [&](size_t ij, uint32_t t, F128 r) {
+    size_t i = ij / 128, j = ij % 128;
+    F128 f = F128::one() + rp[j][t] + r;  // eq(rho_j[t], r)
+    if (t < n) f = f * (F128::one() + claims[i].z_row[t] + r);
+    P[i][j] = P[i][j] * f;
+  };
+  // message of round t; with bind_prev, each item first absorbs round t - 1's challenge
+  // (one parallel pass per round instead of two)
+  auto message = [&](uint32_t t, F128& g1, F128& gi, bool bind_prev, F128 r_prev) {
     g1 = F128(); gi = F128();
     if (t < n) {
       parallel_for(R * 128, [&](size_t ij) {
+        if (bind_prev) absorb(ij, t - 1, r_prev);
         size_t i = ij / 128, j = ij % 128;
         F128 c = P[i][j] * rowsuf[i][j * (n + 1) + t + 1] * Ccol[i][j];
         c1v[ij] = c * claims[i].z_row[t] * rp[j][t];
@@ -500,6 +536,7 @@ inline MultipointTwistedProof prove_multipoint(Transcript& T, const AlignedJagge
     } else {
       uint32_t b = t - n;
       parallel_for(R * 128, [&](size_t ij) {
+        if (bind_prev) absorb(ij, t - 1, r_prev);
         size_t i = ij / 128, j = ij % 128;
         {
           // column weights: u < b bound to s, u = b the round variable, u > b summed against rho_j
@@ -522,7 +559,7 @@ inline MultipointTwistedProof prove_multipoint(Transcript& T, const AlignedJagge
     }
   };
   F128 g1, gi;
-  message(0, g1, gi);
+  message(0, g1, gi, false, F128());
   for (uint32_t t = 0; t < m; ++t) {
     T.observe_f128(g1); T.observe_f128(gi);
     F128 r;
@@ -531,14 +568,7 @@ inline MultipointTwistedProof prove_multipoint(Transcript& T, const AlignedJagge
     pf.rounds.push_back({g1, gi});
     s.push_back(r);
     if (t + 1 == m) break;
-    // absorb the bound variable into the prefix products
-    parallel_for(R * 128, [&](size_t ij) {
-      size_t i = ij / 128, j = ij % 128;
-      F128 f = F128::one() + rp[j][t] + r;  // eq(rho_j[t], r)
-      if (t < n) f = f * (F128::one() + claims[i].z_row[t] + r);
-      P[i][j] = P[i][j] * f;
-    });
-    message(t + 1, g1, gi);
+    message(t + 1, g1, gi, true, r);
   }
   // ---- anchor at the endpoint rho'' = s
   F128 g_at;
