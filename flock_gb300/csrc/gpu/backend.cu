@@ -626,11 +626,11 @@ void GpuBackend::lc_start(F128 alpha, F128 beta, uint32_t pin, F128& e1, F128& e
 }
 
 void GpuBackend::lc_round(F128 r, bool last, F128& e1, F128& ei) {
-  uint32_t nb;
-  { Mark mk(this, ST_LINCHECK); nb = launch_lc_round(comb_, zv_, lc_len_, dev(r), !last, part_, st_); }
+  FusedPublish fp = last ? FusedPublish() : fused_publish();
+  { Mark mk(this, ST_LINCHECK); launch_lc_round(comb_, zv_, lc_len_, dev(r), !last, part_, st_, fp); }
   lc_len_ /= 2;
   if (!last) {
-    auto v = reduce(nb, 2);
+    auto v = read_published(fp.seq, 2);
     e1 = v[0];
     ei = v[1];
   }
@@ -780,15 +780,15 @@ Msg256 GpuBackend::lg_message(size_t d) {
   if (d == 1 || n == d) d = 1;
   Msg256 m;
   if (lg_base_) {
-    uint32_t nb;
-    { Mark mk(this, ST_LIGERITO); nb = launch_lg_message128(z_, lb128_, n, d, part_, st_); }
-    auto v = reduce(nb, 2);
+    FusedPublish fp = fused_publish();
+    { Mark mk(this, ST_LIGERITO); launch_lg_message128(z_, lb128_, n, d, part_, st_, fp); }
+    auto v = read_published(fp.seq, 2);
     m.u0 = F256(v[0]);
     m.u2 = F256(v[1]);
   } else {
-    uint32_t nb;
-    { Mark mk(this, ST_LIGERITO); nb = launch_lg_message256(lf_[lg_cur_], lb_[lg_cur_], n, d, part_, st_); }
-    auto v = reduce(nb, 4);
+    FusedPublish fp = fused_publish();
+    { Mark mk(this, ST_LIGERITO); launch_lg_message256(lf_[lg_cur_], lb_[lg_cur_], n, d, part_, st_, fp); }
+    auto v = read_published(fp.seq, 4);
     m.u0 = F256(v[0], v[1]);
     m.u2 = F256(v[2], v[3]);
   }
@@ -874,9 +874,9 @@ Msg256 GpuBackend::lg_introduce_eq(const std::vector<F128>& zp, F128& answer) {
   scr_off_ = 0;
   if ((uint64_t(1) << zp.size()) != lg_n_) throw std::runtime_error("OOD point size mismatch");
   EqSplit e = eq_split(zp, F128::one(), 10);
-  uint32_t nb;
-  { Mark mk(this, ST_LIGERITO); nb = launch_lg_intro_eq(lf_[lg_cur_], e.lo, e.lo_bits, e.hi, lg_n_, pend_, part_, st_); }
-  auto v = reduce(nb, 3);
+  FusedPublish fp = fused_publish();
+  { Mark mk(this, ST_LIGERITO); launch_lg_intro_eq(lf_[lg_cur_], e.lo, e.lo_bits, e.hi, lg_n_, pend_, part_, st_, fp); }
+  auto v = read_published(fp.seq, 3);
   answer = v[0];
   pend_induced_ = false;
   pend_n_ = lg_n_;
@@ -900,12 +900,12 @@ Msg256 GpuBackend::lg_introduce_induced(uint32_t ln, uint32_t log_rate, const st
   const F128d* dw = upload(w);
   F128d* y = static_cast<F128d*>(scratch(size_t(16) << log_d));
   const F128d* tw = twiddles(log_d);
-  uint32_t nb;
+  FusedPublish fp = fused_publish();
   {
     Mark mk(this, ST_LIGERITO);
-    nb = launch_lg_induced(dpos, dw, nq, ln, log_rate, tw, lf_[lg_cur_], y, pend_, part_, st_);
+    launch_lg_induced(dpos, dw, nq, ln, log_rate, tw, lf_[lg_cur_], y, pend_, part_, st_, fp);
   }
-  auto v = reduce(nb, 2);
+  auto v = read_published(fp.seq, 2);
   pend_induced_ = true;
   pend_n_ = uint64_t(1) << ln;
   Msg256 m;

@@ -92,7 +92,8 @@ void launch_lc_zvec(const F128d* z, uint32_t nu, uint32_t used_chunks, const F12
                     cudaStream_t s);
 uint32_t launch_lc_start(const F128d* ca, const F128d* cb, F128d alpha, F128d beta, uint32_t pin, uint32_t K,
                          F128d* comb, const F128d* zv, F128d* part, cudaStream_t s);                   // width 2
-uint32_t launch_lc_round(F128d* comb, F128d* zv, uint32_t len, F128d r, bool msg, F128d* part, cudaStream_t s);
+uint32_t launch_lc_round(F128d* comb, F128d* zv, uint32_t len, F128d r, bool msg, F128d* part, cudaStream_t s,
+                         FusedPublish pub = FusedPublish());
 uint32_t launch_lc_matrix_evals(const F128d* ca, const F128d* cb, const F128d* er, const F128d* zp, uint32_t K,
                                 F128d* part, cudaStream_t s);                                          // width 2
 void launch_lc_s_hat_v(const F128d* zv, const F128d* et, uint32_t n_tail, F128d* out, cudaStream_t s);
@@ -105,8 +106,10 @@ void launch_lg_eq_fill(const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi,
                        cudaStream_t s);
 uint32_t launch_lg_dot_eq(const F128d* f, uint32_t stride, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi,
                           uint64_t n, F128d* part, cudaStream_t s);                                    // width 1
-uint32_t launch_lg_message128(const F128d* f, const F128d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s);
-uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s);
+uint32_t launch_lg_message128(const F128d* f, const F128d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s,
+                              FusedPublish pub = FusedPublish());
+uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s,
+                              FusedPublish pub = FusedPublish());
 void launch_lg_fold128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, const F256d* r_dev, uint64_t d,
                        F256d* fo, F256d* bo, cudaStream_t s);
 uint32_t launch_lg_fold_msg256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, uint64_t d_fold, uint64_t d_msg,
@@ -117,10 +120,11 @@ void launch_lg_fold256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, 
 void launch_lg_code_switch(const F256d* f, const F256d* b, uint64_t n, F256d* fo, F256d* bo, cudaStream_t s);
 void launch_lg_replicate(const F256d* f, uint64_t msg, uint64_t total, F128d* mat, cudaStream_t s);
 uint32_t launch_lg_intro_eq(const F256d* f, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, uint64_t n,
-                            F128d* pend, F128d* part, cudaStream_t s);                                 // width 3
+                            F128d* pend, F128d* part, cudaStream_t s,
+                            FusedPublish pub = FusedPublish());  // width 3
 uint32_t launch_lg_induced(const uint64_t* pos, const F128d* w, uint32_t n_q, uint32_t ln, uint32_t log_rate,
                            const F128d* tw, const F256d* f, F128d* y, F128d* basis, F128d* part,
-                           cudaStream_t s);                                                            // width 2
+                           cudaStream_t s, FusedPublish pub = FusedPublish());  // width 2
 void launch_lg_glue(F256d* b, const F128d* p, F128d beta, uint64_t n, bool induced, cudaStream_t s);
 
 // rounds.cu

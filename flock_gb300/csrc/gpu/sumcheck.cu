@@ -663,7 +663,7 @@ uint32_t launch_lc_start(const F128d* ca, const F128d* cb, F128d alpha, F128d be
 // Bind the top variable of comb and zv (length len -> len/2) in place and emit the next
 // top-variable message over the bound vectors (pairs (i, i + len/4)).
 __global__ void lc_round_kernel(F128d* __restrict__ comb, F128d* __restrict__ zv, uint32_t len, F128d r, int msg,
-                                F128d* __restrict__ part) {
+                                F128d* __restrict__ part, FusedPublish pub) {
   __shared__ F128d sh[32];
   uint32_t h = len / 2, q = h / 2;
   F128d e1 = f128_zero(), ei = f128_zero();
@@ -690,11 +690,13 @@ __global__ void lc_round_kernel(F128d* __restrict__ comb, F128d* __restrict__ zv
   e1 = block_xor(e1, sh);
   ei = block_xor(ei, sh);
   if (threadIdx.x == 0) { part[blockIdx.x * 2] = e1; part[blockIdx.x * 2 + 1] = ei; }
+  if (pub.out) publish_if_last(part, 2, pub, sh);
 }
-uint32_t launch_lc_round(F128d* comb, F128d* zv, uint32_t len, F128d r, bool msg, F128d* part, cudaStream_t s) {
+uint32_t launch_lc_round(F128d* comb, F128d* zv, uint32_t len, F128d r, bool msg, F128d* part, cudaStream_t s,
+                         FusedPublish pub) {
   uint32_t q = len / 4;
   uint32_t blocks = std::max(1u, std::min((q + 255) / 256, 256u));
-  lc_round_kernel<<<blocks, 256, 0, s>>>(comb, zv, len, r, msg ? 1 : 0, part);
+  lc_round_kernel<<<blocks, 256, 0, s>>>(comb, zv, len, r, msg ? 1 : 0, part, pub);
   LAUNCH_OK();
   return blocks;
 }
@@ -844,7 +846,7 @@ __device__ __forceinline__ uint64_t pair_lo(uint64_t i, uint32_t d_log) {
   return ((i >> d_log) << (d_log + 1)) | (i & ((1ull << d_log) - 1));
 }
 __global__ void lg_message128_kernel(const F128d* __restrict__ f, const F128d* __restrict__ b, uint64_t n, uint32_t d_log,
-                                     F128d* __restrict__ part) {
+                                     F128d* __restrict__ part, FusedPublish pub) {
   __shared__ F128d sh[32];
   F128d u0 = f128_zero(), u2 = f128_zero();
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n / 2; p += (uint64_t)gridDim.x * blockDim.x) {
@@ -856,15 +858,17 @@ __global__ void lg_message128_kernel(const F128d* __restrict__ f, const F128d* _
   u0 = block_xor(u0, sh);
   u2 = block_xor(u2, sh);
   if (threadIdx.x == 0) { part[blockIdx.x * 2] = u0; part[blockIdx.x * 2 + 1] = u2; }
+  if (pub.out) publish_if_last(part, 2, pub, sh);
 }
-uint32_t launch_lg_message128(const F128d* f, const F128d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s) {
+uint32_t launch_lg_message128(const F128d* f, const F128d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s,
+                              FusedPublish pub) {
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n / 2 + 255) / 256, (uint64_t)sm_count() * 8));
-  lg_message128_kernel<<<blocks, 256, 0, s>>>(f, b, n, log2_distance(d), part);
+  lg_message128_kernel<<<blocks, 256, 0, s>>>(f, b, n, log2_distance(d), part, pub);
   LAUNCH_OK();
   return blocks;
 }
 __global__ void lg_message256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n, uint32_t d_log,
-                                     F128d* __restrict__ part) {
+                                     F128d* __restrict__ part, FusedPublish pub) {
   __shared__ F128d sh[32];
   F256d u0 = f256(f128_zero(), f128_zero()), u2 = u0;
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n / 2; p += (uint64_t)gridDim.x * blockDim.x) {
@@ -878,10 +882,12 @@ __global__ void lg_message256_kernel(const F256d* __restrict__ f, const F256d* _
     part[blockIdx.x * 4] = r0; part[blockIdx.x * 4 + 1] = r1;
     part[blockIdx.x * 4 + 2] = r2; part[blockIdx.x * 4 + 3] = r3;
   }
+  if (pub.out) publish_if_last(part, 4, pub, sh);
 }
-uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s) {
+uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s,
+                              FusedPublish pub) {
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n / 2 + 255) / 256, (uint64_t)sm_count() * 8));
-  lg_message256_kernel<<<blocks, 256, 0, s>>>(f, b, n, log2_distance(d), part);
+  lg_message256_kernel<<<blocks, 256, 0, s>>>(f, b, n, log2_distance(d), part, pub);
   LAUNCH_OK();
   return blocks;
 }
@@ -990,7 +996,7 @@ void launch_lg_replicate(const F256d* f, uint64_t msg, uint64_t total, F128d* ma
 // block (answer = sum f e, u0 = sum f[2j] e[2j], u2 = sum (f0 + f1)(e0 + e1)).
 __global__ void lg_intro_eq_kernel(const F256d* __restrict__ f, const F128d* __restrict__ eq_lo, uint32_t lo_bits,
                                    const F128d* __restrict__ eq_hi, uint64_t n, F128d* __restrict__ pend,
-                                   F128d* __restrict__ part) {
+                                   F128d* __restrict__ part, FusedPublish pub) {
   __shared__ F128d sh[32];
   F128d ans = f128_zero(), u0 = f128_zero(), u2 = f128_zero();
   for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n / 2; j += (uint64_t)gridDim.x * blockDim.x) {
@@ -1007,11 +1013,12 @@ __global__ void lg_intro_eq_kernel(const F256d* __restrict__ f, const F128d* __r
   u0 = block_xor(u0, sh);
   u2 = block_xor(u2, sh);
   if (threadIdx.x == 0) { part[blockIdx.x * 3] = ans; part[blockIdx.x * 3 + 1] = u0; part[blockIdx.x * 3 + 2] = u2; }
+  if (pub.out) publish_if_last(part, 3, pub, sh);
 }
 uint32_t launch_lg_intro_eq(const F256d* f, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, uint64_t n,
-                            F128d* pend, F128d* part, cudaStream_t s) {
+                            F128d* pend, F128d* part, cudaStream_t s, FusedPublish pub) {
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n / 2 + 255) / 256, (uint64_t)sm_count() * 8));
-  lg_intro_eq_kernel<<<blocks, 256, 0, s>>>(f, eq_lo, lo_bits, eq_hi, n, pend, part);
+  lg_intro_eq_kernel<<<blocks, 256, 0, s>>>(f, eq_lo, lo_bits, eq_hi, n, pend, part, pub);
   LAUNCH_OK();
   return blocks;
 }
@@ -1043,7 +1050,8 @@ __global__ void ntt_t_layer_kernel(F128d* __restrict__ y, uint32_t log_d, uint32
 // basis[i] = sum_rep y[rep * n + i]; with the split f (length 2n):
 // a = sum f[2i] basis[i], s = sum (f[2i] + f[2i+1]) basis[i].
 __global__ void lg_induced_fold_kernel(const F128d* __restrict__ y, uint32_t ln, uint32_t log_rate,
-                                       const F256d* __restrict__ f, F128d* __restrict__ basis, F128d* __restrict__ part) {
+                                       const F256d* __restrict__ f, F128d* __restrict__ basis, F128d* __restrict__ part,
+                                       FusedPublish pub) {
   __shared__ F128d sh[32];
   uint64_t n = 1ull << ln;
   F128d A = f128_zero(), Sm = f128_zero();
@@ -1058,9 +1066,11 @@ __global__ void lg_induced_fold_kernel(const F128d* __restrict__ y, uint32_t ln,
   A = block_xor(A, sh);
   Sm = block_xor(Sm, sh);
   if (threadIdx.x == 0) { part[blockIdx.x * 2] = A; part[blockIdx.x * 2 + 1] = Sm; }
+  if (pub.out) publish_if_last(part, 2, pub, sh);
 }
 uint32_t launch_lg_induced(const uint64_t* pos, const F128d* w, uint32_t n_q, uint32_t ln, uint32_t log_rate,
-                           const F128d* tw, const F256d* f, F128d* y, F128d* basis, F128d* part, cudaStream_t s) {
+                           const F128d* tw, const F256d* f, F128d* y, F128d* basis, F128d* part, cudaStream_t s,
+                           FusedPublish pub) {
   uint32_t log_d = ln + log_rate;
   CUDA_OK(cudaMemsetAsync(y, 0, (sizeof(F128d)) << log_d, s));
   lg_scatter_kernel<<<(n_q + 127) / 128, 128, 0, s>>>(pos, w, n_q, y);
@@ -1072,7 +1082,7 @@ uint32_t launch_lg_induced(const uint64_t* pos, const F128d* w, uint32_t n_q, ui
   }
   uint64_t n = 1ull << ln;
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, (uint64_t)sm_count() * 8));
-  lg_induced_fold_kernel<<<blocks, 256, 0, s>>>(y, ln, log_rate, f, basis, part);
+  lg_induced_fold_kernel<<<blocks, 256, 0, s>>>(y, ln, log_rate, f, basis, part, pub);
   LAUNCH_OK();
   return blocks;
 }
