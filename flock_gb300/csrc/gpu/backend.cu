@@ -414,8 +414,18 @@ void GpuBackend::witness(const uint8_t* inputs) {
   scr_off_ = 0;
   const void* src = d_user_inputs_;
   if (!src) {
-    memcpy(h_in_, inputs, in_bytes_);
-    CUDA_OK(cudaMemcpyAsync(d_in_, h_in_, in_bytes_, cudaMemcpyHostToDevice, st_));
+    // Host inputs: staged into pinned memory by the host thread pool, 8 MiB at a time, each
+    // group's copy to the device queued as soon as it is staged (it overlaps the next
+    // group's staging).
+    const size_t GROUP = size_t(8) << 20, CHUNK = size_t(512) << 10;
+    for (size_t g0 = 0; g0 < in_bytes_; g0 += GROUP) {
+      const size_t glen = std::min(GROUP, in_bytes_ - g0);
+      parallel_for((glen + CHUNK - 1) / CHUNK, [&](size_t c) {
+        const size_t off = g0 + c * CHUNK;
+        memcpy(h_in_ + off, inputs + off, std::min(CHUNK, g0 + glen - off));
+      });
+      CUDA_OK(cudaMemcpyAsync(d_in_ + g0, h_in_ + g0, glen, cudaMemcpyHostToDevice, st_));
+    }
     h2d_ += in_bytes_;
     src = d_in_;
   }
