@@ -71,8 +71,9 @@ __global__ void ntt_layer_kernel(F128d* __restrict__ data, uint32_t lanes, uint3
 // once, already split for mul_split, after the positions' data.
 constexpr uint32_t NTT_MAX_THREADS = 320;  // with 3 blocks per SM: at most 64 registers a thread
 template <int NL>
-__global__ void __launch_bounds__(NTT_MAX_THREADS, 3) ntt_fused_kernel(F128d* __restrict__ data, uint32_t lanes, uint32_t log_d, uint32_t layer,
-                                 const F128d* __restrict__ tw, uint32_t lane_tile) {
+__global__ void __launch_bounds__(NTT_MAX_THREADS, 3)
+ntt_fused_kernel(F128d* __restrict__ data, uint32_t lanes, uint32_t log_d, uint32_t layer, const F128d* __restrict__ tw,
+                 uint32_t lane_tile) {
   extern __shared__ F128d sm[];  // [2^NL][lane_tile], then F128split[2^NL - 1]
   const uint32_t P = 1u << NL;
   F128split* tws = reinterpret_cast<F128split*>(sm + P * lane_tile);
