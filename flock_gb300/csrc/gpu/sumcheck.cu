@@ -231,7 +231,8 @@ zc_svc_kernel(const F128d* __restrict__ z, uint64_t xo_per_block, const ZcConsts
               F128d* __restrict__ part) {
   __shared__ uint4 zt[SVC_TILE * SVC_WORDS];
   __shared__ F128d et[SVC_TILE];
-  const uint32_t t = threadIdx.x, limb = t >> 5, sh = 31 - (t & 31);
+  __shared__ F128d et4[SVC_TILE / 4][16];  // et4[q][v] = sum of et[4 q + k] over the bits k of v
+  const uint32_t t = threadIdx.x, limb = t >> 5, bit = t & 31;
   const uint32_t g = blockIdx.y;
   const uint64_t xo0 = (uint64_t)blockIdx.x * xo_per_block;
   const uint64_t chunk = 1ull << lo_bits;
@@ -250,15 +251,27 @@ zc_svc_kernel(const F128d* __restrict__ z, uint64_t xo_per_block, const ZcConsts
         zt[i] = z4[(xt + (i / SVC_WORDS)) * 64 + g * SVC_WORDS + (i % SVC_WORDS)];
       if (t < tile) et[t] = eq_lo[(xt + t) & (chunk - 1)];
       __syncthreads();
-      for (uint32_t x = 0; x < tile; ++x) {
-        const F128d e = et[x];
-        const uint32_t* row = reinterpret_cast<const uint32_t*>(zt + x * SVC_WORDS);
+      // four xo at a time: their bits t form a 4-bit index into the subset sums of their eq
+      // weights (one lookup instead of four masked additions). A tile of fewer than four xo
+      // leaves rows past the tile out of every subset sum, whatever bits they hold.
+      const uint32_t groups = (tile + 3) / 4;
+      for (uint32_t i = t; i < groups * 16; i += blockDim.x) {
+        const uint32_t q = i >> 4, v = i & 15;
+        F128d acc = f128_zero();
+#pragma unroll
+        for (uint32_t k = 0; k < 4; ++k)
+          if (((v >> k) & 1) && 4 * q + k < tile) acc += et[4 * q + k];
+        et4[q][v] = acc;
+      }
+      __syncthreads();
+      for (uint32_t q = 0; q < groups; ++q) {
+        const uint32_t* r0 = reinterpret_cast<const uint32_t*>(zt + (4 * q) * SVC_WORDS) + limb;
 #pragma unroll
         for (uint32_t w = 0; w < SVC_WORDS; ++w) {
-          const uint32_t word = row[4 * w + limb];
-          const uint64_t m = (uint64_t)(int64_t)((int32_t)(word << sh) >> 31);  // all ones iff bit t is set
-          U[w].lo ^= e.lo & m;
-          U[w].hi ^= e.hi & m;
+          const uint32_t v = ((r0[4 * w] >> bit) & 1) | (((r0[4 * SVC_WORDS + 4 * w] >> bit) & 1) << 1) |
+                             (((r0[8 * SVC_WORDS + 4 * w] >> bit) & 1) << 2) |
+                             (((r0[12 * SVC_WORDS + 4 * w] >> bit) & 1) << 3);
+          U[w] += et4[q][v];
         }
       }
     }
