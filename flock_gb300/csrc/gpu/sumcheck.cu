@@ -602,6 +602,7 @@ lc_zvec_kernel(const F128d* __restrict__ z, uint32_t nu, uint32_t n_split, const
                F128d* __restrict__ part) {
   __shared__ F128d wz[ZV_TILE];
   __shared__ F128d we[ZV_TILE];
+  __shared__ F128d we4[ZV_TILE / 4][16];  // we4[q][v] = sum of we[4 q + k] over the bits k of v
   uint32_t cc = blockIdx.x / n_split, sp = blockIdx.x % n_split;
   uint64_t rows = 1ull << nu, per = rows / n_split;
   uint64_t r0 = sp * per;
@@ -615,11 +616,23 @@ lc_zvec_kernel(const F128d* __restrict__ z, uint32_t nu, uint32_t n_split, const
       we[i] = eq[base + i];
     }
     __syncthreads();
-    for (uint32_t i = 0; i < n; ++i) {
-      const uint32_t* wl = reinterpret_cast<const uint32_t*>(&wz[i]);
-      uint64_t m = 0ull - (uint64_t)((wl[limb] >> sh) & 1);
-      acc.lo ^= we[i].lo & m;
-      acc.hi ^= we[i].hi & m;
+    // four rows at a time: their bits t index the subset sums of their eq weights (rows
+    // past n are left out of every subset sum)
+    const uint32_t groups = (n + 3) / 4;
+    for (uint32_t i = t; i < groups * 16; i += blockDim.x) {
+      const uint32_t q = i >> 4, v = i & 15;
+      F128d s4 = f128_zero();
+#pragma unroll
+      for (uint32_t k = 0; k < 4; ++k)
+        if (((v >> k) & 1) && 4 * q + k < n) s4 += we[4 * q + k];
+      we4[q][v] = s4;
+    }
+    __syncthreads();
+    for (uint32_t q = 0; q < groups; ++q) {
+      const uint32_t* w0 = reinterpret_cast<const uint32_t*>(&wz[4 * q]) + limb;  // 4 words per row
+      const uint32_t v = ((w0[0] >> sh) & 1) | (((w0[4] >> sh) & 1) << 1) | (((w0[8] >> sh) & 1) << 2) |
+                         (((w0[12] >> sh) & 1) << 3);
+      acc += we4[q][v];
     }
   }
   part[(uint64_t)blockIdx.x * 128 + t] = acc;
