@@ -18,6 +18,66 @@
 namespace flock {
 namespace oracle {
 
+// ---- host parallelism for the checker's bulk loops ------------------------------------
+// Contiguous chunks of [0, n) over the host thread pool. Every sum below is over GF(2^k)
+// (XOR), so per-chunk partial sums combine to the same bits in any split or order.
+inline size_t par_parts(size_t n, size_t grain = 1024) {
+  if (n < 2 * grain) return 1;
+  return std::min<size_t>(n / grain, 8 * (ThreadPool::instance().workers() + 1));
+}
+template <class Fn>
+inline void par_chunks(size_t n, Fn&& fn, size_t grain = 1024) {
+  const size_t parts = par_parts(n, grain);
+  if (parts <= 1) { if (n) fn(size_t(0), n); return; }
+  parallel_for(parts, [&](size_t p) { fn(n * p / parts, n * (p + 1) / parts); });
+}
+// Sum of per-chunk partials: fn(begin, end, acc) adds its chunk's terms into acc.
+template <class T, class Fn>
+inline T par_sum(size_t n, Fn&& fn) {
+  const size_t parts = par_parts(n);
+  std::vector<T> part(std::max<size_t>(parts, 1));
+  if (parts <= 1) { if (n) fn(size_t(0), n, part[0]); return part[0]; }
+  parallel_for(parts, [&](size_t p) { fn(n * p / parts, n * (p + 1) / parts, part[p]); });
+  T acc = part[0];
+  for (size_t p = 1; p < parts; ++p) acc = acc + part[p];
+  return acc;
+}
+struct Two128 {
+  F128 x, y;
+  Two128 operator+(const Two128& o) const { return {x + o.x, y + o.y}; }
+};
+struct Two256 {
+  F256 x, y;
+  Two256 operator+(const Two256& o) const { return {x + o.x, y + o.y}; }
+};
+// eq table of build_eq (field.h) with the widest layers expanded in parallel.
+inline std::vector<F128> par_build_eq(const std::vector<F128>& point, F128 scale = F128::one()) {
+  std::vector<F128> out(size_t(1) << point.size());
+  out[0] = scale;
+  for (size_t j = 0; j < point.size(); ++j) {
+    const size_t len = size_t(1) << j;
+    const F128 r = point[j], r1 = r + F128::one();
+    par_chunks(len, [&](size_t b, size_t e) {
+      for (size_t i = b; i < e; ++i) {
+        F128 v = out[i];
+        out[i + len] = v * r;
+        out[i] = v * r1;
+      }
+    });
+  }
+  return out;
+}
+// GF(2^8) product table (from gf8_mul) for the round-1 extension products.
+inline const std::vector<uint8_t>& gf8_mul_table() {
+  static const std::vector<uint8_t> t = [] {
+    std::vector<uint8_t> v(65536);
+    for (int a = 0; a < 256; ++a)
+      for (int b = 0; b < 256; ++b) v[a * 256 + b] = gf8_mul((uint8_t)a, (uint8_t)b);
+    return v;
+  }();
+  return t;
+}
+
 // ---- GF(2^8) additive NTT (ntt.rs:18-117) --------------------------------------------
 inline std::vector<uint8_t> gf8_twiddles(int k, uint8_t beta) {
   int n = 1 << k;
@@ -114,12 +174,16 @@ struct Ntt128 {
   // Interleaved SoA transform of `lanes` independent NTTs (data[pos * lanes + lane]),
   // layers [start, log_d).
   void forward_interleaved(F128* data, size_t lanes, uint32_t start) const {
+    if (log_d == 0) return;
     for (uint32_t layer = start; layer < log_d; ++layer) {
-      size_t half = size_t(1) << (log_d - layer - 1);
-      for (size_t block = 0; block < (size_t(1) << layer); ++block) {
-        F128 t = tw[(size_t(1) << layer) - 1 + block];
-        size_t bs = block << (log_d - layer);
-        for (size_t i0 = bs; i0 < bs + half; ++i0) {
+      const uint32_t hl = log_d - layer - 1;
+      const size_t half = size_t(1) << hl;
+      // butterfly j: block j >> hl, offset j & (half - 1)
+      par_chunks(size_t(1) << (log_d - 1), [&](size_t jb, size_t je) {
+        for (size_t j = jb; j < je; ++j) {
+          const size_t block = j >> hl;
+          const F128 t = tw[(size_t(1) << layer) - 1 + block];
+          const size_t i0 = (block << (hl + 1)) + (j & (half - 1));
           F128* u = data + i0 * lanes;
           F128* v = data + (i0 | half) * lanes;
           for (size_t l = 0; l < lanes; ++l) {
@@ -128,22 +192,26 @@ struct Ntt128 {
             v[l] = v[l] + nu;
           }
         }
-      }
+      });
     }
   }
 };
 
 inline std::vector<Hash> merkle_tree(const F128* data, size_t n_leaves, size_t leaf_words) {
   std::vector<Hash> tree(2 * n_leaves - 1);
-  for (size_t i = 0; i < n_leaves; ++i) tree[i] = Sha256::hash(data + i * leaf_words, leaf_words * 16);
+  par_chunks(n_leaves, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) tree[i] = Sha256::hash(data + i * leaf_words, leaf_words * 16);
+  });
   size_t rs = 0, rl = n_leaves;
   while (rl > 1) {
-    for (size_t i = 0; i < rl / 2; ++i) {
-      Sha256 h;
-      h.update(tree[rs + 2 * i].data(), 32);
-      h.update(tree[rs + 2 * i + 1].data(), 32);
-      tree[rs + rl + i] = h.digest();
-    }
+    par_chunks(rl / 2, [&](size_t b, size_t e) {
+      for (size_t i = b; i < e; ++i) {
+        Sha256 h;
+        h.update(tree[rs + 2 * i].data(), 32);
+        h.update(tree[rs + 2 * i + 1].data(), 32);
+        tree[rs + rl + i] = h.digest();
+      }
+    });
     rs += rl;
     rl >>= 1;
   }
@@ -165,24 +233,30 @@ inline void merkle_path_capped(const std::vector<Hash>& tree, size_t n_leaves, s
 }
 
 inline Msg256 round_msg(const std::vector<F256>& f, const std::vector<F256>& b, size_t d) {
-  Msg256 m;
   size_t n = f.size();
   if (d == 1 || n == d) d = 1;
-  for (size_t blk = 0; blk < n / (2 * d); ++blk)
-    for (size_t kk = 0; kk < d; ++kk) {
-      size_t lo = 2 * blk * d + kk, hi = lo + d;
-      m.u0 += f[lo] * b[lo];
-      m.u2 += (f[lo] + f[hi]) * (b[lo] + b[hi]);
+  // pair j: block j / d, offset j % d
+  Two256 s = par_sum<Two256>(n / 2, [&](size_t jb, size_t je, Two256& acc) {
+    for (size_t j = jb; j < je; ++j) {
+      size_t lo = 2 * (j / d) * d + j % d, hi = lo + d;
+      acc.x += f[lo] * b[lo];
+      acc.y += (f[lo] + f[hi]) * (b[lo] + b[hi]);
     }
+  });
+  Msg256 m;
+  m.u0 = s.x;
+  m.u2 = s.y;
   return m;
 }
 inline std::vector<F256> fold_ext(const std::vector<F256>& v, F256 r, size_t d) {
   size_t half = v.size() / 2;
   std::vector<F256> o(half);
-  for (size_t i = 0; i < half; ++i) {
-    size_t blk = i / d, w = i % d, lo = 2 * blk * d + w, hi = lo + d;
-    o[i] = v[lo] + r * (v[hi] + v[lo]);
-  }
+  par_chunks(half, [&](size_t ib, size_t ie) {
+    for (size_t i = ib; i < ie; ++i) {
+      size_t blk = i / d, w = i % d, lo = 2 * blk * d + w, hi = lo + d;
+      o[i] = v[lo] + r * (v[hi] + v[lo]);
+    }
+  });
   return o;
 }
 
@@ -192,18 +266,22 @@ inline std::vector<F256> fold_ext(const std::vector<F256>& v, F256 r, size_t d) 
 inline void lincheck_combs(const Statement& S, const std::vector<F128>& skip_w, const std::vector<F128>& xir,
                            std::vector<F128>& comb_a, std::vector<F128>& comb_b) {
   const uint32_t K = 1u << S.k_log;
-  auto er = build_eq(xir);
+  auto er = par_build_eq(xir);
   std::vector<F128> eqi(K);
-  for (uint32_t i = 0; i < K; ++i) eqi[i] = skip_w[i & 63] * er[i >> 6];
+  par_chunks(K, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) eqi[i] = skip_w[i & 63] * er[i >> 6];
+  });
   if (S.hash == HASH_KECCAK) {
     kr1cs::fold_split(eqi.data(), comb_a, comb_b);
     return;
   }
   comb_a.assign(K, F128()); comb_b.assign(K, F128());
-  for (uint32_t c = 0; c < K; ++c) {
-    for (uint32_t p = S.csc_a->col_ptr[c]; p < S.csc_a->col_ptr[c + 1]; ++p) comb_a[c] += eqi[S.csc_a->rows_flat[p]];
-    for (uint32_t p = S.csc_b->col_ptr[c]; p < S.csc_b->col_ptr[c + 1]; ++p) comb_b[c] += eqi[S.csc_b->rows_flat[p]];
-  }
+  par_chunks(K, [&](size_t cb, size_t ce) {
+    for (size_t c = cb; c < ce; ++c) {
+      for (uint32_t p = S.csc_a->col_ptr[c]; p < S.csc_a->col_ptr[c + 1]; ++p) comb_a[c] += eqi[S.csc_a->rows_flat[p]];
+      for (uint32_t p = S.csc_b->col_ptr[c]; p < S.csc_b->col_ptr[c + 1]; ++p) comb_b[c] += eqi[S.csc_b->rows_flat[p]];
+    }
+  });
 }
 
 class CpuBackend : public ProverBackend {
@@ -229,8 +307,10 @@ class CpuBackend : public ProverBackend {
     const size_t nb = S.n_blocks, rec = input_record_bytes(S.hash);
     z.assign(words(), F128()); a.assign(words(), F128()); b.assign(words(), F128());
     stripe.assign(size_t(1) << (S.m - 3), 0);
+    // groups of 8 instances share stripe bytes: chunks are whole groups
+    par_chunks((nb + 7) / 8, [&](size_t gb, size_t ge) {
     std::vector<uint64_t> bz(K / 64), ba(K / 64), bb(K / 64);
-    for (size_t o = 0; o < nb; ++o) {
+    for (size_t o = 8 * gb; o < std::min(nb, 8 * ge); ++o) {
       std::fill(bz.begin(), bz.end(), 0); std::fill(ba.begin(), ba.end(), 0); std::fill(bb.begin(), bb.end(), 0);
       const uint8_t* in = inputs + o * rec;
       if (S.hash == HASH_BLAKE3) {
@@ -253,13 +333,16 @@ class CpuBackend : public ProverBackend {
       for (uint32_t bit = 0; bit < K; ++bit)
         if ((bz[bit >> 6] >> (bit & 63)) & 1) stripe[g * K + bit] |= (uint8_t)(1u << lane);
     }
+    }, 4);
   }
 
   void commit_l0(uint32_t cap_depth, std::vector<Hash>& cap) override {
     const size_t t = S.lanes, D = size_t(1) << S.log_dim, npos = size_t(1) << S.k_code;
     cw0.assign(npos * t, F128());
-    for (size_t p = 0; p < npos; ++p)
-      for (size_t l = 0; l < t; ++l) cw0[p * t + l] = z[l * D + (p % D)];
+    par_chunks(npos, [&](size_t pb, size_t pe) {
+      for (size_t p = pb; p < pe; ++p)
+        for (size_t l = 0; l < t; ++l) cw0[p * t + l] = z[l * D + (p % D)];
+    });
     Ntt128 ntt(S.k_code);
     ntt.forward_interleaved(cw0.data(), t, 1);
     tree0 = merkle_tree(cw0.data(), npos, t);
@@ -274,23 +357,43 @@ class CpuBackend : public ProverBackend {
     const uint32_t m = S.m;
     const size_t nrows = size_t(1) << (m - 6);
     std::vector<F128> rr(r.begin() + 6, r.end());
-    auto eq = build_eq(rr);
+    auto eq = par_build_eq(rr);
     const SkipExtension& E = skip_extension();
-    std::vector<F128> acc(64 * 256), cs(64);
-    uint8_t ea[64], eb[64];
-    for (size_t x = 0; x < nrows; ++x) {
-      uint64_t abits = row_bits(a, x), bbits = row_bits(b, x), cbits = row_bits(z, x);
-      F128 e = eq[x];
-      if (abits && bbits) {
-        E.extend(abits, ea);
-        E.extend(bbits, eb);
-        for (int i = 0; i < 64; ++i) {
-          uint8_t p = gf8_mul(ea[i], eb[i]);
-          if (p) acc[i * 256 + p] += e;
+    const uint8_t* gm = gf8_mul_table().data();
+    // acc[i * 256 + v] = sum of eq over rows whose extended product at point i is v;
+    // cs[s] = sum of eq over rows with bit s of c set
+    struct Round1Acc {
+      std::vector<F128> acc, cs;
+      Round1Acc operator+(const Round1Acc& o) const {
+        Round1Acc r = *this;
+        if (r.acc.empty()) return o;
+        if (!o.acc.empty()) {
+          for (size_t i = 0; i < r.acc.size(); ++i) r.acc[i] += o.acc[i];
+          for (size_t i = 0; i < r.cs.size(); ++i) r.cs[i] += o.cs[i];
         }
+        return r;
       }
-      while (cbits) { int s = __builtin_ctzll(cbits); cs[s] += e; cbits &= cbits - 1; }
-    }
+    };
+    Round1Acc tot = par_sum<Round1Acc>(nrows, [&](size_t xb, size_t xe, Round1Acc& R) {
+      R.acc.assign(64 * 256, F128());
+      R.cs.assign(64, F128());
+      uint8_t ea[64], eb[64];
+      for (size_t x = xb; x < xe; ++x) {
+        uint64_t abits = row_bits(a, x), bbits = row_bits(b, x), cbits = row_bits(z, x);
+        F128 e = eq[x];
+        if (abits && bbits) {
+          E.extend(abits, ea);
+          E.extend(bbits, eb);
+          for (int i = 0; i < 64; ++i) {
+            uint8_t p = gm[ea[i] * 256 + eb[i]];
+            if (p) R.acc[i * 256 + p] += e;
+          }
+        }
+        while (cbits) { int s = __builtin_ctzll(cbits); R.cs[s] += e; cbits &= cbits - 1; }
+      }
+    });
+    std::vector<F128>& acc = tot.acc;
+    std::vector<F128>& cs = tot.cs;
     ab.assign(64, F128()); c.assign(64, F128());
     for (int i = 0; i < 64; ++i)
       for (int v = 1; v < 256; ++v) if (!acc[i * 256 + v].is_zero()) ab[i] += phi8((uint8_t)v) * acc[i * 256 + v];
@@ -298,41 +401,59 @@ class CpuBackend : public ProverBackend {
       for (int s = 0; s < 64; ++s) if (E.unit[s][i]) c[i] += phi8(E.unit[s][i]) * cs[s];
     // s_hat_v_c[t] = sum_w eq(r[7..m], w) * bit_t(z[w])
     std::vector<F128> r7(r.begin() + 7, r.end());
-    auto eq7 = build_eq(r7);
-    svc.assign(128, F128());
-    for (size_t w = 0; w < words(); ++w) {
-      uint64_t lo = z[w].lo, hi = z[w].hi;
-      while (lo) { int t = __builtin_ctzll(lo); svc[t] += eq7[w]; lo &= lo - 1; }
-      while (hi) { int t = __builtin_ctzll(hi); svc[64 + t] += eq7[w]; hi &= hi - 1; }
-    }
+    auto eq7 = par_build_eq(r7);
+    struct Vec128 {
+      std::vector<F128> v;
+      Vec128 operator+(const Vec128& o) const {
+        Vec128 r = *this;
+        for (size_t i = 0; i < r.v.size(); ++i) r.v[i] += o.v[i];
+        return r;
+      }
+    };
+    svc = par_sum<Vec128>(words(), [&](size_t wb, size_t we, Vec128& R) {
+      R.v.assign(128, F128());
+      for (size_t w = wb; w < we; ++w) {
+        uint64_t lo = z[w].lo, hi = z[w].hi;
+        while (lo) { int t = __builtin_ctzll(lo); R.v[t] += eq7[w]; lo &= lo - 1; }
+        while (hi) { int t = __builtin_ctzll(hi); R.v[64 + t] += eq7[w]; hi &= hi - 1; }
+      }
+    }).v;
   }
 
   static void pair_message(const std::vector<F128>& A, const std::vector<F128>& Bv, const std::vector<F128>& eqp,
                            F128& g1, F128& gi) {
-    auto eq = build_eq(eqp);
-    g1 = F128(); gi = F128();
-    for (size_t x = 0; x < A.size() / 2; ++x) {
-      F128 a0 = A[2 * x], a1 = A[2 * x + 1], b0 = Bv[2 * x], b1 = Bv[2 * x + 1];
-      g1 += eq[x] * (a1 * b1);
-      gi += eq[x] * ((a0 + a1) * (b0 + b1));
-    }
+    auto eq = par_build_eq(eqp);
+    Two128 s = par_sum<Two128>(A.size() / 2, [&](size_t xb, size_t xe, Two128& acc) {
+      for (size_t x = xb; x < xe; ++x) {
+        F128 a0 = A[2 * x], a1 = A[2 * x + 1], b0 = Bv[2 * x], b1 = Bv[2 * x + 1];
+        acc.x += eq[x] * (a1 * b1);
+        acc.y += eq[x] * ((a0 + a1) * (b0 + b1));
+      }
+    });
+    g1 = s.x;
+    gi = s.y;
   }
   void zc_fold_skip(const std::vector<F128>& w, const std::vector<F128>& eq_point, F128& g1, F128& gi) override {
     const size_t nrows = size_t(1) << (S.m - 6);
     amlv.assign(nrows, F128()); bmlv.assign(nrows, F128());
-    for (size_t x = 0; x < nrows; ++x) {
-      uint64_t ab_ = row_bits(a, x), bb_ = row_bits(b, x);
-      F128 sa, sb;
-      while (ab_) { int s = __builtin_ctzll(ab_); sa += w[s]; ab_ &= ab_ - 1; }
-      while (bb_) { int s = __builtin_ctzll(bb_); sb += w[s]; bb_ &= bb_ - 1; }
-      amlv[x] = sa; bmlv[x] = sb;
-    }
+    par_chunks(nrows, [&](size_t xb, size_t xe) {
+      for (size_t x = xb; x < xe; ++x) {
+        uint64_t ab_ = row_bits(a, x), bb_ = row_bits(b, x);
+        F128 sa, sb;
+        while (ab_) { int s = __builtin_ctzll(ab_); sa += w[s]; ab_ &= ab_ - 1; }
+        while (bb_) { int s = __builtin_ctzll(bb_); sb += w[s]; bb_ &= bb_ - 1; }
+        amlv[x] = sa; bmlv[x] = sb;
+      }
+    });
     pair_message(amlv, bmlv, eq_point, g1, gi);
   }
   static void fold_low(std::vector<F128>& v, F128 r) {
     size_t h = v.size() / 2;
-    for (size_t x = 0; x < h; ++x) v[x] = v[2 * x] + r * (v[2 * x + 1] + v[2 * x]);
-    v.resize(h);
+    std::vector<F128> o(h);
+    par_chunks(h, [&](size_t xb, size_t xe) {
+      for (size_t x = xb; x < xe; ++x) o[x] = v[2 * x] + r * (v[2 * x + 1] + v[2 * x]);
+    });
+    v.swap(o);
   }
   void zc_fold(F128 rho, const std::vector<F128>& eq_point, F128& g1, F128& gi) override {
     fold_low(amlv, rho); fold_low(bmlv, rho);
@@ -349,15 +470,16 @@ class CpuBackend : public ProverBackend {
   }
   void lc_zvec(const std::vector<F128>& x_outer) override {
     const uint32_t K = 1u << S.k_log, nu = S.nu;
-    auto eo = build_eq(x_outer);
+    auto eo = par_build_eq(x_outer);
     zv.assign(K, F128());
-    for (uint32_t cc = 0; cc < K / 128; ++cc)
+    parallel_for(K / 128, [&](size_t cc) {
       for (size_t row = 0; row < (size_t(1) << nu); ++row) {
         F128 w = z[(size_t(cc) << nu) + row];
         uint64_t lo = w.lo, hi = w.hi;
         while (lo) { int t = __builtin_ctzll(lo); zv[cc * 128 + t] += eo[row]; lo &= lo - 1; }
         while (hi) { int t = __builtin_ctzll(hi); zv[cc * 128 + 64 + t] += eo[row]; hi &= hi - 1; }
       }
+    });
     zv_cap = zv;
   }
   static void top_message(const std::vector<F128>& c, const std::vector<F128>& v, F128& e1, F128& ei) {
@@ -394,10 +516,11 @@ class CpuBackend : public ProverBackend {
     }
   }
   void lc_s_hat_v(const std::vector<F128>& tail, std::vector<F128>& out) override {
-    auto et = build_eq(tail);
+    auto et = par_build_eq(tail);
     out.assign(128, F128());
-    for (size_t k = 0; k < et.size(); ++k)
-      for (int bb = 0; bb < 128; ++bb) out[bb] += et[k] * zv_cap[bb + 128 * k];
+    parallel_for(128, [&](size_t bb) {
+      for (size_t k = 0; k < et.size(); ++k) out[bb] += et[k] * zv_cap[bb + 128 * k];
+    });
   }
 
   // ---- merged open
@@ -405,56 +528,68 @@ class CpuBackend : public ProverBackend {
     const size_t n = words();
     mw.assign(n, F128());
     std::vector<std::vector<F128>> er(cl.size()), ec(cl.size());
-    for (size_t i = 0; i < cl.size(); ++i) { er[i] = build_eq(cl[i].z_row); ec[i] = build_eq(cl[i].z_col); }
-    for (uint64_t d = 0; d < area; ++d) {
-      size_t row = d & ((size_t(1) << nu) - 1), col = d >> nu;
-      F128 acc;
-      for (size_t i = 0; i < cl.size(); ++i) acc += fold_one_slot(er[i][row] * ec[i][col], cl[i].table.data());
-      mw[d] = acc;
-    }
+    for (size_t i = 0; i < cl.size(); ++i) { er[i] = par_build_eq(cl[i].z_row); ec[i] = par_build_eq(cl[i].z_col); }
+    par_chunks(area, [&](size_t db, size_t de) {
+      for (uint64_t d = db; d < de; ++d) {
+        size_t row = d & ((size_t(1) << nu) - 1), col = d >> nu;
+        F128 acc;
+        for (size_t i = 0; i < cl.size(); ++i) acc += fold_one_slot(er[i][row] * ec[i][col], cl[i].table.data());
+        mw[d] = acc;
+      }
+    });
     mq = z;
-    u0 = F128(); u2 = F128();
-    for (size_t i = 0; i < n / 2; ++i) {
-      u0 += mq[2 * i] * mw[2 * i];
-      u2 += (mq[2 * i] + mq[2 * i + 1]) * (mw[2 * i] + mw[2 * i + 1]);
-    }
+    Two128 s = par_sum<Two128>(n / 2, [&](size_t ib, size_t ie, Two128& acc) {
+      for (size_t i = ib; i < ie; ++i) {
+        acc.x += mq[2 * i] * mw[2 * i];
+        acc.y += (mq[2 * i] + mq[2 * i + 1]) * (mw[2 * i] + mw[2 * i + 1]);
+      }
+    });
+    u0 = s.x;
+    u2 = s.y;
   }
   void mo_round(F128 r, bool last, F128& g1, F128& gi) override {
     fold_low(mq, r); fold_low(mw, r);
     if (!last) {
-      g1 = F128(); gi = F128();
-      for (size_t i = 0; i < mq.size() / 2; ++i) {
-        g1 += mq[2 * i + 1] * mw[2 * i + 1];
-        gi += (mq[2 * i] + mq[2 * i + 1]) * (mw[2 * i] + mw[2 * i + 1]);
-      }
+      Two128 s = par_sum<Two128>(mq.size() / 2, [&](size_t ib, size_t ie, Two128& acc) {
+        for (size_t i = ib; i < ie; ++i) {
+          acc.x += mq[2 * i + 1] * mw[2 * i + 1];
+          acc.y += (mq[2 * i] + mq[2 * i + 1]) * (mw[2 * i] + mw[2 * i + 1]);
+        }
+      });
+      g1 = s.x;
+      gi = s.y;
     }
   }
   F128 mo_q_eval() override { return mq[0]; }
 
   // ---- Ligerito
   void lg_basis_eq(F128 gamma, const std::vector<F128>& rho) override {
-    auto e = build_eq(rho, gamma);
+    auto e = par_build_eq(rho, gamma);
     lb.resize(e.size());
-    for (size_t i = 0; i < e.size(); ++i) lb[i] = F256(e[i]);
+    par_chunks(e.size(), [&](size_t b, size_t en) { for (size_t i = b; i < en; ++i) lb[i] = F256(e[i]); });
     lf.resize(z.size());
-    for (size_t i = 0; i < z.size(); ++i) lf[i] = F256(z[i]);
+    par_chunks(z.size(), [&](size_t b, size_t en) { for (size_t i = b; i < en; ++i) lf[i] = F256(z[i]); });
   }
   F128 lg_eval_eq(const std::vector<F128>& zp) override {
-    auto e = build_eq(zp);
-    F128 acc;
-    for (size_t i = 0; i < lf.size(); ++i) acc += lf[i].c0 * e[i];
-    return acc;
+    auto e = par_build_eq(zp);
+    return par_sum<F128>(lf.size(), [&](size_t b, size_t en, F128& acc) {
+      for (size_t i = b; i < en; ++i) acc += lf[i].c0 * e[i];
+    });
   }
   void lg_add_eq(F128 beta, const std::vector<F128>& zp) override {
-    auto e = build_eq(zp, beta);
-    for (size_t i = 0; i < lb.size(); ++i) lb[i] += F256(e[i]);
+    auto e = par_build_eq(zp, beta);
+    par_chunks(lb.size(), [&](size_t b, size_t en) { for (size_t i = b; i < en; ++i) lb[i] += F256(e[i]); });
   }
   Msg256 lg_message(size_t d) override { return round_msg(lf, lb, d); }
   void lg_fold(F256 r, size_t d) override { lf = fold_ext(lf, r, d); lb = fold_ext(lb, r, d); }
   void lg_code_switch() override {
     std::vector<F256> nf(2 * lf.size()), nb(2 * lb.size());
-    for (size_t i = 0; i < lf.size(); ++i) { nf[2 * i] = F256(lf[i].c0); nf[2 * i + 1] = F256(lf[i].c1); }
-    for (size_t i = 0; i < lb.size(); ++i) { nb[2 * i] = lb[i]; nb[2 * i + 1] = F256::u() * lb[i]; }
+    par_chunks(lf.size(), [&](size_t b, size_t e) {
+      for (size_t i = b; i < e; ++i) { nf[2 * i] = F256(lf[i].c0); nf[2 * i + 1] = F256(lf[i].c1); }
+    });
+    par_chunks(lb.size(), [&](size_t b, size_t e) {
+      for (size_t i = b; i < e; ++i) { nb[2 * i] = lb[i]; nb[2 * i + 1] = F256::u() * lb[i]; }
+    });
     lf.swap(nf); lb.swap(nb);
   }
   void lg_commit(uint32_t level, uint32_t log_cols, uint32_t log_lanes, uint32_t log_rate, uint32_t cap_depth,
@@ -464,7 +599,7 @@ class CpuBackend : public ProverBackend {
     L.block_len = size_t(1) << (log_cols + log_rate);
     size_t msg = lf.size();
     L.mat.resize(L.block_len * L.lanes);
-    for (size_t i = 0; i < L.mat.size(); ++i) L.mat[i] = lf[i % msg].c0;
+    par_chunks(L.mat.size(), [&](size_t b, size_t e) { for (size_t i = b; i < e; ++i) L.mat[i] = lf[i % msg].c0; });
     Ntt128 ntt(log_cols + log_rate);
     ntt.forward_interleaved(L.mat.data(), L.lanes, log_rate);
     L.tree = merkle_tree(L.mat.data(), L.block_len, L.lanes);
@@ -473,30 +608,39 @@ class CpuBackend : public ProverBackend {
     levels[level] = std::move(L);
   }
   Msg256 lg_introduce_eq(const std::vector<F128>& zp, F128& answer) override {
-    auto e = build_eq(zp);
-    answer = F128();
+    auto e = par_build_eq(zp);
     pending.resize(e.size());
-    for (size_t i = 0; i < e.size(); ++i) { answer += lf[i].c0 * e[i]; pending[i] = F256(e[i]); }
+    answer = par_sum<F128>(e.size(), [&](size_t b, size_t en, F128& acc) {
+      for (size_t i = b; i < en; ++i) { acc += lf[i].c0 * e[i]; pending[i] = F256(e[i]); }
+    });
     return round_msg(lf, pending, 1);
   }
   Msg256 lg_introduce_induced(uint32_t ln, uint32_t, const std::vector<uint64_t>&, const std::vector<F128>& w,
                               const std::vector<std::vector<F128>>& what) override {
     size_t n = size_t(1) << ln;
-    std::vector<F128> basis(n), tmp(n);
-    for (size_t q = 0; q < w.size(); ++q) {
-      tmp[0] = w[q];
-      for (uint32_t k = 0; k < ln; ++k) {
-        size_t cur = size_t(1) << k;
-        for (size_t i = 0; i < cur; ++i) tmp[i + cur] = what[q][k] * tmp[i];
+    // queries split into a few groups, each summing its own basis vector
+    const size_t groups = std::min<size_t>(w.size(), ThreadPool::instance().workers() + 1);
+    std::vector<std::vector<F128>> part(groups, std::vector<F128>(n));
+    parallel_for(groups, [&](size_t g) {
+      std::vector<F128> tmp(n);
+      for (size_t q = w.size() * g / groups; q < w.size() * (g + 1) / groups; ++q) {
+        tmp[0] = w[q];
+        for (uint32_t k = 0; k < ln; ++k) {
+          size_t cur = size_t(1) << k;
+          for (size_t i = 0; i < cur; ++i) tmp[i + cur] = what[q][k] * tmp[i];
+        }
+        for (size_t i = 0; i < n; ++i) part[g][i] += tmp[i];
       }
-      for (size_t i = 0; i < n; ++i) basis[i] += tmp[i];
-    }
+    });
+    std::vector<F128> basis(n);
+    for (auto& pv : part)
+      for (size_t i = 0; i < n; ++i) basis[i] += pv[i];
     pending.resize(2 * n);
     for (size_t i = 0; i < n; ++i) { pending[2 * i] = F256(basis[i]); pending[2 * i + 1] = F256::u() * F256(basis[i]); }
     return round_msg(lf, pending, 1);
   }
   void lg_glue(F128 beta) override {
-    for (size_t i = 0; i < lb.size(); ++i) lb[i] += pending[i] * beta;
+    par_chunks(lb.size(), [&](size_t b, size_t e) { for (size_t i = b; i < e; ++i) lb[i] += pending[i] * beta; });
   }
   void lg_open(uint32_t level, const std::vector<uint64_t>& pos, uint32_t cap_depth,
                std::vector<std::vector<F128>>& rows, std::vector<Hash>& paths) override {
