@@ -10,12 +10,19 @@
 //         (crates/flock-core/src/field/phi8.rs:19-30, entry 2) is PHI8_OF_X below and
 //         every other entry is generated here as a sum of its powers.
 //
-// Portable C++ (no intrinsics): the same code builds on x86_64 and aarch64 hosts.
+// Portable C++: the same code builds on x86_64 and aarch64 hosts and gives the same bits.
+// On aarch64 hosts built with the AES extension (the build passes -march=armv8-a+crypto
+// there) the 64x64 carry-less product is the PMULL instruction through the ACLE
+// intrinsic vmull_p64; everywhere else it is the integer-multiply form below.
 #pragma once
 #include <cstdint>
 #include <cstring>
 #include <vector>
 #include <array>
+#if defined(__aarch64__) && defined(__ARM_FEATURE_AES)
+#include <arm_neon.h>
+#define FLOCK_HOST_PMULL 1
+#endif
 
 namespace flock {
 
@@ -48,12 +55,18 @@ inline uint64_t clmul32(uint32_t x, uint32_t y) {
   return (z0 & 0x1111111111111111ull) | (z1 & 0x2222222222222222ull) | (z2 & 0x4444444444444444ull) |
          (z3 & 0x8888888888888888ull);
 }
-// 64x64 -> 128 carry-less product (Karatsuba over 32-bit halves).
+// 64x64 -> 128 carry-less product (Karatsuba over 32-bit halves, or PMULL).
 inline void clmul64(uint64_t a, uint64_t b, uint64_t& rlo, uint64_t& rhi) {
+#ifdef FLOCK_HOST_PMULL
+  const uint64x2_t v = vreinterpretq_u64_p128(vmull_p64((poly64_t)a, (poly64_t)b));
+  rlo = vgetq_lane_u64(v, 0);
+  rhi = vgetq_lane_u64(v, 1);
+#else
   const uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32), b0 = (uint32_t)b, b1 = (uint32_t)(b >> 32);
   const uint64_t l = clmul32(a0, b0), h = clmul32(a1, b1), m = clmul32(a0 ^ a1, b0 ^ b1) ^ l ^ h;
   rlo = l ^ (m << 32);
   rhi = h ^ (m >> 32);
+#endif
 }
 
 // Reduce a 256-bit product (r0 lowest) modulo x^128 + x^7 + x^2 + x + 1.

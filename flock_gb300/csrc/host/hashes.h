@@ -8,12 +8,19 @@
 //  * BLAKE3: the compression function (crates/flock-core/src/hash.rs:74-140) and the
 //    standard chunked tree hasher with 32-byte output, which the registry digest
 //    (crates/flock-core/src/schedule.rs:542-578) runs over the R1CS matrices.
+//
+// On aarch64 hosts built with the SHA-2 extension (-march=armv8-a+crypto) the SHA-256
+// block function uses the ACLE SHA-256 intrinsics; elsewhere it is the plain C++ form.
 #pragma once
 #include <cstdint>
 #include <cstring>
 #include <vector>
 #include <array>
 #include <string>
+#if defined(__aarch64__) && defined(__ARM_FEATURE_SHA2)
+#include <arm_neon.h>
+#define FLOCK_HOST_SHA2 1
+#endif
 
 namespace flock {
 
@@ -42,6 +49,23 @@ struct Sha256 {
 
   // One compression over a 64-byte block (big-endian words).
   static void compress(uint32_t st[8], const uint8_t* p) {
+#ifdef FLOCK_HOST_SHA2
+    // four rounds per step: SHA256H / SHA256H2 on (abcd, efgh), the schedule by SHA256SU0/SU1
+    uint32x4_t abcd = vld1q_u32(st), efgh = vld1q_u32(st + 4);
+    const uint32x4_t abcd0 = abcd, efgh0 = efgh;
+    uint32x4_t m[4];
+    for (int i = 0; i < 4; ++i) m[i] = vreinterpretq_u32_u8(vrev32q_u8(vld1q_u8(p + 16 * i)));
+    for (int i = 0; i < 16; ++i) {
+      const uint32x4_t wk = vaddq_u32(m[0], vld1q_u32(K + 4 * i));
+      const uint32x4_t prev = abcd;
+      abcd = vsha256hq_u32(abcd, efgh, wk);
+      efgh = vsha256h2q_u32(efgh, prev, wk);
+      const uint32x4_t next = vsha256su1q_u32(vsha256su0q_u32(m[0], m[1]), m[2], m[3]);
+      m[0] = m[1]; m[1] = m[2]; m[2] = m[3]; m[3] = next;
+    }
+    vst1q_u32(st, vaddq_u32(abcd, abcd0));
+    vst1q_u32(st + 4, vaddq_u32(efgh, efgh0));
+#else
     uint32_t w[64];
     for (int i = 0; i < 16; ++i)
       w[i] = (uint32_t)p[4 * i] << 24 | (uint32_t)p[4 * i + 1] << 16 | (uint32_t)p[4 * i + 2] << 8 | p[4 * i + 3];
@@ -61,6 +85,7 @@ struct Sha256 {
       hh = g; g = f; f = e; e = d + t1; d = c; c = b; b = a; a = t1 + t2;
     }
     st[0] += a; st[1] += b; st[2] += c; st[3] += d; st[4] += e; st[5] += f; st[6] += g; st[7] += hh;
+#endif
   }
 
   void update(const void* data, size_t n) {
