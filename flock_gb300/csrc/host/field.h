@@ -12,14 +12,16 @@
 //
 // Portable C++: the same code builds on x86_64 and aarch64 hosts and gives the same bits.
 // On aarch64 hosts built with the AES extension (the build passes -march=armv8-a+crypto
-// there) the 64x64 carry-less product is the PMULL instruction through the ACLE
-// intrinsic vmull_p64; everywhere else it is the integer-multiply form below.
+// there) host-compiler translation units take the 64x64 carry-less product from the PMULL
+// instruction through the ACLE intrinsic vmull_p64; everywhere else (and in nvcc
+// translation units, whose front end does not parse arm_neon.h) it is the
+// integer-multiply form below.
 #pragma once
 #include <cstdint>
 #include <cstring>
 #include <vector>
 #include <array>
-#if defined(__aarch64__) && defined(__ARM_FEATURE_AES)
+#if defined(__aarch64__) && defined(__ARM_FEATURE_AES) && !defined(__CUDACC__)
 #include <arm_neon.h>
 #define FLOCK_HOST_PMULL 1
 #endif

@@ -9,15 +9,16 @@
 //    standard chunked tree hasher with 32-byte output, which the registry digest
 //    (crates/flock-core/src/schedule.rs:542-578) runs over the R1CS matrices.
 //
-// On aarch64 hosts built with the SHA-2 extension (-march=armv8-a+crypto) the SHA-256
-// block function uses the ACLE SHA-256 intrinsics; elsewhere it is the plain C++ form.
+// On aarch64 hosts built with the SHA-2 extension (-march=armv8-a+crypto), host-compiler
+// translation units run the SHA-256 block function on the ACLE SHA-256 intrinsics;
+// elsewhere (and under nvcc) it is the plain C++ form.
 #pragma once
 #include <cstdint>
 #include <cstring>
 #include <vector>
 #include <array>
 #include <string>
-#if defined(__aarch64__) && defined(__ARM_FEATURE_SHA2)
+#if defined(__aarch64__) && defined(__ARM_FEATURE_SHA2) && !defined(__CUDACC__)
 #include <arm_neon.h>
 #define FLOCK_HOST_SHA2 1
 #endif
