@@ -198,7 +198,7 @@ def dist_init():
         import torch
         import torch.distributed as dist
 
-        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        backend = os.environ.get("FLOCK_GB300_DIST_BACKEND") or ("nccl" if torch.cuda.is_available() else "gloo")
         if backend == "nccl":
             torch.cuda.set_device(local)
         dist.init_process_group(backend=backend)
@@ -229,7 +229,7 @@ def run_reference(args, world, rank):
         return 0
     wl = args.workload
     W, K = args.warmup, args.steps
-    n = CPU_SAMPLE[wl]
+    n = args.batch or CPU_SAMPLE[wl]
     import oracle
     from flock_gb300 import inputs
 

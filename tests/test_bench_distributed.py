@@ -19,7 +19,7 @@ def _free_port() -> int:
 
 def _worker(rank, world, port, q):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), WORLD_SIZE=str(world), RANK=str(rank),
-                      LOCAL_RANK=str(rank))
+                      LOCAL_RANK=str(rank), FLOCK_GB300_DIST_BACKEND="gloo")
     sys.path.insert(0, ROOT)
     import bench
 
@@ -48,8 +48,9 @@ def test_reference_arm_under_torchrun_prints_once():
     pytest.importorskip("torch")
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes", "1", "--nproc-per-node", "2", "--master-addr",
            "127.0.0.1", "--master-port", str(_free_port()), "bench.py", "--impl", "reference", "--gpus", "2", "--steps",
-           "1", "--warmup", "1", "--workload", "keccak"]
-    out = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
+           "1", "--warmup", "1", "--workload", "keccak", "--batch", "64"]
+    env = dict(os.environ, FLOCK_GB300_DIST_BACKEND="gloo")
+    out = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600, env=env)
     assert out.returncode == 0, out.stderr[-2000:]
     lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
     assert len(lines) == 1
