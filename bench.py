@@ -44,8 +44,10 @@ WORKLOADS = {
 HEADLINE = "keccak"
 # CPU sample per workload: the largest batch of the same hash whose oracle prove (all host
 # threads) stays within a few seconds, so that warm-up + best of 3 and the reference arm's
-# W + K steps end within minutes. BLAKE3 2^12 is the configured batch itself.
-CPU_SAMPLE = {"blake3": 1 << 12, "sha256": 1 << 14, "keccak": 1 << 15}
+# W + K steps end within minutes: the configured batch for BLAKE3 2^12 and SHA-256 2^16
+# (about 0.1 s and 2 s per prove on 16 Grace cores), half of it for Keccak-f 2^18 (about
+# 6.5 s per prove at 2^17).
+CPU_SAMPLE = {"blake3": 1 << 12, "sha256": 1 << 16, "keccak": 1 << 17}
 # The reference's own published CPU rates for the configured batches (k hashes/s;
 # README.md:50-64, AMD Threadripper 7970X, best of 3 after a verified warm-up).
 PUBLISHED_CPU = {

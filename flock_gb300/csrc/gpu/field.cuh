@@ -10,6 +10,13 @@
 // stay below 16 are summed as integers, clmul32_classes). The four classes are masked
 // and merged. Two Karatsuba levels build the 128 x 128 product from nine such products,
 // followed by the shift-and-fold reduction.
+//
+// The thinned-operand ("holes") carry-less multiply is a published constant-time
+// technique: Thomas Pornin's BearSSL uses it for GHASH on CPUs without a carry-less
+// multiply instruction (ghash_ctmul32.c / ghash_ctmul64.c, with a write-up in BearSSL's
+// "Constant-Time Mul" notes). The form here — 32x32 -> 64 products from mul.wide/mad.wide,
+// same-class pairs summed in the multiply's addend, two Karatsuba levels — is this
+// library's own arrangement of it for the GPU's integer multiply pipe.
 #pragma once
 #include <cstdint>
 

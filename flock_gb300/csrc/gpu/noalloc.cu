@@ -6,7 +6,10 @@
 // static module storage. No cudaMalloc / cudaFree or allocating library routine is called.
 // First call on a device: the symbol addresses are looked up (cudaGetSymbolAddress) and
 // the twiddle tables and witness constants are copied in (synchronous copies); this set-up
-// should happen before any stream capture that includes the entry point.
+// should happen before any stream capture. Every call is synchronous: it returns after its
+// work on the caller's stream has finished and the cap is in host memory.
+// Limit: codewords of at most 2^13 rows (committed stacks of m <= 25): up to 2^11 BLAKE3,
+// 2^10 SHA-256 or 2^9 Keccak-f instances; the scratch they need stays below the 32 MiB.
 #include "kernels.h"
 #include "../host/setup.h"
 #include "../host/tables.h"
@@ -74,19 +77,21 @@ extern "C" int flock_gb300_commit_cap_noalloc(int hash_kind, const void* d_input
   while ((uint64_t(1) << nu) < n_blocks) ++nu;
   UnionGeometry geo = union_geometry(k_log, useful, nu);
   if (!geo.identity) return fail(FLOCK_GB300_EINVAL, "batch too small for a full-utilisation statement");
-  int n_cfg = 0;
-  const LigeritoFastConfig* cfg = ligerito_fast_configs(&n_cfg);
-  const LigeritoFastConfig* c = nullptr;
-  for (int i = 0; i < n_cfg; ++i)
-    if (cfg[i].m == geo.dense_m) c = &cfg[i];
-  if (!c) return fail(FLOCK_GB300_EINVAL, "no Ligerito configuration for this size");
-  const uint32_t log_batch = c->initial_k, lanes = geo.commit_lanes(log_batch);
+  // the Ligerito parameters, log_dim and cap depth exactly as make_statement derives them
+  // for flock_gb300_prove_fast (the cap depth is the top stratum of level 0's schedule)
+  LigeritoParams lig;
+  try {
+    lig = ligerito_params_for(geo.dense_m);
+  } catch (const std::exception&) {
+    return fail(FLOCK_GB300_EINVAL, "no Ligerito configuration for this size");
+  }
+  const uint32_t log_batch = lig.initial_k, lanes = geo.commit_lanes(log_batch);
   const uint32_t log_dim = geo.dense_m - 7 - log_batch, k_code = log_dim + 1;
-  uint32_t cap_depth = 0;  // first stratum of the level-0 query schedule
-  while ((2u << cap_depth) <= c->levels[0].queries) ++cap_depth;
-  if (cap_depth > k_code) cap_depth = k_code;
+  if (lig.log_n != geo.dense_m - 7 || lig.initial_log_msg_cols != log_dim || lig.log_inv_rates[0] != 1)
+    return fail(FLOCK_GB300_EINVAL, "Ligerito configuration does not match the committed geometry");
+  const uint32_t cap_depth = lig.sched[0].cap_depth();
   const uint64_t W = uint64_t(1) << (geo.m - 7), n_pos = uint64_t(1) << k_code;
-  const size_t need = 2 * W * 16 + n_pos * lanes * 16 + 2 * n_pos * 32;
+  const size_t need = 3 * W * 16 + n_pos * lanes * 16 + 2 * n_pos * 32;
   if (k_code > NOALLOC_MAX_LOG_CODE || need > NOALLOC_SCRATCH_BYTES) {
     static thread_local char msg[200];
     snprintf(msg, sizeof(msg), "batch needs %zu bytes of scratch; the static scratch holds %zu bytes (at most 2^%u codeword rows)",
@@ -104,13 +109,14 @@ extern "C" int flock_gb300_commit_cap_noalloc(int hash_kind, const void* d_input
     if (!st.ready) setup_device(st);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     F128d* z = reinterpret_cast<F128d*>(st.scratch);
-    F128d* dummy = z + W;  // a and b of the witness kernel: written, never read
-    F128d* cw = dummy + W;
+    F128d* a = z + W;  // a = A z and b = B z of the witness kernel: written, not used here
+    F128d* b = a + W;
+    F128d* cw = b + W;
     uint8_t* tree = reinterpret_cast<uint8_t*>(cw + n_pos * lanes);
     const uint64_t used_words = geo.used_cols << nu;
     // chunk columns past the witness must read as zero
     CUDA_OK(cudaMemsetAsync(z + used_words, 0, (W - used_words) * 16, s));
-    launch_witness(hash_kind, d_inputs, (uint32_t)n_blocks, nu, z, dummy, dummy, (uint32_t)geo.used_cols, s);
+    launch_witness(hash_kind, d_inputs, (uint32_t)n_blocks, nu, z, a, b, (uint32_t)geo.used_cols, s);
     launch_fill_lane_major(z, cw, lanes, log_dim, k_code, s);
     launch_ntt(cw, lanes, k_code, 1, st.twiddles + (size_t(1) << k_code), s);
     launch_merkle(cw, lanes, n_pos, tree, s);

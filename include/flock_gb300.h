@@ -109,12 +109,13 @@ int flock_gb300_last_phase_ms(const flock_gb300_setup* setup, double out[8]);
  * memory budget (an HBM-budgeted serving process), or on a stream whose work must not be
  * interleaved with allocator calls. Runs witness generation, the lane-major codeword fill,
  * the additive NTT and the Merkle tree of the batch's committed stack in a fixed static
- * device array (32 MiB, codewords of at most 2^13 rows: e.g. up to 2^11 BLAKE3 or SHA-256
- * compressions); larger batches are rejected with FLOCK_GB300_EINVAL and a message naming
- * the bytes needed. d_inputs: n_blocks packed input records in device memory. On success
+ * device array (32 MiB, codewords of at most 2^13 rows: up to 2^11 BLAKE3, 2^10 SHA-256 or
+ * 2^9 Keccak-f instances); larger batches are rejected with FLOCK_GB300_EINVAL and a message
+ * naming the bytes needed. d_inputs: n_blocks packed input records in device memory. On success
  * cap_out receives the 2^c x 32-byte Merkle cap, identical to the cap in the bundle of
- * flock_gb300_prove_fast for the same inputs, and *cap_len its length; the call returns
- * after the work on `stream` (a cudaStream_t, 0 = legacy default) completes.
+ * flock_gb300_prove_fast for the same inputs, and *cap_len its length. The call is
+ * synchronous: it returns after its work on `stream` (a cudaStream_t, 0 = legacy default)
+ * has completed and the cap has been copied to cap_out.
  * The first call on a device looks up the static arrays and copies the twiddle tables in
  * (synchronous copies): make it before any stream capture. The chunk columns past the
  * witness are cleared on every call (nothing needs to start zeroed). All calls on a device
