@@ -599,14 +599,17 @@ void GpuBackend::lc_comb(const std::vector<F128>& skip_w, const std::vector<F128
   Mark mk(this, ST_LINCHECK);
   launch_lc_eq_inner(dw, der, K_, eqi_, st_);
   if (S.hash == HASH_KECCAK) {
-    // walker fold (additions only) on the host over the downloaded eq vector
-    auto eqi = fetch(eqi_, K_);
-    std::vector<F128> ha, hb;
-    kr1cs::fold_split(eqi.data(), ha, hb);
-    CUDA_OK(cudaMemcpyAsync(ca_, ha.data(), K_ * 16, cudaMemcpyHostToDevice, st_));
-    CUDA_OK(cudaMemcpyAsync(cb_, hb.data(), K_ * 16, cudaMemcpyHostToDevice, st_));
-    h2d_ += 2 * K_ * 16;
-    sync();
+    // the walker's column folds on the device (no materialised matrices)
+    static const KeccakColumnConsts kc = [] {
+      KeccakColumnConsts c{};
+      for (int r = 0; r < 24; ++r) c.rc[r] = kr1cs::RC[r];
+      for (int a = 0; a < 5; ++a)
+        for (int b = 0; b < 5; ++b) c.rho[a + 5 * b] = (uint8_t)(kr1cs::RHO[a][b] % 64);
+      return c;
+    }();
+    CUDA_OK(cudaMemsetAsync(ca_, 0, K_ * 16, st_));
+    CUDA_OK(cudaMemsetAsync(cb_, 0, K_ * 16, st_));
+    launch_keccak_lincheck_columns(eqi_, ca_, cb_, kc, st_);
     return;
   }
   launch_csc_fold(cola_, rowa_, K_, eqi_, ca_, st_);

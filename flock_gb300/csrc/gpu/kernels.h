@@ -88,6 +88,15 @@ uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, 
 void launch_lc_eq_inner(const F128d* w64, const F128d* er, uint32_t K, F128d* eqi, cudaStream_t s);
 void launch_csc_fold(const uint32_t* col_ptr, const uint32_t* rows, uint32_t K, const F128d* eqi, F128d* out,
                      cudaStream_t s);
+// Keccak-f block R1CS: writes the nonzero entries of ca = eq^T A_0 and cb = eq^T B_0 (the
+// caller zeroes both K-word vectors first). rc = the 24 round constants, rho[a + 5 b] = the
+// rotation offset of lane (a, b) mod 64.
+struct KeccakColumnConsts {
+  uint64_t rc[24];
+  uint8_t rho[25];
+};
+void launch_keccak_lincheck_columns(const F128d* eqi, F128d* ca, F128d* cb, const KeccakColumnConsts& kc,
+                                    cudaStream_t s);
 void launch_lc_zvec(const F128d* z, uint32_t nu, uint32_t used_chunks, const F128d* eq, F128d* part, F128d* zv,
                     cudaStream_t s);
 uint32_t launch_lc_start(const F128d* ca, const F128d* cb, F128d alpha, F128d beta, uint32_t pin, uint32_t K,

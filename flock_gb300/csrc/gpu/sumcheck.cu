@@ -594,6 +594,92 @@ void launch_csc_fold(const uint32_t* col_ptr, const uint32_t* rows, uint32_t K, 
   LAUNCH_OK();
 }
 
+// ---- Keccak-f lincheck columns: ca = eq^T A_0 and cb = eq^T B_0 of the Keccak-f block
+// R1CS (the walker of KeccakLincheckCircuit::fold_alpha_batched, crates/flock-prover/src/
+// r1cs_hashes/keccak.rs:692-829), as the adjoint of the constraint map. With st_r the
+// state before round r and phi = pi o rho o theta, the rows are
+//   A[Z] = B[Z] = z_Z;  A[s0] = st_0;  B[s0] = z_Z;  A[s24] = st_24;  B[s24] = z_Z;
+//   A[t_r(x,y,z)] = phi(st_r)[x+1,y,z] + z_Z;  B[t_r(x,y,z)] = phi(st_r)[x+2,y,z];
+//   st_{r+1} = phi(st_r) + t_r + RC_r z_Z,
+// so with lambda_24 = eq[s24] (A) or 0 (B) and, for r = 23..0,
+//   column t_r = lambda_{r+1};  lambda_r = phi^T(lambda_{r+1} + eq[t_r] shifted by 1 (A) / 2 (B) in x),
+// column s0 = eq[s0] (A only) + lambda_0, and column Z collects eq[Z], the "+ z_Z" rows
+// (A: all t rows; B: s0 and s24 rows) and <lambda_{r+1}, RC_r> for every round.
+// phi^T = theta^T o (pi o rho)^T:
+//   (pi o rho)^T: out[a,b,c] = in[b, 2(a-b) mod 5, c + rho(a,b)]
+//   theta^T: out[x,y,z] = in[x,y,z] + sum_y' in[x+1,y',z] + sum_y' in[x-1,y',z+1].
+// One block per side; the 1600-word vectors live in shared memory.
+constexpr uint32_t KW_THREADS = 512;
+constexpr uint32_t KW_STATE = 1600;
+constexpr uint32_t KW_S24_WORD = 2048 / 64, KW_T_WORD = 4160 / 64, KW_Z = 4096;
+__device__ __forceinline__ uint32_t kw_pos(uint32_t base_word, uint32_t s) { return (base_word + s % 25) * 64 + s / 25; }
+
+__global__ void __launch_bounds__(KW_THREADS)
+keccak_lincheck_columns_kernel(const F128d* __restrict__ eqi, F128d* __restrict__ ca, F128d* __restrict__ cb,
+                               KeccakColumnConsts kc) {
+  extern __shared__ F128d kw_sh[];
+  F128d* lam = kw_sh;                // lambda, then mu in place
+  F128d* P = lam + KW_STATE;         // (pi o rho)^T mu
+  F128d* C = P + KW_STATE;           // column sums of P: C[x + 5 z]
+  __shared__ F128d red[KW_THREADS / 32];
+  const bool bside = blockIdx.x == 1;
+  F128d* out = bside ? cb : ca;
+  const uint32_t shift = bside ? 2 : 1, tid = threadIdx.x;
+  F128d zacc = f128_zero();  // this thread's share of column Z beyond eq[Z]
+  for (uint32_t s = tid; s < KW_STATE; s += KW_THREADS) {
+    const F128d e = eqi[kw_pos(KW_S24_WORD, s)];
+    if (bside) { lam[s] = f128_zero(); zacc += e; }
+    else lam[s] = e;
+  }
+  __syncthreads();
+  for (int r = 23; r >= 0; --r) {
+    const uint32_t tb = KW_T_WORD + 25u * r;
+    for (uint32_t s = tid; s < KW_STATE; s += KW_THREADS) {
+      const F128d l = lam[s];
+      out[kw_pos(tb, s)] = l;
+      if (s % 25 == 0 && ((kc.rc[r] >> (s / 25)) & 1)) zacc += l;
+      const uint32_t x = s % 5;
+      const F128d e = eqi[kw_pos(tb, s - x + (x + 5 - shift) % 5)];
+      if (!bside) zacc += e;
+      lam[s] = l + e;
+    }
+    __syncthreads();
+    for (uint32_t o = tid; o < KW_STATE; o += KW_THREADS) {
+      const uint32_t a = o % 5, b = (o / 5) % 5, c = o / 25;
+      const uint32_t y = (2 * (a + 5 - b)) % 5;
+      P[o] = lam[b + 5 * y + 25 * ((c + kc.rho[a + 5 * b]) & 63)];
+    }
+    __syncthreads();
+    for (uint32_t q = tid; q < 320; q += KW_THREADS) {
+      const uint32_t x = q % 5, z = q / 5;
+      F128d acc = f128_zero();
+      for (uint32_t y = 0; y < 5; ++y) acc += P[x + 5 * y + 25 * z];
+      C[q] = acc;
+    }
+    __syncthreads();
+    for (uint32_t s = tid; s < KW_STATE; s += KW_THREADS) {
+      const uint32_t x = s % 5, z = s / 25;
+      lam[s] = P[s] + C[(x + 1) % 5 + 5 * z] + C[(x + 4) % 5 + 5 * ((z + 1) & 63)];
+    }
+    __syncthreads();
+  }
+  for (uint32_t s = tid; s < KW_STATE; s += KW_THREADS) {
+    const uint32_t p = kw_pos(0, s);
+    const F128d e = eqi[p];
+    if (bside) { out[p] = lam[s]; zacc += e; }
+    else out[p] = lam[s] + e;
+  }
+  const F128d tot = block_xor(zacc, red);
+  if (tid == 0) out[KW_Z] = eqi[KW_Z] + tot;
+}
+void launch_keccak_lincheck_columns(const F128d* eqi, F128d* ca, F128d* cb, const KeccakColumnConsts& kc,
+                                    cudaStream_t s) {
+  const int smem = (int)((2 * KW_STATE + 320) * sizeof(F128d));
+  set_dynamic_smem((const void*)keccak_lincheck_columns_kernel, smem);
+  keccak_lincheck_columns_kernel<<<2, KW_THREADS, smem, s>>>(eqi, ca, cb, kc);
+  LAUNCH_OK();
+}
+
 // z_vec[128 cc + t] = sum_row eq(row) * bit_t(z[(cc << nu) + row]). Block = (cc, row split),
 // thread = bit t; rows staged through shared memory.
 constexpr uint32_t ZV_TILE = 256;

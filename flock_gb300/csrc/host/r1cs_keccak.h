@@ -1,6 +1,7 @@
 // Keccak-f[1600] as a block R1CS over GF(2) with C = I and the constraint
 // definition held by a lincheck walker instead of materialised matrices
-// (crates/flock-prover/src/r1cs_hashes/keccak.rs:1-70, :430-560, :678-836).
+// (crates/flock-prover/src/r1cs_hashes/keccak.rs:1-70, :430-560, :678-836). The walker's
+// column folds run on the device (sumcheck.cu, keccak_lincheck_columns_kernel).
 //
 // Layout of one 2^16-bit block: state_0 at [0,1600) (lane-contiguous, slot of 2048),
 // state_24 at [2048,3648), the constant one at 4096, t_0..t_23 (the 24 chi
@@ -35,16 +36,6 @@ constexpr uint64_t RC[24] = {
 
 inline int state_idx(int x, int y, int z) { return x + 5 * y + 25 * z; }
 inline uint64_t rotl64(uint64_t v, uint32_t r) { r &= 63; return r ? (v << r) | (v >> (64 - r)) : v; }
-
-// The 11 state_in bits whose XOR is B[x,y,z], B = (pi o rho o theta)(state_in) (keccak.rs:147-175).
-inline void preimage(int x, int y, int z, int out[11]) {
-  int a = (x + 3 * y) % 5, b = x;
-  int r = (int)(RHO[a][b] % 64);
-  int c = (z + 64 - r) % 64, cp = (c + 63) % 64, am = (a + 4) % 5, ap = (a + 1) % 5;
-  out[0] = state_idx(a, b, c);
-  for (int yp = 0; yp < 5; ++yp) out[1 + yp] = state_idx(am, yp, c);
-  for (int yp = 0; yp < 5; ++yp) out[6 + yp] = state_idx(ap, yp, cp);
-}
 
 // Bit-packed state words (bit j of word i = state bit 64 i + j) -> Keccak lanes (x + 5y).
 inline void words_to_lanes(const uint64_t words[25], uint64_t lanes[25]) {
@@ -100,96 +91,6 @@ inline void witness_block(const uint64_t words[25], uint64_t* z, uint64_t* a, ui
 
 // Column position of state bit s of a lane-contiguous 1600-bit vector starting at u64 `base`.
 inline uint32_t lane_pos(uint32_t base_u64, int s) { return (base_u64 + s % 25) * 64 + s / 25; }
-
-// phi^T: out[s_in] = sum over s_out with s_in in preimage(s_out) of in[s_out].
-inline void apply_phi_t(const F128* in, F128* out) {
-  for (int s = 0; s < STATE_BITS; ++s) out[s] = F128();
-  for (int so = 0; so < STATE_BITS; ++so) {
-    int z = so / 25, xy = so % 25, y = xy / 5, x = xy % 5, pre[11];
-    preimage(x, y, z, pre);
-    for (int k = 0; k < 11; ++k) out[pre[k]] += in[so];
-  }
-}
-inline void apply_phi_bool(const bool* in, bool* out) {
-  for (int so = 0; so < STATE_BITS; ++so) {
-    int z = so / 25, xy = so % 25, y = xy / 5, x = xy % 5, pre[11];
-    preimage(x, y, z, pre);
-    bool v = false;
-    for (int k = 0; k < 11; ++k) v ^= in[pre[k]];
-    out[so] = v;
-  }
-}
-
-// The walker's two column marginals (eq^T A_0, eq^T B_0), kept apart — equal to
-// (fold(1) + fold(0), fold(0)) of KeccakLincheckCircuit::fold_alpha_batched
-// (keccak.rs:692-829). Additions only.
-inline void fold_split(const F128* eq, std::vector<F128>& ca, std::vector<F128>& cb) {
-  ca.assign(K, F128());
-  cb.assign(K, F128());
-  F128 e0 = eq[Z_CONST];
-  ca[Z_CONST] += e0; cb[Z_CONST] += e0;
-  for (int j = 0; j < STATE_BITS; ++j) {
-    uint32_t row = lane_pos(0, j);
-    ca[row] += eq[row];
-    cb[Z_CONST] += eq[row];
-  }
-  std::vector<F128> vec_pin(STATE_BITS);
-  F128 sum_pin;
-  for (int j = 0; j < STATE_BITS; ++j) { vec_pin[j] = eq[lane_pos(STATE24_BIT_BASE / 64, j)]; sum_pin += vec_pin[j]; }
-  cb[Z_CONST] += sum_pin;
-  std::vector<std::vector<F128>> chi_a(N_T, std::vector<F128>(STATE_BITS)), chi_b(N_T, std::vector<F128>(STATE_BITS));
-  F128 sum_t;
-  for (int r = 0; r < N_T; ++r)
-    for (int zp = 0; zp < 64; ++zp)
-      for (int y = 0; y < 5; ++y)
-        for (int x = 0; x < 5; ++x) {
-          F128 e = eq[lane_pos(T_PACKED_BIT_BASE / 64 + r * 25, state_idx(x, y, zp))];
-          sum_t += e;
-          int pre[11];
-          preimage((x + 1) % 5, y, zp, pre);
-          for (int k = 0; k < 11; ++k) chi_a[r][pre[k]] += e;
-          preimage((x + 2) % 5, y, zp, pre);
-          for (int k = 0; k < 11; ++k) chi_b[r][pre[k]] += e;
-        }
-  ca[Z_CONST] += sum_t;
-  std::vector<bool> rcv(STATE_BITS, false);
-  F128 rc_a, rc_b;
-  for (int r = 0; r < N_T; ++r) {
-    for (int s = 0; s < STATE_BITS; ++s) if (rcv[s]) { rc_a += chi_a[r][s]; rc_b += chi_b[r][s]; }
-    bool tmp_in[STATE_BITS], tmp_out[STATE_BITS];
-    for (int s = 0; s < STATE_BITS; ++s) tmp_in[s] = rcv[s];
-    apply_phi_bool(tmp_in, tmp_out);
-    for (int s = 0; s < STATE_BITS; ++s) rcv[s] = tmp_out[s];
-    for (int zp = 0; zp < 64; ++zp) if ((RC[r] >> zp) & 1) rcv[state_idx(0, 0, zp)] = !rcv[state_idx(0, 0, zp)];
-  }
-  F128 rc_pin;
-  for (int s = 0; s < STATE_BITS; ++s) if (rcv[s]) rc_pin += vec_pin[s];
-  ca[Z_CONST] += rc_a; cb[Z_CONST] += rc_b; ca[Z_CONST] += rc_pin;
-  // A-side transpose recurrence.
-  uint32_t t23 = T_PACKED_BIT_BASE / 64 + (N_T - 1) * 25;
-  for (int s = 0; s < STATE_BITS; ++s) ca[lane_pos(t23, s)] += vec_pin[s];
-  std::vector<F128> k(STATE_BITS), nk(STATE_BITS);
-  apply_phi_t(vec_pin.data(), k.data());
-  for (int s = 0; s < STATE_BITS; ++s) k[s] += chi_a[N_T - 1][s];
-  for (int r = N_T - 1; r >= 1; --r) {
-    uint32_t tb = T_PACKED_BIT_BASE / 64 + (r - 1) * 25;
-    for (int s = 0; s < STATE_BITS; ++s) ca[lane_pos(tb, s)] += k[s];
-    apply_phi_t(k.data(), nk.data());
-    for (int s = 0; s < STATE_BITS; ++s) nk[s] += chi_a[r - 1][s];
-    k.swap(nk);
-  }
-  for (int s = 0; s < STATE_BITS; ++s) ca[lane_pos(0, s)] += k[s];
-  // B-side.
-  k = chi_b[N_T - 1];
-  for (int r = N_T - 1; r >= 1; --r) {
-    uint32_t tb = T_PACKED_BIT_BASE / 64 + (r - 1) * 25;
-    for (int s = 0; s < STATE_BITS; ++s) cb[lane_pos(tb, s)] += k[s];
-    apply_phi_t(k.data(), nk.data());
-    for (int s = 0; s < STATE_BITS; ++s) nk[s] += chi_b[r - 1][s];
-    k.swap(nk);
-  }
-  for (int s = 0; s < STATE_BITS; ++s) cb[lane_pos(0, s)] += k[s];
-}
 
 // Empty K x K stub used for the registry digest of the walker-based type.
 inline const SparseRows& empty_stub() {

@@ -9,11 +9,13 @@
 //   zerocheck round 1    crates/flock-core/src/zerocheck/univariate_skip.rs:50-140, :380-470 (naive
 //                        definition, extract-c and s_hat_v_c forms), ntt.rs:18-117 (GF(2^8) NTT)
 //   zerocheck folds      zerocheck/multilinear.rs:250-330, :1148-1200
-//   lincheck             lincheck.rs:238-281 (column folds), :930-990 (row fold), :1479-1630 (sumcheck)
+//   lincheck             lincheck.rs:238-281 (column folds; Keccak-f from the forward rows,
+//                        keccak_columns.h), :930-990 (row fold), :1479-1630 (sumcheck)
 //   merged open          pcs/jagged.rs:1521-1650, :4693-4760
 //   Ligerito             pcs/ligerito/extension.rs:17-80, :210-260, :1507-1600, pcs/ligerito.rs:3086-3150
 #pragma once
 #include "../flock_gb300/csrc/host/prover.h"
+#include "keccak_columns.h"
 
 namespace flock {
 namespace oracle {
@@ -272,7 +274,7 @@ inline void lincheck_combs(const Statement& S, const std::vector<F128>& skip_w, 
     for (size_t i = b; i < e; ++i) eqi[i] = skip_w[i & 63] * er[i >> 6];
   });
   if (S.hash == HASH_KECCAK) {
-    kr1cs::fold_split(eqi.data(), comb_a, comb_b);
+    keccak_columns_forward(eqi.data(), comb_a, comb_b);
     return;
   }
   comb_a.assign(K, F128()); comb_b.assign(K, F128());

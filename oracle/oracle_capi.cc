@@ -132,7 +132,8 @@ int oracle_registry_digest_kat(int which, uint8_t out[32]) {
 }  // extern "C"
 
 // R1CS self-checks of one block per hash on seeded inputs (the encoders' satisfiability
-// and, for the walker-based Keccak type, the walker's transpose identity):
+// and, for the walker-based Keccak type, the transpose identity <eq, A z> = <eq^T A, z>
+// of the oracle's column folds):
 //   out[0] = rows where a != A z, out[1] = rows where b != B z (BLAKE3 / SHA-256, the
 //            materialised matrices; Keccak: 0 / 1 walker identity failures),
 //   out[2] = rows where a AND b != z (C = I),
@@ -161,7 +162,7 @@ extern "C" int oracle_r1cs_check(int hash_kind, uint64_t seed, uint64_t out[4]) 
       std::vector<F128> eq(K);
       for (auto& e : eq) e = F128(next(), next());
       std::vector<F128> ca, cb;
-      kr1cs::fold_split(eq.data(), ca, cb);
+      oracle::keccak_columns_forward(eq.data(), ca, cb);
       F128 l1, r1, l2, r2;
       for (uint32_t i = 0; i < K; ++i) {
         if (bit(a, i)) l1 += eq[i];
