@@ -480,11 +480,32 @@ def run_batched(args):
         setups.setdefault((kind, len(recs)), flock_gb300.SETUPS[kind](len(recs)))
     for (kind, n), st in setups.items():  # warm-up: device buffers and level twiddles
         st.prove_fast_bytes(next(r for k, r, _ in reqs if k == kind and len(r) == n), b"warm")
+    # device-busy fraction of the plain run: kernel time inside the stages (CUDA events
+    # around every stage; includes the device idle time inside a stage's round trips, so
+    # an upper bound) over the wall time
+    for st in setups.values():
+        st.set_stage_timing(True)
     t0 = time.perf_counter()
-    plain = [setups[(k, len(r))].prove_fast_bytes(r, d) for k, r, d in reqs]
+    plain = []
+    stage_ms = 0.0
+    for k, r, d in reqs:
+        st = setups[(k, len(r))]
+        plain.append(st.prove_fast_bytes(r, d))
+        stage_ms += sum(v[0] for v in st.last_stage_ms().values())
+    t_plain = time.perf_counter() - t0
+    for st in setups.values():
+        st.set_stage_timing(False)
+    t0 = time.perf_counter()
+    plain_untimed = [setups[(k, len(r))].prove_fast_bytes(r, d) for k, r, d in reqs]
     t_plain = time.perf_counter() - t0
     for st in setups.values():
         st.close()
+    if plain_untimed != plain:
+        raise SystemExit("plain proves differ between runs")
+    if args.plain_only:
+        print(json.dumps({"mode": "batched-plain", "plain_value": hashes / t_plain / 1e3, "unit": UNIT,
+                          "plain_s": t_plain, "stage_event_ms": stage_ms, "n_proofs": len(reqs)}), flush=True)
+        return 0
     with flock_gb300.ProofServer(workers=args.workers) as srv:
         srv.prove_batch(reqs, raw=True)  # warm-up: the server's provers for every shape of the batch
         t0 = time.perf_counter()
@@ -494,6 +515,7 @@ def run_batched(args):
     lat = sorted(o.latency_ms for o in outs)
     line = {"metric": METRIC, "mode": "batched", "value": hashes / t_batch / 1e3, "unit": UNIT,
             "plain_value": hashes / t_plain / 1e3, "speedup_vs_plain": t_plain / t_batch, "identical_bundles": same,
+            "plain_stage_event_busy_upper_bound": stage_ms / 1e3 / t_plain,
             "n_proofs": len(reqs), "hashes": hashes, "workers": args.workers,
             "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
             "config": {"workload": f"{len(reqs)} proofs, hash uniform over BLAKE3/SHA-256/Keccak-f, batch 2^U(10..{args.max_log})",
@@ -503,36 +525,51 @@ def run_batched(args):
 
 
 def run_served(args):
-    """Poisson arrivals at --rate proofs/s through the serving loop; p50/p99 latency."""
+    """Poisson arrivals through the serving loop at each rate of --rates (proofs/s); p50/p99
+    latency and throughput per rate, for the served form (--workers provers) and the plain
+    one-proof-at-a-time form (the same engine with one prover) on the same stream. Every
+    served bundle is checked against the plain one of the same request."""
     import random
 
     import flock_gb300
 
     reqs = mixed_workload(args.count, SEED + 1, 10, args.max_log)
-    rng = random.Random(SEED)
     hashes = sum(len(r) for _, r, _ in reqs)
-    with flock_gb300.ProofServer(workers=args.workers) as srv:
-        # warm-up: one request of every shape of the stream (provers, buffers, twiddles)
-        seen = {}
-        for k, r, d in reqs:
-            seen.setdefault((k, len(r)), (k, r, d))
-        srv.prove_batch(list(seen.values()), raw=True)
-        tickets = []
-        t0 = time.perf_counter()
-        t_next = t0
-        for k, r, d in reqs:
-            now = time.perf_counter()
-            if t_next > now:
-                time.sleep(t_next - now)
-            tickets.append(srv.submit(k, r, d))
-            t_next += rng.expovariate(args.rate)
-        outs = [srv.result(t, raw=True) for t in tickets]
-        t_all = time.perf_counter() - t0
-    lat = sorted(o.latency_ms for o in outs)
-    line = {"metric": METRIC, "mode": "served", "value": hashes / t_all / 1e3, "unit": UNIT,
-            "offered_rate_proofs_per_s": args.rate, "n_proofs": len(reqs), "workers": args.workers,
-            "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
-                           "max": lat[-1]},
+    rates = [float(x) for x in (args.rates.split(",") if args.rates else [args.rate])]
+
+    def serve(workers, rate):
+        rng = random.Random(SEED)
+        with flock_gb300.ProofServer(workers=workers, hbm_budget_bytes=args.hbm_budget_gib << 30) as srv:
+            # warm-up: one request of every shape of the stream (provers, buffers, twiddles)
+            seen = {}
+            for k, r, d in reqs:
+                seen.setdefault((k, len(r)), (k, r, d))
+            srv.prove_batch(list(seen.values()), raw=True)
+            tickets = []
+            t0 = time.perf_counter()
+            t_next = t0
+            for k, r, d in reqs:
+                now = time.perf_counter()
+                if t_next > now:
+                    time.sleep(t_next - now)
+                tickets.append(srv.submit(k, r, d))
+                t_next += rng.expovariate(rate)
+            outs = [srv.result(t, raw=True) for t in tickets]
+            t_all = time.perf_counter() - t0
+        lat = sorted(o.latency_ms for o in outs)
+        return outs, {"value": hashes / t_all / 1e3, "wall_s": t_all,
+                      "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                                     "max": lat[-1]}}
+
+    points = []
+    for rate in rates:
+        outs, served = serve(args.workers, rate)
+        plain_outs, plain = serve(1, rate)
+        same = all(a.bundle_bytes == b.bundle_bytes for a, b in zip(outs, plain_outs))
+        points.append({"offered_rate_proofs_per_s": rate, "served": served, "plain_one_prover": plain,
+                       "identical_bundles": same})
+    line = {"metric": METRIC, "mode": "served", "unit": UNIT, "n_proofs": len(reqs), "hashes": hashes,
+            "workers": args.workers, "hbm_budget_gib": args.hbm_budget_gib, "rates": points,
             "config": {"workload": f"{len(reqs)} Poisson arrivals, hash uniform, batch 2^U(10..{args.max_log})",
                        "seed": SEED}, "data": "synthetic (seeded SplitMix64 inputs)", "n_gpus": 1}
     print(json.dumps(line), flush=True)
@@ -556,6 +593,9 @@ def main():
     ap.add_argument("--max-log", type=int, default=16, help="largest batch 2^max_log in the mixed workloads")
     ap.add_argument("--workers", type=int, default=2)
     ap.add_argument("--rate", type=float, default=200.0, help="served mode: Poisson arrival rate (proofs/s)")
+    ap.add_argument("--rates", default="", help="served mode: comma-separated arrival rates to sweep")
+    ap.add_argument("--hbm-budget-gib", type=int, default=200, help="served mode: device-memory budget")
+    ap.add_argument("--plain-only", action="store_true", help="batched mode: the plain run only")
     args = ap.parse_args()
     if args.mode != "plain":
         import __graft_entry__

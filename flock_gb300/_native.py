@@ -29,6 +29,7 @@ EXPORTS = (
     "flock_gb300_launch_count",
     "flock_gb300_last_phase_ms",
     "flock_gb300_commit_cap_noalloc",
+    "flock_gb300_estimate_device_bytes",
     "flock_gb300_prove_batch",
     "flock_gb300_server_new",
     "flock_gb300_server_submit",
@@ -120,6 +121,8 @@ def load() -> ctypes.CDLL:
         lib.flock_gb300_commit_cap_noalloc.argtypes = [c.c_int, c.c_void_p, c.c_uint64, c.c_char_p, c.c_size_t,
                                                        c.POINTER(c.c_size_t), c.c_void_p]
         lib.flock_gb300_commit_cap_noalloc.restype = c.c_int
+        lib.flock_gb300_estimate_device_bytes.argtypes = [c.c_int, c.c_uint64, c.POINTER(c.c_uint64)]
+        lib.flock_gb300_estimate_device_bytes.restype = c.c_int
         lib.flock_gb300_prove_batch.argtypes = [c.POINTER(Request), c.c_size_t, c.c_int, c.c_uint64, c.POINTER(Result)]
         lib.flock_gb300_prove_batch.restype = c.c_int
         lib.flock_gb300_server_new.argtypes = [c.c_uint64, c.c_int, c.POINTER(c.c_void_p)]

@@ -220,6 +220,18 @@ int flock_gb300_proof_io(int hash_kind, uint64_t n_blocks, const uint8_t* bundle
   });
 }
 
+int flock_gb300_estimate_device_bytes(int hash_kind, uint64_t n_blocks, uint64_t* bytes) {
+  g_last_error.clear();
+  if (!bytes) return fail(FLOCK_GB300_EINVAL, "null argument");
+  if (hash_kind < 0 || hash_kind > 2) return fail(FLOCK_GB300_EINVAL, "unknown hash kind");
+  if (n_blocks < 8 || (n_blocks & (n_blocks - 1)) || n_blocks > (uint64_t(1) << 24))
+    return fail(FLOCK_GB300_EINVAL, "n_blocks must be a power of two in [8, 2^24]");
+  return guarded([&] {
+    *bytes = gpu::GpuBackend::estimate_device_bytes(*statement_for_shape((HashKind)hash_kind, (uint32_t)n_blocks));
+    return FLOCK_GB300_OK;
+  });
+}
+
 int flock_gb300_device_count(void) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;

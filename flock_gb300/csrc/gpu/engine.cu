@@ -7,6 +7,14 @@
 // device-memory budget: a worker takes a request only when the backend it needs is
 // already cached or fits in the budget next to everything else held; idle cached backends
 // of other shapes are evicted first. Results are byte-identical to one prove_fast call.
+//
+// Admission is first fit over the queue in arrival order, with aging: a request that later
+// requests have overtaken MAX_BYPASS times becomes a barrier, and nothing behind it is
+// admitted until it is, so a large request (a Keccak-f 2^18 proof needs about 35 GB) is not
+// starved by a stream of small ones. Statements (and their device-byte estimates) are
+// built by the submitting thread, and evicted backends are released by the worker that
+// evicted them after it leaves the engine lock, so neither a statement build nor a
+// cudaFree stalls the other workers' round trips.
 #include "../../../include/flock_gb300.h"
 #include "backend.h"
 #include <condition_variable>
@@ -33,6 +41,9 @@ struct Job {
   std::vector<uint8_t> inputs;
   std::vector<uint8_t> domain;
   double t_submit = 0;
+  std::shared_ptr<Statement> stmt;  // built at submission, outside the engine lock
+  uint64_t need = 0;                // device bytes of a new backend of this shape
+  uint32_t bypassed = 0;            // times a later request was admitted before this one
   // result
   bool done = false;
   int status = 0;
@@ -66,6 +77,8 @@ class Engine {
   }
 
   uint64_t submit(std::shared_ptr<Job> j) {
+    j->stmt = statement_for_shape((HashKind)j->hash, (uint32_t)j->n);
+    j->need = gpu::GpuBackend::estimate_device_bytes(*j->stmt);
     std::lock_guard<std::mutex> g(mu_);
     j->ticket = ++next_ticket_;
     j->t_submit = now_ms();
@@ -94,25 +107,41 @@ class Engine {
   };
 
   // Picks the first queued job whose backend is available (cached idle, or admissible
-  // within the budget after evicting idle backends). Called with mu_ held.
-  std::shared_ptr<Job> take(CachedBackend*& cb, bool& create, uint64_t& need) {
+  // within the budget after evicting idle backends), in arrival order; an aged job (see
+  // MAX_BYPASS) stops the scan. Evicted backends move to `evicted` for the caller to
+  // release outside the lock. Called with mu_ held.
+  static constexpr uint32_t MAX_BYPASS = 4;
+  std::shared_ptr<Job> take(CachedBackend*& cb, bool& create, uint64_t& need,
+                            std::vector<std::unique_ptr<CachedBackend>>& evicted) {
     for (auto it = queue_.begin(); it != queue_.end(); ++it) {
       auto j = *it;
+      auto admit = [&]() {
+        for (auto b = queue_.begin(); b != it; ++b) (*b)->bypassed++;
+        queue_.erase(it);
+        return j;
+      };
       Key key{j->hash, j->n};
       auto& lst = cache_[key];
       for (auto& c : lst)
         if (!c->busy) {
           cb = c.get();
           create = false;
-          queue_.erase(it);
-          return j;
+          return admit();
         }
-      need = est_[key];
-      if (!need) {
-        auto st = statement_for_shape((HashKind)j->hash, (uint32_t)j->n);
-        need = est_[key] = gpu::GpuBackend::estimate_device_bytes(*st);
+      need = j->need;
+      if (held_ + reserved_ + need > budget_) {
+        // evict only when that admits this job: idle backends (least recently used first)
+        // until it fits, or all of them when it then runs alone
+        uint64_t idle = 0;
+        for (auto& kv : cache_)
+          for (auto& c : kv.second)
+            if (!c->busy) idle += c->bytes;
+        const uint64_t after = held_ - idle + reserved_;
+        if (after + need > budget_ && after != 0) {
+          if (j->bypassed >= MAX_BYPASS) break;  // aged: wait for room rather than admit around it
+          continue;
+        }
       }
-      // evict idle backends (least recently used first) until the new one fits
       while (held_ + reserved_ + need > budget_) {
         CachedBackend* victim = nullptr;
         Key vkey;
@@ -127,16 +156,14 @@ class Engine {
         for (auto vi = vl.begin(); vi != vl.end(); ++vi)
           if (vi->get() == victim) {
             held_ -= victim->bytes;
+            evicted.push_back(std::move(*vi));
             vl.erase(vi);
             break;
           }
       }
-      if (held_ + reserved_ + need <= budget_ || (held_ + reserved_ == 0)) {
-        reserved_ += need;
-        create = true;
-        queue_.erase(it);
-        return j;
-      }
+      reserved_ += need;
+      create = true;
+      return admit();
     }
     return nullptr;
   }
@@ -148,11 +175,12 @@ class Engine {
       CachedBackend* cb = nullptr;
       bool create = false;
       uint64_t need = 0;
+      std::vector<std::unique_ptr<CachedBackend>> evicted;
       {
         std::unique_lock<std::mutex> g(mu_);
         cv_.wait(g, [&] {
           if (stop_) return true;
-          j = take(cb, create, need);
+          j = take(cb, create, need, evicted);
           return j != nullptr;
         });
         if (stop_ && !j) return;
@@ -161,10 +189,13 @@ class Engine {
           cb->last_use = ++clock_;
         }
       }
+      // device memory of evicted backends is released here, outside the lock and before this
+      // worker allocates the admitted job's backend
+      evicted.clear();
       try {
         if (create) {
           auto owned = std::make_unique<CachedBackend>();
-          owned->stmt = statement_for_shape((HashKind)j->hash, (uint32_t)j->n);
+          owned->stmt = j->stmt;
           owned->backend = std::make_unique<gpu::GpuBackend>(*owned->stmt);
           owned->busy = true;
           std::lock_guard<std::mutex> g(mu_);
@@ -208,7 +239,6 @@ class Engine {
   std::deque<std::shared_ptr<Job>> queue_;
   std::unordered_map<uint64_t, std::shared_ptr<Job>> jobs_;
   std::unordered_map<Key, std::list<std::unique_ptr<CachedBackend>>, KeyHash> cache_;
-  std::unordered_map<Key, uint64_t, KeyHash> est_;
   uint64_t held_ = 0, reserved_ = 0, clock_ = 0, next_ticket_ = 0;
   bool stop_ = false;
   std::vector<std::thread> threads_;

@@ -67,6 +67,15 @@ def _run_batch(call, requests, raw: bool):
     return outs
 
 
+def estimate_device_bytes(kind: int, n_blocks: int) -> int:
+    """Device bytes one prover of this shape holds (the admission figure of the batch and
+    serving entry points)."""
+    lib = _native.load()
+    out = ctypes.c_uint64()
+    _native.check(lib.flock_gb300_estimate_device_bytes(kind, n_blocks, ctypes.byref(out)))
+    return out.value
+
+
 def prove_batch(requests: Sequence[Tuple[int, np.ndarray, bytes]], workers: int = DEFAULT_WORKERS,
                 hbm_budget_bytes: int = 64 * GiB, raw: bool = False) -> List[Outcome]:
     """Proves [(kind, records, domain), ...] concurrently; results in request order. The

@@ -145,6 +145,12 @@ typedef struct {
   double latency_ms;       /* submission to completion */
 } flock_gb300_result;
 
+/* Device bytes a prover of (hash_kind, n_blocks) holds: the figure the batch and serving
+ * entry points admit requests by (witness, L0 codeword and tree, sumcheck and Ligerito
+ * buffers, scratch). Builds (and caches) the statement on the calling thread. No
+ * reference counterpart. */
+int flock_gb300_estimate_device_bytes(int hash_kind, uint64_t n_blocks, uint64_t* bytes);
+
 /* Proves n requests with `workers` concurrent provers within hbm_budget_bytes of device
  * memory (a request larger than the budget still runs, alone). results[i] answers reqs[i];
  * returns the first failing status, or 0. */

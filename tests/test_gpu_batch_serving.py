@@ -85,3 +85,35 @@ def test_server_batches_reuse_cached_provers():
         want = single(kind, len(recs), recs, dom)
         assert a.bundle_bytes == want and b.bundle_bytes == want
     assert extra.bundle.to_bytes() == first[0].bundle_bytes
+
+
+def test_large_request_is_admitted_while_small_ones_keep_arriving():
+    """Aging: a Keccak-f 2^18 request whose prover fits the budget only when no small
+    prover is busy is admitted after a few small requests overtake it, although small
+    requests keep arriving, and its bundle equals the single prove."""
+    from flock_gb300.serving import estimate_device_bytes
+
+    big_kind, big_n = KECCAK, 1 << 18
+    small_kind, small_n = SHA256, 1 << 15
+    need_big = estimate_device_bytes(big_kind, big_n)
+    need_small = estimate_device_bytes(small_kind, small_n)
+    big = inputs.batch(big_kind, big_n, 5)
+    small = [inputs.batch(small_kind, small_n, 100 + i) for i in range(3)]
+    max_small = 60
+    submitted, small_tickets = 0, []
+    with flock_gb300.ProofServer(hbm_budget_bytes=need_big + need_small // 2, workers=2) as srv:
+        for _ in range(4):
+            small_tickets.append((submitted, srv.submit(small_kind, small[submitted % 3], b"s%d" % submitted)))
+            submitted += 1
+        t_big = srv.submit(big_kind, big, b"big")
+        out_big = None
+        while out_big is None:
+            assert submitted < max_small, "the large request was starved by the stream of small ones"
+            small_tickets.append((submitted, srv.submit(small_kind, small[submitted % 3], b"s%d" % submitted)))
+            submitted += 1
+            out_big = srv.result(t_big, wait_ms=10, raw=True)
+        outs = [(i, srv.result(t, raw=True)) for i, t in small_tickets[:6]]
+    assert out_big.bundle_bytes == single(big_kind, big_n, big, b"big")
+    with flock_gb300.SETUPS[small_kind](small_n) as s:
+        for i, o in outs:
+            assert o.bundle_bytes == s.prove_fast_bytes(small[i % 3], b"s%d" % i)
