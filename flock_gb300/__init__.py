@@ -6,12 +6,12 @@ package is the host-side mirror of the reference's Setup / prove_fast interface.
 from ._native import BLAKE3, KECCAK, SHA256, FlockError, NativeLibraryError, load
 from .bundle import ProofBundle
 from .setups import (BLAKE3_DTYPE, KECCAK_DTYPE, SHA256_DTYPE, SETUPS, Blake3Setup, KeccakSetup,
-                     Sha256HybridSetup)
+                     Sha256HybridSetup, UnionSetup)
 from . import inputs
 from .serving import ProofServer, prove_batch
 
 __all__ = [
     "BLAKE3", "SHA256", "KECCAK", "FlockError", "NativeLibraryError", "load", "ProofBundle",
-    "Blake3Setup", "Sha256HybridSetup", "KeccakSetup", "SETUPS",
+    "Blake3Setup", "Sha256HybridSetup", "KeccakSetup", "SETUPS", "UnionSetup",
     "BLAKE3_DTYPE", "SHA256_DTYPE", "KECCAK_DTYPE", "inputs", "ProofServer", "prove_batch",
 ]

@@ -35,6 +35,10 @@ EXPORTS = (
     "flock_gb300_server_submit",
     "flock_gb300_server_poll",
     "flock_gb300_server_prove_batch",
+    "flock_gb300_union_setup_new",
+    "flock_gb300_union_setup_free",
+    "flock_gb300_prove_union",
+    "flock_gb300_mixed_proof_io",
     "flock_gb300_f128_mul_rate",
     "flock_gb300_proof_io",
     "flock_gb300_server_free",
@@ -136,6 +140,17 @@ def load() -> ctypes.CDLL:
         lib.flock_gb300_proof_io.argtypes = [c.c_int, c.c_uint64, c.c_char_p, c.c_size_t,
                                              c.POINTER(c.POINTER(c.c_uint8)), c.POINTER(c.c_size_t)]
         lib.flock_gb300_proof_io.restype = c.c_int
+        lib.flock_gb300_union_setup_new.argtypes = [c.POINTER(c.c_int), c.c_size_t, c.c_uint32,
+                                                    c.POINTER(c.c_void_p), c.POINTER(c.c_int)]
+        lib.flock_gb300_union_setup_new.restype = c.c_int
+        lib.flock_gb300_union_setup_free.argtypes = [c.c_void_p]
+        lib.flock_gb300_union_setup_free.restype = None
+        lib.flock_gb300_prove_union.argtypes = [c.c_void_p, c.POINTER(c.c_uint64), c.POINTER(c.c_void_p), c.c_char_p,
+                                                c.c_size_t, c.POINTER(c.POINTER(c.c_uint8)), c.POINTER(c.c_size_t)]
+        lib.flock_gb300_prove_union.restype = c.c_int
+        lib.flock_gb300_mixed_proof_io.argtypes = [c.c_void_p, c.POINTER(c.c_uint64), c.c_char_p, c.c_size_t,
+                                                   c.POINTER(c.POINTER(c.c_uint8)), c.POINTER(c.c_size_t)]
+        lib.flock_gb300_mixed_proof_io.restype = c.c_int
         lib.flock_gb300_f128_mul_rate.argtypes = [c.c_int, c.POINTER(c.c_double)]
         lib.flock_gb300_f128_mul_rate.restype = c.c_int
         lib.flock_gb300_server_free.argtypes = [c.c_void_p]

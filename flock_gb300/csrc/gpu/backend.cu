@@ -84,13 +84,18 @@ static uint64_t zc_tables_entries(uint32_t L) {
 // the constructor, the Ligerito level codewords and trees, the twiddle tables).
 uint64_t GpuBackend::estimate_device_bytes(const Statement& S) {
   const uint64_t W = uint64_t(1) << (S.m - 7), K = uint64_t(1) << S.k_log, n_pos = uint64_t(1) << S.k_code;
-  uint64_t b = (uint64_t)S.n_blocks * input_record_bytes(S.hash);
+  uint64_t b = 0;
+  for (const SlotInfo& t : S.slots) b += t.count * input_record_bytes(t.hash);
   b += 3 * W * 16;                          // z, a, b
+  if (!S.identity) b += S.committed_words * 16;  // the compacted stack
   b += n_pos * S.lanes * 16 + 2 * n_pos * 32;  // L0 codeword and tree
   b += (W / 2 * 2 + W * 2 + 64) * 16;       // zerocheck folds
   b += zc_tables_entries(S.m - 7) * 16;
   b += 6 * K * 16;                          // lincheck vectors
-  if (S.csc_a) b += 4 * (S.csc_a->col_ptr.size() + S.csc_a->rows_flat.size() + S.csc_b->col_ptr.size() + S.csc_b->rows_flat.size());
+  for (const SlotInfo& t : S.slots) {
+    b += 2 * (uint64_t(16) << t.k_log);
+    if (t.csc_a) b += 4 * (t.csc_a->col_ptr.size() + t.csc_a->rows_flat.size() + t.csc_b->col_ptr.size() + t.csc_b->rows_flat.size());
+  }
   b += (W + W + W / 2) * 16;                // merged weight and fold buffers
   b += W * 16 + 4 * (W / 2) * 32 + (W / 2) * 16;  // Ligerito basis, f/b ping-pong, pending
   b += (uint64_t(1) << 20) * 16 + 4096 * 16 + (size_t(96) << 20) + (size_t(8) << 20);  // partials, scratch, staging
@@ -115,7 +120,9 @@ GpuBackend::GpuBackend(const Statement& s) : S(s) {
   W_ = uint64_t(1) << (S.m - 7);
   K_ = 1u << S.k_log;
   const uint64_t W = W_;
-  in_bytes_ = (size_t)S.n_blocks * input_record_bytes(S.hash);
+  in_bytes_ = 0;
+  for (const SlotInfo& t : S.slots) in_bytes_ += (size_t)t.count * input_record_bytes(t.hash);
+  in_bytes_ = std::max<size_t>(in_bytes_, 16);
   d_in_ = dmalloc<uint8_t>(in_bytes_, owned_, device_bytes_);
   CUDA_OK(cudaMallocHost(&h_in_, in_bytes_));
   z_ = dmalloc<F128d>(W, owned_, device_bytes_);
@@ -134,24 +141,35 @@ GpuBackend::GpuBackend(const Statement& s) : S(s) {
   zc2a_ = dmalloc<F128d>(W, owned_, device_bytes_);
   zc2b_ = dmalloc<F128d>(W, owned_, device_bytes_);
   zc_w64_ = dmalloc<F128d>(64, owned_, device_bytes_);
-  eqi_ = dmalloc<F128d>(K_, owned_, device_bytes_);
-  ca_ = dmalloc<F128d>(K_, owned_, device_bytes_);
-  cb_ = dmalloc<F128d>(K_, owned_, device_bytes_);
   comb_ = dmalloc<F128d>(K_, owned_, device_bytes_);
   zv_ = dmalloc<F128d>(K_, owned_, device_bytes_);
   zvcap_ = dmalloc<F128d>(K_, owned_, device_bytes_);
-  if (S.hash != HASH_KECCAK) {
-    const Csc& A = *S.csc_a;
-    const Csc& B = *S.csc_b;
-    cola_ = dmalloc<uint32_t>(A.col_ptr.size(), owned_, device_bytes_);
-    rowa_ = dmalloc<uint32_t>(A.rows_flat.size(), owned_, device_bytes_);
-    colb_ = dmalloc<uint32_t>(B.col_ptr.size(), owned_, device_bytes_);
-    rowb_ = dmalloc<uint32_t>(B.rows_flat.size(), owned_, device_bytes_);
-    CUDA_OK(cudaMemcpy(cola_, A.col_ptr.data(), A.col_ptr.size() * 4, cudaMemcpyHostToDevice));
-    CUDA_OK(cudaMemcpy(rowa_, A.rows_flat.data(), A.rows_flat.size() * 4, cudaMemcpyHostToDevice));
-    CUDA_OK(cudaMemcpy(colb_, B.col_ptr.data(), B.col_ptr.size() * 4, cudaMemcpyHostToDevice));
-    CUDA_OK(cudaMemcpy(rowb_, B.rows_flat.data(), B.rows_flat.size() * 4, cudaMemcpyHostToDevice));
+  uint32_t k_max = 0;
+  for (const SlotInfo& t : S.slots) {
+    SlotDev sd;
+    sd.K = 1u << t.k_log;
+    k_max = std::max(k_max, sd.K);
+    sd.ca = dmalloc<F128d>(sd.K, owned_, device_bytes_);
+    sd.cb = dmalloc<F128d>(sd.K, owned_, device_bytes_);
+    if (t.hash != HASH_KECCAK) {
+      const Csc& A = *t.csc_a;
+      const Csc& B = *t.csc_b;
+      sd.cola = dmalloc<uint32_t>(A.col_ptr.size(), owned_, device_bytes_);
+      sd.rowa = dmalloc<uint32_t>(A.rows_flat.size(), owned_, device_bytes_);
+      sd.colb = dmalloc<uint32_t>(B.col_ptr.size(), owned_, device_bytes_);
+      sd.rowb = dmalloc<uint32_t>(B.rows_flat.size(), owned_, device_bytes_);
+      CUDA_OK(cudaMemcpy(sd.cola, A.col_ptr.data(), A.col_ptr.size() * 4, cudaMemcpyHostToDevice));
+      CUDA_OK(cudaMemcpy(sd.rowa, A.rows_flat.data(), A.rows_flat.size() * 4, cudaMemcpyHostToDevice));
+      CUDA_OK(cudaMemcpy(sd.colb, B.col_ptr.data(), B.col_ptr.size() * 4, cudaMemcpyHostToDevice));
+      CUDA_OK(cudaMemcpy(sd.rowb, B.rows_flat.data(), B.rows_flat.size() * 4, cudaMemcpyHostToDevice));
+    }
+    slot_dev_.push_back(sd);
   }
+  eqi_ = dmalloc<F128d>(k_max, owned_, device_bytes_);
+  ca_ = slot_dev_[0].ca;
+  cb_ = slot_dev_[0].cb;
+  Q_ = S.committed_words;
+  q_ = S.identity ? z_ : dmalloc<F128d>(Q_, owned_, device_bytes_);
   mw_ = dmalloc<F128d>(W, owned_, device_bytes_);
   moAq_ = dmalloc<F128d>(W / 2, owned_, device_bytes_);
   moAw_ = dmalloc<F128d>(W / 2, owned_, device_bytes_);
@@ -410,8 +428,38 @@ GpuBackend::EqSplit GpuBackend::eq_split_dev(const F128d* dp, uint32_t n, F128 s
 }
 
 // ------------------------------------------------------------------ witness + commit
-void GpuBackend::witness(const uint8_t* inputs) {
+void GpuBackend::witness(const std::vector<const uint8_t*>& slot_inputs) {
   scr_off_ = 0;
+  if (S.slots.size() != 1 || !S.identity) {
+    // union: each slot's records are staged into consecutive regions of the input buffer;
+    // the padded buffers are cleared (rows past a count, unused columns and gaps are zero)
+    // and each slot's witness is written into its aligned block
+    size_t off = 0;
+    std::vector<size_t> offs;
+    for (size_t t = 0; t < S.slots.size(); ++t) {
+      const size_t bytes = (size_t)S.slots[t].count * input_record_bytes(S.slots[t].hash);
+      offs.push_back(off);
+      if (bytes) {
+        memcpy(h_in_ + off, slot_inputs[t], bytes);
+        CUDA_OK(cudaMemcpyAsync(d_in_ + off, h_in_ + off, bytes, cudaMemcpyHostToDevice, st_));
+      }
+      h2d_ += bytes;
+      off += bytes;
+    }
+    Mark mk(this, ST_WITNESS);
+    CUDA_OK(cudaMemsetAsync(z_, 0, W_ * 16, st_));
+    CUDA_OK(cudaMemsetAsync(a_, 0, W_ * 16, st_));
+    CUDA_OK(cudaMemsetAsync(b_, 0, W_ * 16, st_));
+    for (size_t t = 0; t < S.slots.size(); ++t) {
+      const SlotInfo& T = S.slots[t];
+      if (!T.count) continue;
+      const size_t w0 = T.offset >> 7;
+      launch_witness((int)T.hash, d_in_ + offs[t], (uint32_t)T.count, S.nu, z_ + w0, a_ + w0, b_ + w0,
+                     (uint32_t)T.used_cols, st_);
+    }
+    return;
+  }
+  const uint8_t* inputs = slot_inputs[0];
   const void* src = d_user_inputs_;
   if (!src) {
     // Host inputs: staged into pinned memory by the host thread pool, 8 MiB at a time, each
@@ -434,7 +482,20 @@ void GpuBackend::witness(const uint8_t* inputs) {
 }
 
 void GpuBackend::commit_l0(uint32_t cap_depth, std::vector<Hash>& cap) {
-  { Mark mk(this, ST_L0_FILL); launch_fill_lane_major(z_, cw0_, S.lanes, S.log_dim, S.k_code, st_); }
+  if (!S.identity) {
+    // height-n_t compaction: each slot's used columns, the first `count` words of each,
+    // stacked column after column (one strided copy per slot), then the zero tail
+    Mark mk(this, ST_L0_FILL);
+    uint64_t cursor = 0;
+    for (const SlotInfo& T : S.slots) {
+      if (!T.count || !T.used_cols) continue;
+      CUDA_OK(cudaMemcpy2DAsync(q_ + cursor, T.count * 16, z_ + (T.offset >> 7), (size_t(16) << S.nu), T.count * 16,
+                                T.used_cols, cudaMemcpyDeviceToDevice, st_));
+      cursor += T.count * T.used_cols;
+    }
+    if (Q_ > cursor) CUDA_OK(cudaMemsetAsync(q_ + cursor, 0, (Q_ - cursor) * 16, st_));
+  }
+  { Mark mk(this, ST_L0_FILL); launch_fill_lane_major(q_, cw0_, S.lanes, S.log_dim, S.k_code, st_); }
   { Mark mk(this, ST_L0_NTT); launch_ntt(cw0_, S.lanes, S.k_code, 1, tw0_, st_); }
   { Mark mk(this, ST_L0_MERKLE); launch_merkle(cw0_, S.lanes, n_pos0_, tree0_, st_); }
   cap = read_cap(tree0_, n_pos0_, cap_depth);
@@ -595,10 +656,19 @@ void GpuBackend::zc_final(F128 rho, F128& ae, F128& be) {
 void GpuBackend::lc_comb(const std::vector<F128>& skip_w, const std::vector<F128>& xir) {
   scr_off_ = 0;
   const F128d* dw = upload(skip_w);
-  const F128d* der = upload(build_eq(xir));
-  Mark mk(this, ST_LINCHECK);
-  launch_lc_eq_inner(dw, der, K_, eqi_, st_);
-  if (S.hash == HASH_KECCAK) {
+  for (size_t t = 0; t < S.slots.size(); ++t) {
+    // slot t folds its own matrices by skip_w (x) eq(xir[.. k_log_t - 6])
+    const SlotInfo& T = S.slots[t];
+    const SlotDev& sd = slot_dev_[t];
+    const F128d* der = upload(build_eq(std::vector<F128>(xir.begin(), xir.begin() + (T.k_log - 6))));
+    Mark mk(this, ST_LINCHECK);
+    launch_lc_eq_inner(dw, der, sd.K, eqi_, st_);
+    lc_fold_slot(T.hash, sd);
+  }
+}
+
+void GpuBackend::lc_fold_slot(HashKind hash, const SlotDev& sd) {
+  if (hash == HASH_KECCAK) {
     // the walker's column folds on the device (no materialised matrices)
     static const KeccakColumnConsts kc = [] {
       KeccakColumnConsts c{};
@@ -607,13 +677,13 @@ void GpuBackend::lc_comb(const std::vector<F128>& skip_w, const std::vector<F128
         for (int b = 0; b < 5; ++b) c.rho[a + 5 * b] = (uint8_t)(kr1cs::RHO[a][b] % 64);
       return c;
     }();
-    CUDA_OK(cudaMemsetAsync(ca_, 0, K_ * 16, st_));
-    CUDA_OK(cudaMemsetAsync(cb_, 0, K_ * 16, st_));
-    launch_keccak_lincheck_columns(eqi_, ca_, cb_, kc, st_);
+    CUDA_OK(cudaMemsetAsync(sd.ca, 0, sd.K * 16, st_));
+    CUDA_OK(cudaMemsetAsync(sd.cb, 0, sd.K * 16, st_));
+    launch_keccak_lincheck_columns(eqi_, sd.ca, sd.cb, kc, st_);
     return;
   }
-  launch_csc_fold(cola_, rowa_, K_, eqi_, ca_, st_);
-  launch_csc_fold(colb_, rowb_, K_, eqi_, cb_, st_);
+  launch_csc_fold(sd.cola, sd.rowa, sd.K, eqi_, sd.ca, st_);
+  launch_csc_fold(sd.colb, sd.rowb, sd.K, eqi_, sd.cb, st_);
 }
 
 void GpuBackend::lc_zvec(const std::vector<F128>& x_outer) {
@@ -623,16 +693,28 @@ void GpuBackend::lc_zvec(const std::vector<F128>& x_outer) {
   F128d* eq = static_cast<F128d*>(scratch(size_t(16) << nu));
   Mark mk(this, ST_LINCHECK);
   launch_eq_table(dp, nu, dev(F128::one()), eq, st_);
-  uint32_t used = (uint32_t)S.geo.used_cols;
+  // a single slot folds its used columns only; a union folds every union column (the
+  // gaps and unused columns of z are zero)
+  uint32_t used = S.slots.size() == 1 ? (uint32_t)S.slots[0].used_cols : K_ / 128;
   if ((uint64_t)used * 128 < K_) CUDA_OK(cudaMemsetAsync(zv_ + used * 128, 0, (K_ - used * 128) * 16, st_));
   launch_lc_zvec(z_, nu, used, eq, part_, zv_, st_);
   CUDA_OK(cudaMemcpyAsync(zvcap_, zv_, K_ * 16, cudaMemcpyDeviceToDevice, st_));
   lc_len_ = K_;
 }
 
-void GpuBackend::lc_start(F128 alpha, F128 beta, uint32_t pin, F128& e1, F128& ei) {
+void GpuBackend::lc_start(F128 alpha, const std::vector<SlotComb>& sc, F128& e1, F128& ei) {
   uint32_t nb;
-  { Mark mk(this, ST_LINCHECK); nb = launch_lc_start(ca_, cb_, dev(alpha), dev(beta), pin, K_, comb_, zv_, part_, st_); }
+  if (S.slots.size() == 1 && sc[0].offset == 0 && sc[0].weight == F128::one()) {
+    Mark mk(this, ST_LINCHECK);
+    nb = launch_lc_start(ca_, cb_, dev(alpha), dev(sc[0].beta), sc[0].pin, K_, comb_, zv_, part_, st_);
+  } else {
+    Mark mk(this, ST_LINCHECK);
+    CUDA_OK(cudaMemsetAsync(comb_, 0, size_t(K_) * 16, st_));
+    for (size_t t = 0; t < S.slots.size(); ++t)
+      launch_lc_slot_comb(slot_dev_[t].ca, slot_dev_[t].cb, dev(alpha), dev(sc[t].weight), dev(sc[t].beta), sc[t].pin,
+                          slot_dev_[t].K, comb_ + sc[t].offset, st_);
+    nb = launch_lc_top_message(comb_, zv_, K_, part_, st_);
+  }
   auto v = reduce(nb, 2);
   e1 = v[0];
   ei = v[1];
@@ -654,15 +736,21 @@ void GpuBackend::lc_partial(std::vector<F128>& zp) {
   zp = fetch(zv_, 64);
 }
 
-void GpuBackend::lc_matrix_evals(const std::vector<F128>& rest, const std::vector<F128>& zp, F128& ea, F128& eb) {
-  scr_off_ = 0;
-  const F128d* der = upload(build_eq(rest));
-  const F128d* dzp = upload(zp);
-  uint32_t nb;
-  { Mark mk(this, ST_LINCHECK); nb = launch_lc_matrix_evals(ca_, cb_, der, dzp, K_, part_, st_); }
-  auto v = reduce(nb, 2);
-  ea = v[0];
-  eb = v[1];
+void GpuBackend::lc_matrix_evals(const std::vector<F128>& rest, const std::vector<F128>& zp,
+                                 std::vector<Pair128>& evals) {
+  for (size_t t = 0; t < S.slots.size(); ++t) {
+    scr_off_ = 0;
+    const SlotInfo& T = S.slots[t];
+    const F128d* der = upload(build_eq(std::vector<F128>(rest.begin(), rest.begin() + (T.k_log - 6))));
+    const F128d* dzp = upload(zp);
+    uint32_t nb;
+    {
+      Mark mk(this, ST_LINCHECK);
+      nb = launch_lc_matrix_evals(slot_dev_[t].ca, slot_dev_[t].cb, der, dzp, slot_dev_[t].K, part_, st_);
+    }
+    auto v = reduce(nb, 2);
+    evals.push_back({v[0], v[1]});
+  }
 }
 
 void GpuBackend::lc_s_hat_v(const std::vector<F128>& tail, std::vector<F128>& out) {
@@ -688,7 +776,21 @@ uint32_t GpuBackend::launch_build_w(const std::vector<WeightClaim>& cl, uint32_t
   std::vector<F128> tabs(cl[0].table);
   tabs.insert(tabs.end(), cl[1].table.begin(), cl[1].table.end());
   const F128d* dt = upload(tabs);
-  return launch_mo_build_w(z_, er[0], ec[0], er[1], ec[1], dt, nu, area, W_, mw_, part_, st_);
+  if (S.slots.size() == 1 && S.identity)
+    return launch_mo_build_w(q_, er[0], ec[0], er[1], ec[1], dt, nu, area, Q_, mw_, part_, st_);
+  JaggedSegs g;
+  uint64_t base = 0;
+  for (const SlotInfo& T : S.slots) {
+    if (!T.count || !T.used_cols) continue;
+    if (g.n == 4) throw std::runtime_error("the merged weight supports at most four non-empty slots");
+    g.base[g.n] = base;
+    g.rows[g.n] = T.count;
+    g.cols[g.n] = T.used_cols;
+    g.col_off[g.n] = T.col_offset(S.nu);
+    base += T.count * T.used_cols;
+    g.n++;
+  }
+  return launch_mo_build_w(q_, er[0], ec[0], er[1], ec[1], dt, nu, area, Q_, mw_, part_, st_, &g);
 }
 
 void GpuBackend::mo_build_w(const std::vector<WeightClaim>& cl, uint32_t nu, uint64_t area, F128& u0, F128& u2) {
@@ -701,9 +803,9 @@ void GpuBackend::mo_build_w(const std::vector<WeightClaim>& cl, uint32_t nu, uin
   auto v = reduce(nb, 2);
   u0 = v[0];
   u2 = v[1];
-  mo_q_ = z_;
+  mo_q_ = q_;
   mo_w_ = mw_;
-  mo_len_ = W_;
+  mo_len_ = Q_;
 }
 
 void GpuBackend::mo_round(F128 r, bool last, F128& g1, F128& gi) {
@@ -742,11 +844,11 @@ F128 GpuBackend::mo_q_eval() {
 void GpuBackend::lg_basis_eq(F128 gamma, const std::vector<F128>& rho) {
   lg_flush_fold();
   scr_off_ = 0;
-  if ((uint64_t(1) << rho.size()) != W_) throw std::runtime_error("Ligerito basis size mismatch");
+  if ((uint64_t(1) << rho.size()) != Q_) throw std::runtime_error("Ligerito basis size mismatch");
   EqSplit e = eq_split(rho, gamma, 10);
-  { Mark mk(this, ST_LIGERITO); launch_lg_eq_fill(e.lo, e.lo_bits, e.hi, W_, lb128_, false, st_); }
+  { Mark mk(this, ST_LIGERITO); launch_lg_eq_fill(e.lo, e.lo_bits, e.hi, Q_, lb128_, false, st_); }
   lg_base_ = true;
-  lg_n_ = W_;
+  lg_n_ = Q_;
   lg_cur_ = 0;
 }
 
@@ -756,7 +858,7 @@ F128 GpuBackend::lg_eval_eq(const std::vector<F128>& zp) {
   if (!lg_base_) throw std::runtime_error("OOD evaluation expects the committed base vector");
   EqSplit e = eq_split(zp, F128::one(), 10);
   uint32_t nb;
-  { Mark mk(this, ST_LIGERITO); nb = launch_lg_dot_eq(z_, 1, e.lo, e.lo_bits, e.hi, W_, part_, st_); }
+  { Mark mk(this, ST_LIGERITO); nb = launch_lg_dot_eq(q_, 1, e.lo, e.lo_bits, e.hi, Q_, part_, st_); }
   return reduce(nb, 1)[0];
 }
 
@@ -765,7 +867,7 @@ void GpuBackend::lg_add_eq(F128 beta, const std::vector<F128>& zp) {
   scr_off_ = 0;
   if (!lg_base_) throw std::runtime_error("basis update expects the base stage");
   EqSplit e = eq_split(zp, beta, 10);
-  { Mark mk(this, ST_LIGERITO); launch_lg_eq_fill(e.lo, e.lo_bits, e.hi, W_, lb128_, true, st_); }
+  { Mark mk(this, ST_LIGERITO); launch_lg_eq_fill(e.lo, e.lo_bits, e.hi, Q_, lb128_, true, st_); }
 }
 
 Msg256 GpuBackend::lg_message(size_t d) {
@@ -794,7 +896,7 @@ Msg256 GpuBackend::lg_message(size_t d) {
   Msg256 m;
   if (lg_base_) {
     FusedPublish fp = fused_publish();
-    { Mark mk(this, ST_LIGERITO); launch_lg_message128(z_, lb128_, n, d, part_, st_, fp); }
+    { Mark mk(this, ST_LIGERITO); launch_lg_message128(q_, lb128_, n, d, part_, st_, fp); }
     auto v = read_published(fp.seq, 2);
     m.u0 = F256(v[0]);
     m.u2 = F256(v[1]);
@@ -833,7 +935,7 @@ void GpuBackend::lg_fold(F256 r, size_t d) {
   uint64_t n_out = lg_n_ / 2;
   Mark mk(this, ST_LIGERITO);
   if (lg_base_) {
-    launch_lg_fold128(z_, lb128_, n_out, dev(r), nullptr, d, lf_[0], lb_[0], st_);
+    launch_lg_fold128(q_, lb128_, n_out, dev(r), nullptr, d, lf_[0], lb_[0], st_);
     lg_cur_ = 0;
     lg_base_ = false;
   } else {

@@ -16,7 +16,7 @@ class GpuBackend : public ProverBackend {
   GpuBackend(const GpuBackend&) = delete;
   GpuBackend& operator=(const GpuBackend&) = delete;
 
-  void witness(const uint8_t* inputs) override;
+  void witness(const std::vector<const uint8_t*>& slot_inputs) override;
   void commit_l0(uint32_t cap_depth, std::vector<Hash>& cap) override;
   void zc_round1(const std::vector<F128>& r, std::vector<F128>& ab, std::vector<F128>& c,
                  std::vector<F128>& s_hat_v_c) override;
@@ -25,10 +25,11 @@ class GpuBackend : public ProverBackend {
   void zc_final(F128 rho, F128& a_eval, F128& b_eval) override;
   void lc_comb(const std::vector<F128>& skip_w, const std::vector<F128>& x_inner_rest) override;
   void lc_zvec(const std::vector<F128>& x_outer) override;
-  void lc_start(F128 alpha, F128 beta, uint32_t pin, F128& e1, F128& einf) override;
+  void lc_start(F128 alpha, const std::vector<SlotComb>& slots, F128& e1, F128& einf) override;
   void lc_round(F128 r, bool last, F128& e1, F128& einf) override;
   void lc_partial(std::vector<F128>& z_partial64) override;
-  void lc_matrix_evals(const std::vector<F128>& rest_point, const std::vector<F128>& zp, F128& ea, F128& eb) override;
+  void lc_matrix_evals(const std::vector<F128>& rest_point, const std::vector<F128>& zp,
+                       std::vector<Pair128>& evals) override;
   void lc_s_hat_v(const std::vector<F128>& tail, std::vector<F128>& out128) override;
   void mo_build_w(const std::vector<WeightClaim>& claims, uint32_t nu, uint64_t area, F128& u0, F128& u2) override;
   void mo_round(F128 r, bool last, F128& g1, F128& ginf) override;
@@ -133,6 +134,17 @@ class GpuBackend : public ProverBackend {
   uint8_t* d_in_ = nullptr;
   uint8_t* h_in_ = nullptr;
   F128d *z_ = nullptr, *a_ = nullptr, *b_ = nullptr;
+  // the committed stack: z_ itself under identity compaction, else its own Q_ words
+  F128d* q_ = nullptr;
+  uint64_t Q_ = 0;
+  // per-slot lincheck state: the slot's column folds and its matrices (CSC) on the device
+  struct SlotDev {
+    F128d *ca = nullptr, *cb = nullptr;
+    uint32_t *cola = nullptr, *rowa = nullptr, *colb = nullptr, *rowb = nullptr;
+    uint32_t K = 0;
+  };
+  std::vector<SlotDev> slot_dev_;
+  void lc_fold_slot(HashKind hash, const SlotDev& sd);
   uint64_t n_pos0_ = 0;
   F128d* cw0_ = nullptr;
   uint8_t* tree0_ = nullptr;

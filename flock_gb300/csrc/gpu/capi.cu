@@ -3,7 +3,9 @@
 #include "backend.h"
 #include "../host/proof_io.h"
 #include <cstdlib>
+#include <map>
 #include <memory>
+#include <mutex>
 
 using namespace flock;
 
@@ -228,6 +230,114 @@ int flock_gb300_estimate_device_bytes(int hash_kind, uint64_t n_blocks, uint64_t
     return fail(FLOCK_GB300_EINVAL, "n_blocks must be a power of two in [8, 2^24]");
   return guarded([&] {
     *bytes = gpu::GpuBackend::estimate_device_bytes(*statement_for_shape((HashKind)hash_kind, (uint32_t)n_blocks));
+    return FLOCK_GB300_OK;
+  });
+}
+
+}  // extern "C"
+
+struct flock_gb300_union_setup {
+  std::vector<HashKind> kinds;  // slot order
+  uint32_t nu = 0;
+  std::array<uint8_t, 32> digest{};
+  std::mutex mu;
+  struct Prover {
+    std::shared_ptr<Statement> stmt;
+    std::unique_ptr<gpu::GpuBackend> backend;
+  };
+  std::map<std::vector<uint64_t>, Prover> provers;  // per counts vector
+  std::shared_ptr<Statement> statement(const std::vector<uint64_t>& counts) {
+    auto s = std::make_shared<Statement>(make_union_statement(kinds, nu, counts));
+    s->registry_digest = digest;
+    return s;
+  }
+};
+
+extern "C" {
+
+int flock_gb300_union_setup_new(const int* hash_kinds, size_t n_types, uint32_t nu, flock_gb300_union_setup** out,
+                                int* slot_kinds) {
+  g_last_error.clear();
+  if (!out || !hash_kinds || !n_types) return fail(FLOCK_GB300_EINVAL, "null argument");
+  *out = nullptr;
+  if (n_types > 3) return fail(FLOCK_GB300_EINVAL, "at most three hash types");
+  if (nu < 3 || nu > 24) return fail(FLOCK_GB300_EINVAL, "nu must be in [3, 24]");
+  std::vector<HashKind> kinds;
+  for (size_t i = 0; i < n_types; ++i) {
+    if (hash_kinds[i] < 0 || hash_kinds[i] > 2) return fail(FLOCK_GB300_EINVAL, "unknown hash kind");
+    for (HashKind k : kinds)
+      if (k == (HashKind)hash_kinds[i]) return fail(FLOCK_GB300_EINVAL, "registry types must be distinct");
+    kinds.push_back((HashKind)hash_kinds[i]);
+  }
+  return guarded([&] {
+    auto u = std::make_unique<flock_gb300_union_setup>();
+    for (size_t i : registry_slot_order(kinds)) u->kinds.push_back(kinds[i]);
+    u->nu = nu;
+    // the registry digest does not depend on the counts
+    Statement s = make_union_statement(u->kinds, nu, std::vector<uint64_t>(u->kinds.size(), 0));
+    compute_registry_digest(s);
+    u->digest = s.registry_digest;
+    if (slot_kinds)
+      for (size_t i = 0; i < u->kinds.size(); ++i) slot_kinds[i] = (int)u->kinds[i];
+    *out = u.release();
+    return FLOCK_GB300_OK;
+  });
+}
+
+void flock_gb300_union_setup_free(flock_gb300_union_setup* setup) { delete setup; }
+
+int flock_gb300_prove_union(flock_gb300_union_setup* setup, const uint64_t* counts, const void* const* inputs,
+                            const uint8_t* domain, size_t domain_len, uint8_t** out, size_t* out_len) {
+  g_last_error.clear();
+  if (!setup || !counts || !inputs || !out || !out_len || (!domain && domain_len))
+    return fail(FLOCK_GB300_EINVAL, "null argument");
+  *out = nullptr;
+  *out_len = 0;
+  std::vector<uint64_t> cv(counts, counts + setup->kinds.size());
+  for (size_t t = 0; t < cv.size(); ++t) {
+    if (cv[t] > (uint64_t(1) << setup->nu)) return fail(FLOCK_GB300_EINVAL, "declared count exceeds 2^nu");
+    if (cv[t] && !inputs[t]) return fail(FLOCK_GB300_EINVAL, "null input records for a non-empty slot");
+  }
+  return guarded([&] {
+    std::lock_guard<std::mutex> g(setup->mu);
+    auto it = setup->provers.find(cv);
+    if (it == setup->provers.end()) {
+      if (setup->provers.size() >= 4) setup->provers.erase(setup->provers.begin());
+      flock_gb300_union_setup::Prover p;
+      p.stmt = setup->statement(cv);
+      p.backend = std::make_unique<gpu::GpuBackend>(*p.stmt);
+      it = setup->provers.emplace(cv, std::move(p)).first;
+    }
+    auto& P = it->second;
+    CUDA_OK(cudaSetDevice(P.backend->device()));
+    P.backend->begin_prove(nullptr);
+    std::vector<const uint8_t*> in;
+    for (size_t t = 0; t < cv.size(); ++t) in.push_back(static_cast<const uint8_t*>(inputs[t]));
+    ProveResult R = prove_fast(*P.stmt, *P.backend, in, domain, domain_len);
+    std::vector<uint8_t> bundle = make_bundle(R);
+    *out = static_cast<uint8_t*>(malloc(bundle.size()));
+    if (!*out) return fail(FLOCK_GB300_EINTERNAL, "out of host memory");
+    memcpy(*out, bundle.data(), bundle.size());
+    *out_len = bundle.size();
+    return FLOCK_GB300_OK;
+  });
+}
+
+int flock_gb300_mixed_proof_io(const flock_gb300_union_setup* setup, const uint64_t* counts, const uint8_t* bundle,
+                               size_t bundle_len, uint8_t** out, size_t* out_len) {
+  g_last_error.clear();
+  if (!setup || !counts || !bundle || !out || !out_len) return fail(FLOCK_GB300_EINVAL, "null argument");
+  return guarded([&] {
+    auto u = const_cast<flock_gb300_union_setup*>(setup);
+    std::vector<uint64_t> cv(counts, counts + u->kinds.size());
+    for (uint64_t c : cv)
+      if (c > (uint64_t(1) << u->nu)) return fail(FLOCK_GB300_EINVAL, "declared count exceeds 2^nu");
+    auto s = u->statement(cv);
+    std::vector<uint8_t> v = mixed_proof_io_from_bundle(*s, bundle, bundle_len);
+    *out = static_cast<uint8_t*>(malloc(v.size()));
+    if (!*out) return fail(FLOCK_GB300_EINTERNAL, "out of host memory");
+    memcpy(*out, v.data(), v.size());
+    *out_len = v.size();
     return FLOCK_GB300_OK;
   });
 }

@@ -103,13 +103,25 @@ uint32_t launch_lc_start(const F128d* ca, const F128d* cb, F128d alpha, F128d be
                          F128d* comb, const F128d* zv, F128d* part, cudaStream_t s);                   // width 2
 uint32_t launch_lc_round(F128d* comb, F128d* zv, uint32_t len, F128d r, bool msg, F128d* part, cudaStream_t s,
                          FusedPublish pub = FusedPublish());
+// Union lincheck: one slot's weighted comb (out = weight (alpha ca + cb), + beta at pin),
+// and the first message of a comb built that way.
+void launch_lc_slot_comb(const F128d* ca, const F128d* cb, F128d alpha, F128d weight, F128d beta, uint32_t pin,
+                         uint32_t K, F128d* out, cudaStream_t s);
+uint32_t launch_lc_top_message(const F128d* comb, const F128d* zv, uint32_t K, F128d* part, cudaStream_t s);  // width 2
 uint32_t launch_lc_matrix_evals(const F128d* ca, const F128d* cb, const F128d* er, const F128d* zp, uint32_t K,
                                 F128d* part, cudaStream_t s);                                          // width 2
 void launch_lc_s_hat_v(const F128d* zv, const F128d* et, uint32_t n_tail, F128d* out, cudaStream_t s);
 
+// The committed stack of a union with non-identity compaction, as at most four slot
+// segments (dense [base, base + rows * cols), column-major, first column col_off).
+struct JaggedSegs {
+  uint32_t n = 0;
+  uint64_t base[4] = {0, 0, 0, 0}, rows[4] = {1, 1, 1, 1}, cols[4] = {0, 0, 0, 0}, col_off[4] = {0, 0, 0, 0};
+};
+// segs == nullptr: the aligned layout (row = d mod 2^nu, col = d >> nu).
 uint32_t launch_mo_build_w(const F128d* q, const F128d* er0, const F128d* ec0, const F128d* er1, const F128d* ec1,
                            const F128d* tables, uint32_t nu, uint64_t area, uint64_t n, F128d* w, F128d* part,
-                           cudaStream_t s);                                                            // width 2
+                           cudaStream_t s, const JaggedSegs* segs = nullptr);                          // width 2
 
 void launch_lg_eq_fill(const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, uint64_t n, F128d* out, bool add,
                        cudaStream_t s);

@@ -772,6 +772,44 @@ uint32_t launch_lc_start(const F128d* ca, const F128d* cb, F128d alpha, F128d be
   LAUNCH_OK();
   return blocks;
 }
+// A union slot's share of the lincheck comb: out[i] = weight (alpha ca[i] + cb[i]), plus
+// beta at the slot's const-pin column.
+__global__ void lc_slot_comb_kernel(const F128d* __restrict__ ca, const F128d* __restrict__ cb, F128d alpha,
+                                    F128d weight, F128d beta, uint32_t pin, uint32_t K, F128d* __restrict__ out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x) {
+    F128d c = weight * (alpha * ca[i] + cb[i]);
+    if (i == pin) c += beta;
+    out[i] = c;
+  }
+}
+void launch_lc_slot_comb(const F128d* ca, const F128d* cb, F128d alpha, F128d weight, F128d beta, uint32_t pin,
+                         uint32_t K, F128d* out, cudaStream_t s) {
+  lc_slot_comb_kernel<<<std::max(1u, std::min((K + 255) / 256, 1024u)), 256, 0, s>>>(ca, cb, alpha, weight, beta, pin,
+                                                                                    K, out);
+  LAUNCH_OK();
+}
+// First top-variable message of a built comb against zv (pairs (i, i + K/2)).
+__global__ void lc_top_message_kernel(const F128d* __restrict__ comb, const F128d* __restrict__ zv, uint32_t K,
+                                      F128d* __restrict__ part) {
+  __shared__ F128d sh[32];
+  uint32_t h = K / 2;
+  F128d e1 = f128_zero(), ei = f128_zero();
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < h; i += gridDim.x * blockDim.x) {
+    F128d c0 = comb[i], c1 = comb[i + h], z0 = zv[i], z1 = zv[i + h];
+    e1 += c1 * z1;
+    ei += (c0 + c1) * (z0 + z1);
+  }
+  e1 = block_xor(e1, sh);
+  ei = block_xor(ei, sh);
+  if (threadIdx.x == 0) { part[blockIdx.x * 2] = e1; part[blockIdx.x * 2 + 1] = ei; }
+}
+uint32_t launch_lc_top_message(const F128d* comb, const F128d* zv, uint32_t K, F128d* part, cudaStream_t s) {
+  uint32_t blocks = std::max(1u, std::min((K / 2 + 255) / 256, 256u));
+  lc_top_message_kernel<<<blocks, 256, 0, s>>>(comb, zv, K, part);
+  LAUNCH_OK();
+  return blocks;
+}
+
 // Bind the top variable of comb and zv (length len -> len/2) in place and emit the next
 // top-variable message over the bound vectors (pairs (i, i + len/4)).
 __global__ void lc_round_kernel(F128d* __restrict__ comb, F128d* __restrict__ zv, uint32_t len, F128d r, int msg,
@@ -861,10 +899,27 @@ __device__ __forceinline__ F128d fold_slot(F128d x, const F128d* tab) {
   for (int k = 0; k < 8; ++k) acc += tab[(8 + k) * 256 + ((x.hi >> (8 * k)) & 255)];
   return acc;
 }
+// Jagged unrank of a union's committed stack: slot s holds dense [base, base + rows * cols),
+// column-major with `rows` (the declared count) words per column, its first column at
+// union chunk-column col_off.
+__device__ __forceinline__ bool jagged_unrank(const JaggedSegs& g, uint64_t d, uint64_t& row, uint64_t& col) {
+  for (uint32_t s = 0; s < g.n; ++s) {
+    const uint64_t end = g.base[s] + g.rows[s] * g.cols[s];
+    if (d >= g.base[s] && d < end) {
+      const uint64_t local = d - g.base[s];
+      col = g.col_off[s] + local / g.rows[s];
+      row = local % g.rows[s];
+      return true;
+    }
+  }
+  return false;
+}
+template <bool JAGGED>
 __global__ void __launch_bounds__(512, 1)
 mo_build_w_kernel(const F128d* __restrict__ q, const F128d* __restrict__ er0, const F128d* __restrict__ ec0,
                   const F128d* __restrict__ er1, const F128d* __restrict__ ec1, const F128d* __restrict__ tables,
-                  uint32_t nu, uint64_t area, uint64_t n, F128d* __restrict__ w, F128d* __restrict__ part) {
+                  uint32_t nu, uint64_t area, uint64_t n, F128d* __restrict__ w, F128d* __restrict__ part,
+                  JaggedSegs segs) {
   extern __shared__ __align__(16) F128d tab[];  // 2 x 16 x 256
   __shared__ F128d sh[32];
   for (uint32_t i = threadIdx.x; i < 2 * 16 * 256; i += blockDim.x) tab[i] = tables[i];
@@ -877,10 +932,9 @@ mo_build_w_kernel(const F128d* __restrict__ q, const F128d* __restrict__ er0, co
     for (int k = 0; k < 2; ++k) {
       uint64_t d = 2 * i + k;
       F128d acc = f128_zero();
-      if (d < area) {
-        uint64_t row = d & rmask, col = d >> nu;
+      uint64_t row = d & rmask, col = d >> nu;
+      if (d < area && (!JAGGED || jagged_unrank(segs, d, row, col)))
         acc = fold_slot(mul_call(er0[row], ec0[col]), tab) + fold_slot(mul_call(er1[row], ec1[col]), tab + 16 * 256);
-      }
       W[k] = acc;
       w[d] = acc;
     }
@@ -894,11 +948,17 @@ mo_build_w_kernel(const F128d* __restrict__ q, const F128d* __restrict__ er0, co
 }
 uint32_t launch_mo_build_w(const F128d* q, const F128d* er0, const F128d* ec0, const F128d* er1, const F128d* ec1,
                            const F128d* tables, uint32_t nu, uint64_t area, uint64_t n, F128d* w, F128d* part,
-                           cudaStream_t s) {
+                           cudaStream_t s, const JaggedSegs* segs) {
   size_t smem = 2 * 16 * 256 * sizeof(F128d);
-  set_dynamic_smem((const void*)mo_build_w_kernel, (int)smem);
   uint32_t blocks = (uint32_t)std::min<uint64_t>((n / 2 + 511) / 512, (uint64_t)sm_count());
-  mo_build_w_kernel<<<blocks, 512, smem, s>>>(q, er0, ec0, er1, ec1, tables, nu, area, n, w, part);
+  if (segs) {
+    set_dynamic_smem((const void*)mo_build_w_kernel<true>, (int)smem);
+    mo_build_w_kernel<true><<<blocks, 512, smem, s>>>(q, er0, ec0, er1, ec1, tables, nu, area, n, w, part, *segs);
+  } else {
+    set_dynamic_smem((const void*)mo_build_w_kernel<false>, (int)smem);
+    mo_build_w_kernel<false><<<blocks, 512, smem, s>>>(q, er0, ec0, er1, ec1, tables, nu, area, n, w, part,
+                                                       JaggedSegs());
+  }
   LAUNCH_OK();
   return blocks;
 }

@@ -168,6 +168,14 @@ inline RingSwitchOut ring_switch_claim(Transcript& T, const std::vector<F128>& s
 }
 
 // ---------------------------------------------------------------- aligned jagged layout
+// General jagged layout (jagged.rs:87-140): column y of 2^k occupies dense indices
+// [pfx[y], pfx[y+1]); rows n, dense variables m.
+struct JaggedLayout {
+  uint32_t n = 0, k = 0, m = 0;
+  std::vector<uint64_t> pfx;
+  uint64_t area() const { return pfx.empty() ? 0 : pfx.back(); }
+};
+
 struct AlignedJagged {
   uint32_t n = 0;       // row variables (nu)
   uint32_t k = 0;       // column variables (col_log)
@@ -581,6 +589,184 @@ inline MultipointTwistedProof prove_multipoint(Transcript& T, const AlignedJagge
   for (int j = 0; j < 128; ++j) g_at += gj[j];
   std::vector<AssistStatement> sts;
   for (size_t i = 0; i < R; ++i) sts.push_back(aligned_statement(J, claims[i].z_row, claims[i].z_col, gpow[128 * i] * g_at));
+  pf.anchor = prove_anchor_assist(T, sts, s, m, anchor_round_bits);
+  return pf;
+}
+
+// Runs of equal boundary pairs (t_y, t_{y+1}) of a general layout, each with its summed
+// column weight coeff * eq(z_col, y) (jagged.rs:564-620; grouping identical summands
+// does not change any transcript value).
+inline AssistStatement jagged_statement(const JaggedLayout& L, const std::vector<F128>& z_row,
+                                        const std::vector<F128>& z_col, F128 coeff) {
+  AssistStatement a;
+  a.z_row = z_row;
+  auto eqc = build_eq(z_col);
+  for (size_t y = 0; y + 1 < L.pfx.size(); ++y) {
+    std::pair<uint64_t, uint64_t> b{L.pfx[y], L.pfx[y + 1]};
+    F128 w = eqc[y] * coeff;
+    if (!a.t.empty() && a.t.back() == b) a.w.back() += w;
+    else { a.w.push_back(w); a.t.push_back(b); }
+  }
+  return a;
+}
+
+// sum over runs of w * g_hat(z_row, point, t_c, t_next): the jagged weight's multilinear
+// extension at `point` by the branching-program DP (jagged.rs:2547-2580, assist_g_values).
+inline F128 jagged_weight_eval(const AssistStatement& a, const std::vector<F128>& point, uint32_t m) {
+  const int L = (int)m + 1;
+  auto pbit = [](const std::vector<F128>& z, int l) { return l < (int)z.size() ? z[l] : F128(); };
+  std::vector<std::array<std::array<std::array<F128, 4>, 4>, 4>> Mc(L);
+  for (int l = 0; l < L; ++l) {
+    auto e = build_eq({pbit(a.z_row, l), pbit(point, l)});
+    F128 eq4[4] = {e[0], e[1], e[2], e[3]};
+    for (int cd = 0; cd < 4; ++cd) {
+      F128 M[4][4];
+      bp_layer_matrix(eq4, cd & 1, (cd >> 1) & 1, M);
+      for (int st = 0; st < 4; ++st)
+        for (int o = 0; o < 4; ++o) Mc[l][cd][st][o] = M[st][o];
+    }
+  }
+  F128 acc;
+  for (size_t r = 0; r < a.w.size(); ++r) {
+    std::array<F128, 4> v{};
+    v[BP_SUCCESS] = F128::one();
+    for (int l = L - 1; l >= 0; --l) {
+      const int c = (int)((a.t[r].first >> l) & 1), d = (int)((a.t[r].second >> l) & 1);
+      const auto& M = Mc[l][c + 2 * d];
+      std::array<F128, 4> out{};
+      for (int st = 0; st < 4; ++st) {
+        F128 x;
+        for (int o = 0; o < 4; ++o) x += M[st][o] * v[o];
+        out[st] = x;
+      }
+      v = out;
+    }
+    acc += a.w[r] * v[BP_INITIAL];
+  }
+  return acc;
+}
+
+// The multipoint twisted evaluation over a general jagged layout (jagged.rs:2884-3380,
+// the materialised path): dual values A_ij = sum_d a_i(d) eq(rho^(2^-j), d) from the
+// branching-program DP, then the m-round two-product sumcheck of sum_d abar(d) g(d) with
+// abar = sum_i gamma^(128 i) a_i and g = sum_j gamma^j eq(rho^(2^-j), .) both
+// materialised (g(d) is the F2-linear map x -> sum_j gamma^j x^(2^-j) of eq(rho, d)),
+// then the untwisted anchor. The same field values as prove_multipoint on an aligned layout.
+inline MultipointTwistedProof prove_multipoint_jagged(Transcript& T, const JaggedLayout& L,
+                                                      const std::vector<RsClaimPoint>& claims,
+                                                      const std::vector<F128>& rho, uint32_t round_bits,
+                                                      uint32_t anchor_round_bits) {
+  const uint32_t n = L.n, m = L.m;
+  const size_t R = claims.size();
+  auto rp = rho_inverse_powers(rho);
+  MultipointTwistedProof pf;
+  std::vector<AssistStatement> unit(R);
+  for (size_t i = 0; i < R; ++i) unit[i] = jagged_statement(L, claims[i].z_row, claims[i].z_col, F128::one());
+  pf.values.assign(R, std::vector<F128>(128));
+  parallel_for(R * 128, [&](size_t ij) {
+    const size_t i = ij / 128, j = ij % 128;
+    pf.values[i][j] = jagged_weight_eval(unit[i], rp[j], m);
+  });
+  T.observe_label("flock-multipoint-twisted-v1");
+  for (auto& vs : pf.values) for (auto& v : vs) T.observe_f128(v);
+  uint32_t gamma_bits = std::max<uint32_t>(1, grinding_bits_for_degree(128 * R - 1));
+  auto gp = T.grind_pow_and_sample_f128(gamma_bits);
+  pf.gamma_grinding_nonce = gp.first;
+  F128 gamma = gp.second;
+  std::vector<F128> gpow(128 * R);
+  F128 p = F128::one();
+  for (auto& g : gpow) { g = p; p = p * gamma; }
+  // ---- materialised abar (zero past the area) and g
+  const size_t N = size_t(1) << m;
+  std::vector<F128> abar(N), g(N);
+  {
+    std::vector<std::vector<F128>> er(R), ec(R);
+    for (size_t i = 0; i < R; ++i) { er[i] = build_eq(claims[i].z_row); ec[i] = build_eq(claims[i].z_col); }
+    const size_t ncol = L.pfx.size() - 1;
+    parallel_for(ncol, [&](size_t y) {
+      for (uint64_t d = L.pfx[y]; d < L.pfx[y + 1]; ++d) {
+        F128 acc;
+        for (size_t i = 0; i < R; ++i) acc += gpow[128 * i] * er[i][d - L.pfx[y]] * ec[i][y];
+        abar[d] = acc;
+      }
+    });
+    // images of the basis under x -> sum_j gamma^j x^(2^(128-j)), byte tables
+    std::vector<F128> img(128);
+    parallel_for(128, [&](size_t b) {
+      std::vector<F128> sq(128);
+      F128 x = bit_basis((int)b);
+      for (int e = 0; e < 128; ++e) { sq[e] = x; x = x * x; }
+      F128 acc;
+      for (int j = 0; j < 128; ++j) acc += gpow[j] * sq[(128 - j) % 128];
+      img[b] = acc;
+    });
+    std::vector<F128> tab(16 * 256);
+    for (int kb = 0; kb < 16; ++kb)
+      for (int v = 0; v < 256; ++v) {
+        F128 acc;
+        for (int i = 0; i < 8; ++i) if ((v >> i) & 1) acc += img[8 * kb + i];
+        tab[kb * 256 + v] = acc;
+      }
+    auto e = build_eq(rho);
+    parallel_for((N + 4095) / 4096, [&](size_t c) {
+      for (size_t d = c * 4096; d < std::min(N, (c + 1) * 4096); ++d) g[d] = fold_one_slot(e[d], tab.data());
+    });
+  }
+  auto message = [&](size_t len, F128& g1, F128& gi) {
+    const size_t half = len / 2, nch = std::max<size_t>(1, std::min<size_t>(64, half / 1024));
+    std::vector<F128> p1(nch), pi(nch);
+    parallel_for(nch, [&](size_t c) {
+      F128 a1, ai;
+      for (size_t i = half * c / nch; i < half * (c + 1) / nch; ++i) {
+        a1 += abar[2 * i + 1] * g[2 * i + 1];
+        ai += (abar[2 * i] + abar[2 * i + 1]) * (g[2 * i] + g[2 * i + 1]);
+      }
+      p1[c] = a1;
+      pi[c] = ai;
+    });
+    g1 = F128(); gi = F128();
+    for (size_t c = 0; c < nch; ++c) { g1 += p1[c]; gi += pi[c]; }
+  };
+  auto fold = [&](size_t len, F128 r) {
+    const size_t half = len / 2;
+    std::vector<F128> na(half), ng(half);
+    parallel_for((half + 4095) / 4096, [&](size_t c) {
+      for (size_t i = c * 4096; i < std::min(half, (c + 1) * 4096); ++i) {
+        na[i] = abar[2 * i] + r * (abar[2 * i + 1] + abar[2 * i]);
+        ng[i] = g[2 * i] + r * (g[2 * i + 1] + g[2 * i]);
+      }
+    });
+    abar.swap(na);
+    g.swap(ng);
+  };
+  std::vector<F128> s;
+  F128 g1, gi;
+  size_t len = N;
+  message(len, g1, gi);
+  for (uint32_t t = 0; t < m; ++t) {
+    T.observe_f128(g1); T.observe_f128(gi);
+    F128 r;
+    if (round_bits) { auto pr = T.grind_pow_and_sample_f128(round_bits); pf.round_grinding_nonces.push_back(pr.first); r = pr.second; }
+    else r = T.sample_f128();
+    pf.rounds.push_back({g1, gi});
+    s.push_back(r);
+    if (t + 1 == m) break;
+    fold(len, r);
+    len /= 2;
+    message(len, g1, gi);
+  }
+  (void)n;
+  // ---- anchor at the endpoint rho'' = s
+  F128 g_at;
+  std::vector<F128> gj(128);
+  parallel_for(128, [&](size_t j) {
+    F128 prod = gpow[j];
+    for (uint32_t t = 0; t < m; ++t) prod = prod * (s[t] * rp[j][t] + (F128::one() + s[t]) * (F128::one() + rp[j][t]));
+    gj[j] = prod;
+  });
+  for (int j = 0; j < 128; ++j) g_at += gj[j];
+  std::vector<AssistStatement> sts;
+  for (size_t i = 0; i < R; ++i) sts.push_back(jagged_statement(L, claims[i].z_row, claims[i].z_col, gpow[128 * i] * g_at));
   pf.anchor = prove_anchor_assist(T, sts, s, m, anchor_round_bits);
   return pf;
 }

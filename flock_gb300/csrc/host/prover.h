@@ -27,9 +27,11 @@ namespace flock {
 class ProverBackend {
  public:
   virtual ~ProverBackend() = default;
-  // Witness of n_blocks = 2^nu instances, records of input_record_bytes(hash).
-  virtual void witness(const uint8_t* inputs) = 0;
-  // L0 commit of the lane-major stack q = z: replicate-fill, NTT from layer 1, Merkle.
+  // Witness of every slot: slot_inputs[t] holds slots[t].count records of
+  // input_record_bytes(slots[t].hash); rows [count, 2^nu) of a slot are zero.
+  virtual void witness(const std::vector<const uint8_t*>& slot_inputs) = 0;
+  // L0 commit of the committed stack q (the height-n_t compaction of z; z itself under
+  // identity compaction): lane-major fill, NTT from layer 1, Merkle.
   virtual void commit_l0(uint32_t cap_depth, std::vector<Hash>& cap) = 0;
 
   // ---- zerocheck (r has m coordinates; all values in wire convention)
@@ -43,18 +45,27 @@ class ProverBackend {
   virtual void zc_final(F128 rho, F128& a_eval, F128& b_eval) = 0;
 
   // ---- lincheck
-  // eq_inner = skip_w (64) tensor eq(x_inner_rest); comb_a, comb_b = eq_inner^T (A_0, B_0).
+  // Per slot t: eq_inner_t = skip_w (64) tensor eq(x_inner_rest[.. k_log_t - 6]);
+  // comb_a_t, comb_b_t = eq_inner_t^T (A_0, B_0) of the slot's type.
   virtual void lc_comb(const std::vector<F128>& skip_w, const std::vector<F128>& x_inner_rest) = 0;
-  // z_vec[c] = sum_row eq(x_outer, row) * z(row, c), also kept as the captured copy.
+  // z_vec[c] = sum_row eq(x_outer, row) * z(row, c) over the union columns, also kept as
+  // the captured copy.
   virtual void lc_zvec(const std::vector<F128>& x_outer) = 0;
-  // comb = alpha * comb_a + comb_b, comb[pin] += beta; first product-sumcheck message.
-  virtual void lc_start(F128 alpha, F128 beta, uint32_t pin, F128& e1, F128& einf) = 0;
+  // The union comb: per slot t, comb[off_t + c] = w_t (alpha comb_a_t[c] + comb_b_t[c]),
+  // then comb[off_t + pin_t] += beta_t; first product-sumcheck message.
+  struct SlotComb {
+    F128 weight, beta;
+    uint64_t offset = 0;  // off_t = prefix_t << k_log_t
+    uint32_t pin = 0;
+  };
+  virtual void lc_start(F128 alpha, const std::vector<SlotComb>& slots, F128& e1, F128& einf) = 0;
   // Bind the top variable of comb and z_vec at r; next message unless `last`.
   virtual void lc_round(F128 r, bool last, F128& e1, F128& einf) = 0;
   virtual void lc_partial(std::vector<F128>& z_partial64) = 0;
-  // (<w_col, comb_a>, <w_col, comb_b>) with w_col = eq(rest_point) tensor z_partial.
+  // Per slot t: (<w_col_t, comb_a_t>, <w_col_t, comb_b_t>) with
+  // w_col_t = eq(rest_point[.. k_log_t - 6]) tensor z_partial.
   virtual void lc_matrix_evals(const std::vector<F128>& rest_point, const std::vector<F128>& z_partial64,
-                               F128& ea, F128& eb) = 0;
+                               std::vector<Pair128>& evals) = 0;
   // s_hat_v[b] = sum_k eq(tail, k) * z_vec_captured[b + 128 k].
   virtual void lc_s_hat_v(const std::vector<F128>& tail, std::vector<F128>& out128) = 0;
 
@@ -63,8 +74,10 @@ class ProverBackend {
     std::vector<F128> z_row, z_col;
     std::vector<F128> table;  // 16 x 256, gamma baked
   };
-  // W[d] = sum_i fold_one_slot(eq(z_row_i)[row] * eq(z_col_i)[col], table_i) for d < area,
-  // 0 beyond; returns the round-0 prime (u0, u2) of sum_d q[d] W[d].
+  // W[d] = sum_i fold_one_slot(eq(z_row_i)[row(d)] * eq(z_col_i)[col(d)], table_i) for
+  // d < area, 0 beyond, with (row, col) the jagged unrank of d (the statement's column
+  // prefix sums; col = d >> nu, row = d mod 2^nu under identity compaction); returns the
+  // round-0 prime (u0, u2) of sum_d q[d] W[d].
   virtual void mo_build_w(const std::vector<WeightClaim>& claims, uint32_t nu, uint64_t area, F128& u0, F128& u2) = 0;
   // Fold q and W at r (low bit); next (g1, ginf) unless `last`.
   virtual void mo_round(F128 r, bool last, F128& g1, F128& ginf) = 0;
@@ -170,7 +183,11 @@ struct ProveResult {
   ProveTimings t;
 };
 
-inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_t* inputs,
+// prove_fast_ligerito_union over the statement's registry and declared counts
+// (prover.rs:587-620, 831-1468); slot_inputs[t] holds the records of slot t (slot order).
+// A single-hash statement is the one-slot union: Blake3Setup / Sha256HybridSetup /
+// KeccakSetup ::prove_fast.
+inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const std::vector<const uint8_t*>& slot_inputs,
                               const uint8_t* domain, size_t domain_len) {
   ProveResult R;
   double t0 = now_ms();
@@ -178,17 +195,20 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
   T.set_pow_search(B.pow_search());
   const uint32_t m = S.m, nu = S.nu, k_log = S.k_log;
   const uint32_t n_mlv = m - 6;
+  if (slot_inputs.size() != S.slots.size()) throw std::runtime_error("one input pointer per registry slot");
 
-  // ---- witness + commit + bind
-  B.witness(inputs);
+  // ---- witness + commit + bind (union.rs:619-628: label, registry digest, the counts
+  // vector as one u64 LE per slot, the cap)
+  B.witness(slot_inputs);
   double t1 = now_ms();
   B.commit_l0(S.lig.sched[0].cap_depth(), R.cap);
   double t2 = now_ms();
   T.observe_label("flock-mixed-v1");
   T.observe_bytes(S.registry_digest.data(), 32);
-  uint8_t counts[8];
-  for (int i = 0; i < 8; ++i) counts[i] = (uint8_t)((uint64_t)S.n_blocks >> (8 * i));
-  T.observe_bytes(counts, 8);
+  std::vector<uint8_t> counts;
+  for (const SlotInfo& t : S.slots)
+    for (int i = 0; i < 8; ++i) counts.push_back((uint8_t)(t.count >> (8 * i)));
+  T.observe_bytes(counts.data(), counts.size());
   {
     std::vector<uint8_t> capb;
     for (auto& h : R.cap) capb.insert(capb.end(), h.begin(), h.end());
@@ -255,15 +275,29 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
   lc.grinding_nonces.push_back(pa.first);
   F128 alpha = pa.second;
   B.lc_comb(skip_w, x_inner_rest);
-  auto pb = T.grind_pow_and_sample_f128(1);
-  lc.grinding_nonces.push_back(pb.first);
-  F128 beta = pb.second;
+  // one const-pin challenge per slot, in slot order; a slot's comb is scaled by the eq
+  // weight of its prefix over the remaining column coordinates (lincheck/union.rs:270-330)
+  std::vector<ProverBackend::SlotComb> slot_comb;
+  for (const SlotInfo& t : S.slots) {
+    auto pb = T.grind_pow_and_sample_f128(1);
+    lc.grinding_nonces.push_back(pb.first);
+    ProverBackend::SlotComb c;
+    c.beta = pb.second;
+    c.offset = t.prefix << t.k_log;
+    c.pin = t.const_pin;
+    c.weight = F128::one();
+    for (size_t j = t.k_log - 6; j < x_inner_rest.size(); ++j) {
+      const uint64_t bit = (t.prefix >> (j - (t.k_log - 6))) & 1;
+      c.weight = c.weight * (bit ? x_inner_rest[j] : F128::one() + x_inner_rest[j]);
+    }
+    slot_comb.push_back(c);
+  }
   B.lc_zvec(x_outer);
   const uint32_t inner_rest_len = k_log - 6;
   std::vector<F128> r_rounds;
   {
     F128 e1, ei;
-    B.lc_start(alpha, beta, S.const_pin, e1, ei);
+    B.lc_start(alpha, slot_comb, e1, ei);
     for (uint32_t t = 0; t < inner_rest_len; ++t) {
       T.observe_f128(e1); T.observe_f128(ei);
       auto pr = T.grind_pow_and_sample_f128(2);
@@ -284,11 +318,7 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
     for (int i = 0; i < 64; ++i) w_ab += lw[i] * lc.z_partial[i];
   }
   std::vector<F128> r_inner_rest(r_rounds.rbegin(), r_rounds.rend());
-  {
-    F128 ea, eb;
-    B.lc_matrix_evals(r_inner_rest, lc.z_partial, ea, eb);
-    lc.matrix_evals.push_back({ea, eb});
-  }
+  B.lc_matrix_evals(r_inner_rest, lc.z_partial, lc.matrix_evals);
   std::vector<F128> s_hat_v_ab;
   B.lc_s_hat_v(std::vector<F128>(r_inner_rest.begin() + 1, r_inner_rest.end()), s_hat_v_ab);
   R.claims.ab_value = w_ab;
@@ -319,7 +349,12 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
   F128 target = g_ab * rs_ab.sumcheck_claim + g_c * rs_c.sumcheck_claim;
   mo.ring_switches = {rs_ab.proof, rs_c.proof};
   const uint32_t dense_log = S.geo.dense_m - 7;
-  AlignedJagged J{nu, S.geo.col_log, dense_log, S.geo.used_cols};
+  // the jagged layout of the committed stack: one slot at full height with its used
+  // columns first is the aligned shape with closed-form assist sums; any other layout
+  // takes the general (materialised) path
+  const bool aligned = S.slots.size() == 1 && S.identity;
+  AlignedJagged J{nu, S.geo.col_log, dense_log, aligned ? S.slots[0].used_cols : 0};
+  JaggedLayout JL{nu, S.geo.col_log, dense_log, S.col_prefix};
   std::vector<ProverBackend::WeightClaim> wc(2);
   wc[0].z_row.assign(x_ab.begin() + 1, x_ab.begin() + 1 + nu);
   wc[0].z_col.assign(x_ab.begin() + 1 + nu, x_ab.end());
@@ -330,7 +365,7 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
   std::vector<F128> rho;
   {
     F128 u0, u2;
-    B.mo_build_w(wc, nu, J.area(), u0, u2);
+    B.mo_build_w(wc, nu, S.area(), u0, u2);
     F128 g1 = target + u0, gi = u2;
     for (uint32_t rd = 0; rd < dense_log; ++rd) {
       T.observe_f128(g1); T.observe_f128(gi);
@@ -355,7 +390,7 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
   double assist_ms = 0;
   std::thread assist([&] {
     double a0 = now_ms();
-    mo.frobenius = prove_multipoint(ch_a, J, fcl, rho, 2, 2);
+    mo.frobenius = aligned ? prove_multipoint(ch_a, J, fcl, rho, 2, 2) : prove_multipoint_jagged(ch_a, JL, fcl, rho, 2, 2);
     assist_ms = now_ms() - a0;
   });
 
@@ -521,6 +556,11 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_
   R.t.witness = t1 - t0; R.t.commit = t2 - t1; R.t.zerocheck = t3 - t2; R.t.lincheck = t4 - t3;
   R.t.open = t5 - t4; R.t.total = t5 - t0;
   return R;
+}
+
+inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const uint8_t* inputs, const uint8_t* domain,
+                              size_t domain_len) {
+  return prove_fast(S, B, std::vector<const uint8_t*>{inputs}, domain, domain_len);
 }
 
 // SHA-256 over bincode(proof) || cap || claim values (the byte-identity digest of

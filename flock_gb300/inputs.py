@@ -66,5 +66,30 @@ def keccak_batch(n: int, seed: int) -> np.ndarray:
     return out
 
 
+def _blake3_from_draws(d: np.ndarray, flags: int) -> np.ndarray:
+    n = d.shape[0]
+    out = np.zeros(n, dtype=BLAKE3_DTYPE)
+    out["cv"] = d[:, :8]
+    out["m"] = d[:, 8:24]
+    out["counter"] = (d[:, 24].astype(np.uint64) << np.uint64(32)) | d[:, 25].astype(np.uint64)
+    out["block_len"] = 64
+    out["flags"] = flags
+    return out
+
+
+def mixed_fixture(n_sha2: int, n_blake3: int, seed: int):
+    """One SplitMix64 stream from `seed`: n_sha2 SHA-256 records (h[8], w[16]) first, then
+    n_blake3 BLAKE3 records (cv[8], m[16], counter = (hi << 32) | lo, block_len 64,
+    flags 11) — the mixed-union fixture generator of union_m6_fixtures.rs:226-268."""
+    d = splitmix_u32(seed, 24 * n_sha2 + 26 * n_blake3)
+    sha = np.zeros(n_sha2, dtype=SHA256_DTYPE)
+    if n_sha2:
+        s = d[:24 * n_sha2].reshape(n_sha2, 24)
+        sha["h"] = s[:, :8]
+        sha["w"] = s[:, 8:]
+    b3 = _blake3_from_draws(d[24 * n_sha2:].reshape(n_blake3, 26), 11) if n_blake3 else np.zeros(0, dtype=BLAKE3_DTYPE)
+    return sha, b3
+
+
 def batch(kind: int, n: int, seed: int) -> np.ndarray:
     return (blake3_batch, sha256_batch, keccak_batch)[kind](n, seed)

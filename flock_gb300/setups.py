@@ -169,3 +169,77 @@ class KeccakSetup(_Setup):
 
 
 SETUPS = {_native.BLAKE3: Blake3Setup, _native.SHA256: Sha256HybridSetup, _native.KECCAK: KeccakSetup}
+
+
+class UnionSetup:
+    """Mixed multi-type union proofs: ``UnionSetup(types, nu).prove(counts, records, domain)``
+    mirrors ``prover::prove_fast_ligerito_union(&UnionInstance::new(&Registry::new(types,
+    nu), counts), ...)`` (crates/flock-prover/src/prover.rs:587-620). ``slot_kinds`` is the
+    registry's slot order (k_log descending); ``counts`` and ``records`` follow it, each
+    count at most ``2**nu`` (zero allowed)."""
+
+    def __init__(self, types, nu: int):
+        lib = _native.load()
+        n = len(types)
+        kinds = (ctypes.c_int * n)(*types)
+        order = (ctypes.c_int * n)()
+        h = ctypes.c_void_p()
+        _native.check(lib.flock_gb300_union_setup_new(kinds, n, nu, ctypes.byref(h), order))
+        self._h, self._lib, self.nu = h, lib, nu
+        self.slot_kinds = list(order)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.flock_gb300_union_setup_free(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _counts(self, counts):
+        if len(counts) != len(self.slot_kinds):
+            raise ValueError("one count per registry slot")
+        return (ctypes.c_uint64 * len(counts))(*[int(c) for c in counts])
+
+    def prove_bytes(self, counts, records, domain: bytes) -> bytes:
+        """The union proof bundle (the prove_fast bundle format)."""
+        if self._h is None:
+            raise RuntimeError("setup is closed")
+        arrs = []
+        for kind, c, r in zip(self.slot_kinds, counts, records):
+            a = np.ascontiguousarray(r)
+            if a.dtype != SETUPS[kind].DTYPE or a.shape[0] != int(c):
+                raise TypeError(f"slot records must be {int(c)} records of dtype {SETUPS[kind].DTYPE}")
+            arrs.append(a)
+        ptrs = (ctypes.c_void_p * len(arrs))(*[a.ctypes.data if a.size else None for a in arrs])
+        out = ctypes.POINTER(ctypes.c_uint8)()
+        out_len = ctypes.c_size_t()
+        _native.check(self._lib.flock_gb300_prove_union(self._h, self._counts(counts), ptrs, domain, len(domain),
+                                                        ctypes.byref(out), ctypes.byref(out_len)))
+        try:
+            return ctypes.string_at(out, out_len.value)
+        finally:
+            self._lib.flock_gb300_free(out)
+
+    def prove(self, counts, records, domain: bytes) -> ProofBundle:
+        return ProofBundle.parse(self.prove_bytes(counts, records, domain))
+
+    def mixed_proof_io(self, counts, bundle: bytes) -> bytes:
+        """MixedProofBundleLigerito::to_bytes of a bundle of this registry (built-in tiers)."""
+        out = ctypes.POINTER(ctypes.c_uint8)()
+        out_len = ctypes.c_size_t()
+        _native.check(self._lib.flock_gb300_mixed_proof_io(self._h, self._counts(counts), bundle, len(bundle),
+                                                           ctypes.byref(out), ctypes.byref(out_len)))
+        try:
+            return ctypes.string_at(out, out_len.value)
+        finally:
+            self._lib.flock_gb300_free(out)

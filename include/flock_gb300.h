@@ -180,6 +180,35 @@ void flock_gb300_server_free(flock_gb300_server* server);
 int flock_gb300_proof_io(int hash_kind, uint64_t n_blocks, const uint8_t* bundle, size_t bundle_len, uint8_t** out,
                          size_t* out_len);
 
+/* ---- mixed multi-type union proofs: several hash types with arbitrary declared counts in
+ * one proof (prover::prove_fast_ligerito_union, crates/flock-prover/src/prover.rs:587-620,
+ * over UnionInstance::new(&Registry::new(types, nu), counts), crates/flock-core/src/union.rs,
+ * schedule.rs:337-690). */
+typedef struct flock_gb300_union_setup flock_gb300_union_setup;
+/* A registry of n_types distinct hash kinds at uniform row capacity 2^nu (3 <= nu <= 24).
+ * Registry::new sorts the types into slot order (k_log descending, stable); that order is
+ * written to slot_kinds[0 .. n_types) and every per-slot argument below follows it. The
+ * registry digest is computed here. */
+int flock_gb300_union_setup_new(const int* hash_kinds, size_t n_types, uint32_t nu, flock_gb300_union_setup** out,
+                                int* slot_kinds);
+void flock_gb300_union_setup_free(flock_gb300_union_setup* setup);
+/* prove_fast_ligerito_union(&UnionInstance::new(&registry, counts), pcs_params, slots,
+ * &mut FsChallenger::new(domain)) on the GPU. counts[t] <= 2^nu declared invocations of slot
+ * t (zero allowed); inputs[t] points at counts[t] host records of slot t's hash (the records
+ * of flock_gb300_prove_fast); rows past a count are the zero dummy rows of the reference's
+ * generate_witness_batch_major_partial drivers. *out receives a bundle in the format of
+ * flock_gb300_prove_fast (the proof's lincheck carries one matrix-evaluation pair per slot).
+ * Provers are cached per counts vector on the setup (device buffers sized for 2^(M-7)
+ * words). */
+int flock_gb300_prove_union(flock_gb300_union_setup* setup, const uint64_t* counts, const void* const* inputs,
+                            const uint8_t* domain, size_t domain_len, uint8_t** out, size_t* out_len);
+/* MixedProofBundleLigerito::to_bytes (crates/flock-prover/src/proof_io.rs:254-282) of a
+ * union bundle: "FLOCK" | 21 | flavor 4 | registry id (u8) | counts (Vec<u64>) | Commitment |
+ * proof. Only the built-in tiers have a registry id (mixed.rs:55-97: BLAKE3 + SHA-256 at nu 7
+ * or 10); other registries get FLOCK_GB300_EINVAL. Host-only. */
+int flock_gb300_mixed_proof_io(const flock_gb300_union_setup* setup, const uint64_t* counts, const uint8_t* bundle,
+                               size_t bundle_len, uint8_t** out, size_t* out_len);
+
 /* Measurement helper (no reference counterpart): products per second of the device
  * GF(2^128) multiply that the NTT and sumcheck kernels use, from `iters` chained products
  * per thread on a full grid (about 256 gives a ~10 ms launch). The integer-pipe peak that

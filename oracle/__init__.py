@@ -34,6 +34,14 @@ def load() -> ctypes.CDLL:
         lib.oracle_verify.argtypes = [c.c_int, c.c_uint64, c.c_char_p, c.c_size_t, c.c_char_p, c.c_size_t,
                                       c.c_char_p, c.c_size_t]
         lib.oracle_verify.restype = c.c_int
+        lib.oracle_prove_union.argtypes = [c.POINTER(c.c_int), c.c_size_t, c.c_uint32, c.POINTER(c.c_uint64),
+                                           c.POINTER(c.c_void_p), c.c_char_p, c.c_size_t,
+                                           c.POINTER(c.POINTER(c.c_uint8)), c.POINTER(c.c_size_t)]
+        lib.oracle_prove_union.restype = c.c_int
+        lib.oracle_mixed_proof_io.argtypes = [c.POINTER(c.c_int), c.c_size_t, c.c_uint32, c.POINTER(c.c_uint64),
+                                              c.c_char_p, c.c_size_t, c.POINTER(c.POINTER(c.c_uint8)),
+                                              c.POINTER(c.c_size_t)]
+        lib.oracle_mixed_proof_io.restype = c.c_int
         _lib = lib
     return _lib
 
@@ -79,3 +87,41 @@ def verify(kind: int, n_blocks: int, bundle: bytes, domain: bytes) -> tuple:
     if rc == 2:
         raise RuntimeError(reason.value.decode())
     return rc == 0, reason.value.decode()
+
+
+def _union_args(kinds, counts):
+    n = len(kinds)
+    return (ctypes.c_int * n)(*kinds), n, (ctypes.c_uint64 * n)(*counts)
+
+
+def prove_union_bytes(kinds, nu: int, counts, records, domain: bytes) -> bytes:
+    """Oracle prove_fast_ligerito_union of a registry given in slot order (k_log
+    descending), declared counts and per-slot record arrays; returns the bundle."""
+    import numpy as np
+
+    lib = load()
+    k, n, c = _union_args(kinds, counts)
+    arrs = [np.ascontiguousarray(r) for r in records]
+    ptrs = (ctypes.c_void_p * n)(*[a.ctypes.data if a.size else 0 for a in arrs])
+    out = ctypes.POINTER(ctypes.c_uint8)()
+    ln = ctypes.c_size_t()
+    if lib.oracle_prove_union(k, n, nu, c, ptrs, domain, len(domain), ctypes.byref(out), ctypes.byref(ln)) != 0:
+        raise RuntimeError(lib.oracle_last_error().decode())
+    try:
+        return ctypes.string_at(out, ln.value)
+    finally:
+        lib.oracle_free(out)
+
+
+def mixed_proof_io(kinds, nu: int, counts, bundle: bytes) -> bytes:
+    """MixedProofBundleLigerito::to_bytes of a union bundle."""
+    lib = load()
+    k, n, c = _union_args(kinds, counts)
+    out = ctypes.POINTER(ctypes.c_uint8)()
+    ln = ctypes.c_size_t()
+    if lib.oracle_mixed_proof_io(k, n, nu, c, bundle, len(bundle), ctypes.byref(out), ctypes.byref(ln)) != 0:
+        raise RuntimeError(lib.oracle_last_error().decode())
+    try:
+        return ctypes.string_at(out, ln.value)
+    finally:
+        lib.oracle_free(out)

@@ -262,28 +262,32 @@ inline std::vector<F256> fold_ext(const std::vector<F256>& v, F256 r, size_t d) 
   return o;
 }
 
-// Column folds of the lincheck matrices by the row weight eq_inner = skip_w (x) eq(xir)
-// (lincheck.rs:238-281): comb_a = eq_inner^T A_0, comb_b = eq_inner^T B_0 (CSC for
-// BLAKE3 / SHA-256, the walker for Keccak).
-inline void lincheck_combs(const Statement& S, const std::vector<F128>& skip_w, const std::vector<F128>& xir,
+// Column folds of one slot's matrices by the row weight eq_inner = skip_w (x) eq(xir)
+// (lincheck.rs:238-281, lincheck/union.rs:255-275): comb_a = eq_inner^T A_0,
+// comb_b = eq_inner^T B_0 (CSC for BLAKE3 / SHA-256; Keccak-f from the forward rows).
+inline void lincheck_combs(const SlotInfo& T, const std::vector<F128>& skip_w, const std::vector<F128>& xir,
                            std::vector<F128>& comb_a, std::vector<F128>& comb_b) {
-  const uint32_t K = 1u << S.k_log;
+  const uint32_t K = 1u << T.k_log;
   auto er = par_build_eq(xir);
   std::vector<F128> eqi(K);
   par_chunks(K, [&](size_t b, size_t e) {
     for (size_t i = b; i < e; ++i) eqi[i] = skip_w[i & 63] * er[i >> 6];
   });
-  if (S.hash == HASH_KECCAK) {
+  if (T.hash == HASH_KECCAK) {
     keccak_columns_forward(eqi.data(), comb_a, comb_b);
     return;
   }
   comb_a.assign(K, F128()); comb_b.assign(K, F128());
   par_chunks(K, [&](size_t cb, size_t ce) {
     for (size_t c = cb; c < ce; ++c) {
-      for (uint32_t p = S.csc_a->col_ptr[c]; p < S.csc_a->col_ptr[c + 1]; ++p) comb_a[c] += eqi[S.csc_a->rows_flat[p]];
-      for (uint32_t p = S.csc_b->col_ptr[c]; p < S.csc_b->col_ptr[c + 1]; ++p) comb_b[c] += eqi[S.csc_b->rows_flat[p]];
+      for (uint32_t p = T.csc_a->col_ptr[c]; p < T.csc_a->col_ptr[c + 1]; ++p) comb_a[c] += eqi[T.csc_a->rows_flat[p]];
+      for (uint32_t p = T.csc_b->col_ptr[c]; p < T.csc_b->col_ptr[c + 1]; ++p) comb_b[c] += eqi[T.csc_b->rows_flat[p]];
     }
   });
+}
+// Slot t's share of x_inner_rest: its own k_log_t - 6 column coordinates.
+inline std::vector<F128> slot_inner(const SlotInfo& T, const std::vector<F128>& x_inner_rest) {
+  return std::vector<F128>(x_inner_rest.begin(), x_inner_rest.begin() + (T.k_log - 6));
 }
 
 class CpuBackend : public ProverBackend {
@@ -291,9 +295,10 @@ class CpuBackend : public ProverBackend {
   explicit CpuBackend(const Statement& s) : S(s) {}
 
   const Statement& S;
-  std::vector<F128> z, a, b;        // 2^(m-7) words, batch-major
-  std::vector<uint8_t> stripe;      // 2^(m-3) bytes
+  std::vector<F128> z, a, b;        // 2^(m-7) words, batch-major union buffers
+  std::vector<F128> q;              // the committed stack (the compaction of z)
   std::vector<F128> cw0;            // L0 codeword, SoA (pos * lanes + lane)
+  std::vector<std::vector<F128>> slot_ca, slot_cb;  // per-slot column folds
   std::vector<Hash> tree0;
   std::vector<F128> amlv, bmlv;
   std::vector<F128> comb_a, comb_b, comb, zv, zv_cap;
@@ -304,46 +309,64 @@ class CpuBackend : public ProverBackend {
 
   size_t words() const { return size_t(1) << (S.m - 7); }
 
-  void witness(const uint8_t* inputs) override {
-    const uint32_t K = 1u << S.k_log, nu = S.nu;
-    const size_t nb = S.n_blocks, rec = input_record_bytes(S.hash);
+  // Union witness (union.rs:674-760): slot t's block is the aligned word range starting
+  // at its offset / 128; instance o of the slot writes word ((c << nu) + o) of that block;
+  // rows [count, 2^nu), unused columns and gaps stay zero.
+  void witness(const std::vector<const uint8_t*>& slot_inputs) override {
+    const uint32_t nu = S.nu;
     z.assign(words(), F128()); a.assign(words(), F128()); b.assign(words(), F128());
-    stripe.assign(size_t(1) << (S.m - 3), 0);
-    // groups of 8 instances share stripe bytes: chunks are whole groups
-    par_chunks((nb + 7) / 8, [&](size_t gb, size_t ge) {
-    std::vector<uint64_t> bz(K / 64), ba(K / 64), bb(K / 64);
-    for (size_t o = 8 * gb; o < std::min(nb, 8 * ge); ++o) {
-      std::fill(bz.begin(), bz.end(), 0); std::fill(ba.begin(), ba.end(), 0); std::fill(bb.begin(), bb.end(), 0);
-      const uint8_t* in = inputs + o * rec;
-      if (S.hash == HASH_BLAKE3) {
-        b3r1cs::Compression c; memcpy(&c, in, sizeof(c));
-        b3r1cs::witness_block(c, bz.data(), ba.data(), bb.data());
-      } else if (S.hash == HASH_SHA256) {
-        s2r1cs::Compression c; memcpy(&c, in, sizeof(c));
-        s2r1cs::witness_block(c, bz.data(), ba.data(), bb.data());
-      } else {
-        uint64_t w[25]; memcpy(w, in, sizeof(w));
-        kr1cs::witness_block(w, bz.data(), ba.data(), bb.data());
-      }
-      for (uint32_t c = 0; c < K / 128; ++c) {
-        size_t wi = (size_t(c) << nu) + o;
-        z[wi] = F128(bz[2 * c], bz[2 * c + 1]);
-        a[wi] = F128(ba[2 * c], ba[2 * c + 1]);
-        b[wi] = F128(bb[2 * c], bb[2 * c + 1]);
-      }
-      size_t g = o / 8, lane = o % 8;
-      for (uint32_t bit = 0; bit < K; ++bit)
-        if ((bz[bit >> 6] >> (bit & 63)) & 1) stripe[g * K + bit] |= (uint8_t)(1u << lane);
+    for (size_t si = 0; si < S.slots.size(); ++si) {
+      const SlotInfo& T = S.slots[si];
+      const uint32_t K = 1u << T.k_log;
+      const size_t rec = input_record_bytes(T.hash), base = T.offset >> 7;
+      const uint8_t* inputs = slot_inputs[si];
+      par_chunks(T.count, [&](size_t ob, size_t oe) {
+        std::vector<uint64_t> bz(K / 64), ba(K / 64), bb(K / 64);
+        for (size_t o = ob; o < oe; ++o) {
+          std::fill(bz.begin(), bz.end(), 0); std::fill(ba.begin(), ba.end(), 0); std::fill(bb.begin(), bb.end(), 0);
+          const uint8_t* in = inputs + o * rec;
+          if (T.hash == HASH_BLAKE3) {
+            b3r1cs::Compression c; memcpy(&c, in, sizeof(c));
+            b3r1cs::witness_block(c, bz.data(), ba.data(), bb.data());
+          } else if (T.hash == HASH_SHA256) {
+            s2r1cs::Compression c; memcpy(&c, in, sizeof(c));
+            s2r1cs::witness_block(c, bz.data(), ba.data(), bb.data());
+          } else {
+            uint64_t w[25]; memcpy(w, in, sizeof(w));
+            kr1cs::witness_block(w, bz.data(), ba.data(), bb.data());
+          }
+          for (uint32_t c = 0; c < K / 128; ++c) {
+            size_t wi = base + (size_t(c) << nu) + o;
+            z[wi] = F128(bz[2 * c], bz[2 * c + 1]);
+            a[wi] = F128(ba[2 * c], ba[2 * c + 1]);
+            b[wi] = F128(bb[2 * c], bb[2 * c + 1]);
+          }
+        }
+      }, 4);
     }
-    }, 4);
+  }
+
+  // q = the declared n_t-row prefix of every used chunk-column, slot by slot, zero-padded
+  // to the committed length (union.rs:436-495, compact_witness).
+  void compact() {
+    if (S.identity) { q = z; return; }
+    q.assign(S.committed_words, F128());
+    const uint32_t nu = S.nu;
+    size_t cursor = 0;
+    for (const SlotInfo& T : S.slots) {
+      const size_t start = T.offset >> 7;
+      for (uint64_t c = 0; c < T.used_cols; ++c)
+        for (uint64_t r = 0; r < T.count; ++r) q[cursor++] = z[start + (c << nu) + r];
+    }
   }
 
   void commit_l0(uint32_t cap_depth, std::vector<Hash>& cap) override {
     const size_t t = S.lanes, D = size_t(1) << S.log_dim, npos = size_t(1) << S.k_code;
+    compact();
     cw0.assign(npos * t, F128());
     par_chunks(npos, [&](size_t pb, size_t pe) {
       for (size_t p = pb; p < pe; ++p)
-        for (size_t l = 0; l < t; ++l) cw0[p * t + l] = z[l * D + (p % D)];
+        for (size_t l = 0; l < t; ++l) cw0[p * t + l] = q[l * D + (p % D)];
     });
     Ntt128 ntt(S.k_code);
     ntt.forward_interleaved(cw0.data(), t, 1);
@@ -468,7 +491,10 @@ class CpuBackend : public ProverBackend {
 
   // ---- lincheck
   void lc_comb(const std::vector<F128>& skip_w, const std::vector<F128>& xir) override {
-    lincheck_combs(S, skip_w, xir, comb_a, comb_b);
+    slot_ca.assign(S.slots.size(), {});
+    slot_cb.assign(S.slots.size(), {});
+    for (size_t t = 0; t < S.slots.size(); ++t)
+      lincheck_combs(S.slots[t], skip_w, slot_inner(S.slots[t], xir), slot_ca[t], slot_cb[t]);
   }
   void lc_zvec(const std::vector<F128>& x_outer) override {
     const uint32_t K = 1u << S.k_log, nu = S.nu;
@@ -492,10 +518,16 @@ class CpuBackend : public ProverBackend {
       ei += (c[h + i] + c[i]) * (v[h + i] + v[i]);
     }
   }
-  void lc_start(F128 alpha, F128 beta, uint32_t pin, F128& e1, F128& ei) override {
-    comb.resize(comb_a.size());
-    for (size_t i = 0; i < comb.size(); ++i) comb[i] = alpha * comb_a[i] + comb_b[i];
-    comb[pin] += beta;
+  void lc_start(F128 alpha, const std::vector<SlotComb>& sc, F128& e1, F128& ei) override {
+    comb.assign(size_t(1) << S.k_log, F128());
+    for (size_t t = 0; t < S.slots.size(); ++t) {
+      const auto& ca = slot_ca[t];
+      const auto& cb = slot_cb[t];
+      par_chunks(ca.size(), [&](size_t b0, size_t e0) {
+        for (size_t i = b0; i < e0; ++i) comb[sc[t].offset + i] = sc[t].weight * (alpha * ca[i] + cb[i]);
+      });
+    }
+    for (size_t t = 0; t < S.slots.size(); ++t) comb[sc[t].offset + sc[t].pin] += sc[t].beta;
     top_message(comb, zv, e1, ei);
   }
   static void bind_top(std::vector<F128>& v, F128 r) {
@@ -508,13 +540,16 @@ class CpuBackend : public ProverBackend {
     if (!last) top_message(comb, zv, e1, ei);
   }
   void lc_partial(std::vector<F128>& zp) override { zp = zv; }
-  void lc_matrix_evals(const std::vector<F128>& rest, const std::vector<F128>& zp, F128& ea, F128& eb) override {
-    auto er = build_eq(rest);
-    ea = F128(); eb = F128();
-    for (size_t c = 0; c < comb_a.size(); ++c) {
-      F128 w = er[c >> 6] * zp[c & 63];
-      ea += w * comb_a[c];
-      eb += w * comb_b[c];
+  void lc_matrix_evals(const std::vector<F128>& rest, const std::vector<F128>& zp, std::vector<Pair128>& evals) override {
+    for (size_t t = 0; t < S.slots.size(); ++t) {
+      auto er = build_eq(slot_inner(S.slots[t], rest));
+      F128 ea, eb;
+      for (size_t c = 0; c < slot_ca[t].size(); ++c) {
+        F128 w = er[c >> 6] * zp[c & 63];
+        ea += w * slot_ca[t][c];
+        eb += w * slot_cb[t][c];
+      }
+      evals.push_back({ea, eb});
     }
   }
   void lc_s_hat_v(const std::vector<F128>& tail, std::vector<F128>& out) override {
@@ -527,19 +562,22 @@ class CpuBackend : public ProverBackend {
 
   // ---- merged open
   void mo_build_w(const std::vector<WeightClaim>& cl, uint32_t nu, uint64_t area, F128& u0, F128& u2) override {
-    const size_t n = words();
+    const size_t n = q.size();
     mw.assign(n, F128());
     std::vector<std::vector<F128>> er(cl.size()), ec(cl.size());
     for (size_t i = 0; i < cl.size(); ++i) { er[i] = par_build_eq(cl[i].z_row); ec[i] = par_build_eq(cl[i].z_col); }
-    par_chunks(area, [&](size_t db, size_t de) {
-      for (uint64_t d = db; d < de; ++d) {
-        size_t row = d & ((size_t(1) << nu) - 1), col = d >> nu;
+    // jagged unrank (jagged.rs:132-140): column y holds dense [pfx[y], pfx[y+1])
+    const auto& pfx = S.col_prefix;
+    parallel_for(pfx.size() - 1, [&](size_t col) {
+      for (uint64_t d = pfx[col]; d < pfx[col + 1] && d < area; ++d) {
+        const size_t row = d - pfx[col];
         F128 acc;
         for (size_t i = 0; i < cl.size(); ++i) acc += fold_one_slot(er[i][row] * ec[i][col], cl[i].table.data());
         mw[d] = acc;
       }
     });
-    mq = z;
+    (void)nu;
+    mq = q;
     Two128 s = par_sum<Two128>(n / 2, [&](size_t ib, size_t ie, Two128& acc) {
       for (size_t i = ib; i < ie; ++i) {
         acc.x += mq[2 * i] * mw[2 * i];
@@ -569,8 +607,8 @@ class CpuBackend : public ProverBackend {
     auto e = par_build_eq(rho, gamma);
     lb.resize(e.size());
     par_chunks(e.size(), [&](size_t b, size_t en) { for (size_t i = b; i < en; ++i) lb[i] = F256(e[i]); });
-    lf.resize(z.size());
-    par_chunks(z.size(), [&](size_t b, size_t en) { for (size_t i = b; i < en; ++i) lf[i] = F256(z[i]); });
+    lf.resize(q.size());
+    par_chunks(q.size(), [&](size_t b, size_t en) { for (size_t i = b; i < en; ++i) lf[i] = F256(q[i]); });
   }
   F128 lg_eval_eq(const std::vector<F128>& zp) override {
     auto e = par_build_eq(zp);

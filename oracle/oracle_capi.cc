@@ -7,6 +7,7 @@
 //   u64 proof_len | bincode proof | u64 cap_len | cap x 32 | ab_value (16) | c_value (16)
 #include "cpu_backend.h"
 #include "verifier.h"
+#include "../flock_gb300/csrc/host/proof_io.h"
 #include <cstdlib>
 #include <map>
 #include <memory>
@@ -53,12 +54,7 @@ int oracle_last_phase_ms(double out[6]) {
   return 0;
 }
 
-int oracle_prove_fast(int hash_kind, uint64_t n_blocks, const void* inputs, const uint8_t* domain, size_t domain_len,
-                      uint8_t** out, size_t* out_len) {
-  try {
-    auto s = statement_for(hash_kind, (uint32_t)n_blocks);
-    oracle::CpuBackend B(*s);
-    ProveResult R = prove_fast(*s, B, static_cast<const uint8_t*>(inputs), domain, domain_len);
+static int emit_bundle(const ProveResult& R, uint8_t** out, size_t* out_len) {
     g_last_ms[0] = R.t.witness; g_last_ms[1] = R.t.commit; g_last_ms[2] = R.t.zerocheck;
     g_last_ms[3] = R.t.lincheck; g_last_ms[4] = R.t.open; g_last_ms[5] = R.t.total;
     std::vector<uint8_t> pb = proof_bytes(R.proof);
@@ -74,6 +70,68 @@ int oracle_prove_fast(int hash_kind, uint64_t n_blocks, const void* inputs, cons
     for (F128 v : {R.claims.ab_value, R.claims.c_value}) { u64(v.lo); u64(v.hi); }
     *out = buf;
     *out_len = len;
+    return 0;
+}
+
+int oracle_prove_fast(int hash_kind, uint64_t n_blocks, const void* inputs, const uint8_t* domain, size_t domain_len,
+                      uint8_t** out, size_t* out_len) {
+  try {
+    auto s = statement_for(hash_kind, (uint32_t)n_blocks);
+    oracle::CpuBackend B(*s);
+    ProveResult R = prove_fast(*s, B, static_cast<const uint8_t*>(inputs), domain, domain_len);
+    return emit_bundle(R, out, out_len);
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
+namespace {
+std::shared_ptr<Statement> union_statement_for(const int* kinds, size_t n_types, uint32_t nu, const uint64_t* counts) {
+  static std::mutex mu;
+  static std::map<std::vector<uint64_t>, std::shared_ptr<Statement>> cache;
+  std::vector<uint64_t> key{nu};
+  for (size_t i = 0; i < n_types; ++i) { key.push_back((uint64_t)kinds[i]); key.push_back(counts[i]); }
+  std::lock_guard<std::mutex> g(mu);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  std::vector<HashKind> types;
+  for (size_t i = 0; i < n_types; ++i) types.push_back((HashKind)kinds[i]);
+  auto s = std::make_shared<Statement>(make_union_statement(types, nu, std::vector<uint64_t>(counts, counts + n_types)));
+  compute_registry_digest(*s);
+  cache[key] = s;
+  return s;
+}
+}  // namespace
+
+// prove_fast_ligerito_union (prover.rs:587-620) of a registry given in slot order
+// (kinds[t], k_log descending) at row capacity 2^nu, declared counts and per-slot input
+// records in slot order. Output: the bundle format above.
+int oracle_prove_union(const int* kinds, size_t n_types, uint32_t nu, const uint64_t* counts,
+                       const void* const* inputs, const uint8_t* domain, size_t domain_len, uint8_t** out,
+                       size_t* out_len) {
+  try {
+    auto s = union_statement_for(kinds, n_types, nu, counts);
+    std::vector<const uint8_t*> in;
+    for (size_t i = 0; i < n_types; ++i) in.push_back(static_cast<const uint8_t*>(inputs[i]));
+    oracle::CpuBackend B(*s);
+    ProveResult R = prove_fast(*s, B, in, domain, domain_len);
+    return emit_bundle(R, out, out_len);
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
+// MixedProofBundleLigerito::to_bytes of a union bundle (proof_io.rs:254-282).
+int oracle_mixed_proof_io(const int* kinds, size_t n_types, uint32_t nu, const uint64_t* counts, const uint8_t* bundle,
+                          size_t len, uint8_t** out, size_t* out_len) {
+  try {
+    auto s = union_statement_for(kinds, n_types, nu, counts);
+    auto v = mixed_proof_io_from_bundle(*s, bundle, len);
+    *out = static_cast<uint8_t*>(malloc(v.size()));
+    memcpy(*out, v.data(), v.size());
+    *out_len = v.size();
     return 0;
   } catch (const std::exception& e) {
     g_err = e.what();

@@ -704,7 +704,8 @@ inline void verify_bundle(const Statement& S, const Bundle& B, const uint8_t* do
   {
     // matrix discharge: the comb collapse at the bound column point
     std::vector<F128> ca, cb;
-    lincheck_combs(S, lagrange_weights64(zskip, 0), x_inner_rest, ca, cb);
+    if (S.slots.size() != 1) throw std::runtime_error("the restated verifier checks single-slot statements");
+    lincheck_combs(S.slots[0], lagrange_weights64(zskip, 0), x_inner_rest, ca, cb);
     auto er = build_eq(rr);
     F128 acc;
     for (size_t c = 0; c < ca.size(); ++c) {

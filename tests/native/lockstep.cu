@@ -47,7 +47,7 @@ struct Lockstep : ProverBackend {
     CUDA_OK(cudaMemcpy(h.data(), d, n * sizeof(T), cudaMemcpyDeviceToHost));
     return h;
   }
-  void witness(const uint8_t* in) override {
+  void witness(const std::vector<const uint8_t*>& in) override {
     C.witness(in); G.witness(in);
     auto z = dl<F128>(G.z(), G.words());
     check("witness z", z, C.z);
@@ -82,8 +82,8 @@ struct Lockstep : ProverBackend {
   }
   void lc_comb(const std::vector<F128>& w, const std::vector<F128>& x) override { C.lc_comb(w, x); G.lc_comb(w, x); }
   void lc_zvec(const std::vector<F128>& x) override { C.lc_zvec(x); G.lc_zvec(x); }
-  void lc_start(F128 al, F128 be, uint32_t pin, F128& e1, F128& ei) override {
-    F128 a, b; C.lc_start(al, be, pin, e1, ei); G.lc_start(al, be, pin, a, b);
+  void lc_start(F128 al, const std::vector<SlotComb>& sc, F128& e1, F128& ei) override {
+    F128 a, b; C.lc_start(al, sc, e1, ei); G.lc_start(al, sc, a, b);
     check("lc start e1", e1, a); check("lc start einf", ei, b);
   }
   void lc_round(F128 r, bool last, F128& e1, F128& ei) override {
@@ -93,9 +93,10 @@ struct Lockstep : ProverBackend {
   void lc_partial(std::vector<F128>& zp) override {
     std::vector<F128> z2; C.lc_partial(zp); G.lc_partial(z2); check("lc z_partial", zp, z2);
   }
-  void lc_matrix_evals(const std::vector<F128>& r, const std::vector<F128>& zp, F128& ea, F128& eb) override {
-    F128 a, b; C.lc_matrix_evals(r, zp, ea, eb); G.lc_matrix_evals(r, zp, a, b);
-    check("lc matrix ea", ea, a); check("lc matrix eb", eb, b);
+  void lc_matrix_evals(const std::vector<F128>& r, const std::vector<F128>& zp, std::vector<Pair128>& ev) override {
+    std::vector<Pair128> e2; C.lc_matrix_evals(r, zp, ev); G.lc_matrix_evals(r, zp, e2);
+    if (ev.size() != e2.size()) throw std::runtime_error("lc matrix eval count");
+    for (size_t i = 0; i < ev.size(); ++i) { check("lc matrix ea", ev[i].first, e2[i].first); check("lc matrix eb", ev[i].second, e2[i].second); }
   }
   void lc_s_hat_v(const std::vector<F128>& t, std::vector<F128>& o) override {
     std::vector<F128> o2; C.lc_s_hat_v(t, o); G.lc_s_hat_v(t, o2); check("lc s_hat_v", o, o2);
