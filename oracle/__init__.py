@@ -42,6 +42,9 @@ def load() -> ctypes.CDLL:
                                               c.c_char_p, c.c_size_t, c.POINTER(c.POINTER(c.c_uint8)),
                                               c.POINTER(c.c_size_t)]
         lib.oracle_mixed_proof_io.restype = c.c_int
+        lib.oracle_verify_union.argtypes = [c.POINTER(c.c_int), c.c_size_t, c.c_uint32, c.POINTER(c.c_uint64),
+                                            c.c_char_p, c.c_size_t, c.c_char_p, c.c_size_t, c.c_char_p, c.c_size_t]
+        lib.oracle_verify_union.restype = c.c_int
         _lib = lib
     return _lib
 
@@ -125,3 +128,15 @@ def mixed_proof_io(kinds, nu: int, counts, bundle: bytes) -> bytes:
         return ctypes.string_at(out, ln.value)
     finally:
         lib.oracle_free(out)
+
+
+def verify_union(kinds, nu: int, counts, bundle: bytes, domain: bytes) -> tuple:
+    """The restated verifier on a union bundle (registry in slot order, declared counts).
+    Returns (accepted, reason)."""
+    lib = load()
+    k, n, c = _union_args(kinds, counts)
+    reason = ctypes.create_string_buffer(256)
+    rc = lib.oracle_verify_union(k, n, nu, c, bundle, len(bundle), domain, len(domain), reason, 256)
+    if rc == 2:
+        raise RuntimeError(reason.value.decode())
+    return rc == 0, reason.value.decode()

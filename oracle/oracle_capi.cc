@@ -139,6 +139,33 @@ int oracle_mixed_proof_io(const int* kinds, size_t n_types, uint32_t nu, const u
   }
 }
 
+// Verifies a union bundle for the registry (slot order), nu and counts: 0 = accepted,
+// 1 = rejected (reason written), 2 = internal error.
+int oracle_verify_union(const int* kinds, size_t n_types, uint32_t nu, const uint64_t* counts, const uint8_t* bundle,
+                        size_t len, const uint8_t* domain, size_t domain_len, char* reason, size_t reason_len) {
+  auto say = [&](const std::string& m) {
+    if (reason && reason_len) {
+      size_t n = std::min(reason_len - 1, m.size());
+      memcpy(reason, m.data(), n);
+      reason[n] = 0;
+    }
+  };
+  try {
+    auto s = union_statement_for(kinds, n_types, nu, counts);
+    oracle::Bundle b = oracle::parse_bundle(bundle, len);
+    oracle::verify_bundle(*s, b, domain, domain_len);
+    say("accepted");
+    return 0;
+  } catch (const oracle::Reject& e) {
+    say(e.what());
+    return 1;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    say(std::string("internal error: ") + e.what());
+    return 2;
+  }
+}
+
 void oracle_free(uint8_t* p) { free(p); }
 
 // Verifies a bundle (the format above) for the statement (hash_kind, n_blocks) and the

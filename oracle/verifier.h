@@ -177,6 +177,28 @@ struct Quad256 {  // c + b X + a X^2 from a message (u0, u2) and the running cla
 // ---------------------------------------------------------------- anchor + multipoint
 // Anchor assist: replay 2 (m + 1) rounds, then the expected endpoint value
 // sum_st (sum_runs w_r eq(t_r, sigma)) * g_hat(z_row, point, sigma) (jagged.rs:2068-2210).
+// prod_j eq(coords[j], bit_j(bits)) (lincheck/union.rs:90-101).
+inline F128 eq_prefix_weight(const std::vector<F128>& coords, uint64_t bits) {
+  F128 acc = F128::one();
+  for (size_t j = 0; j < coords.size(); ++j) acc = acc * (((bits >> j) & 1) ? coords[j] : F128::one() + coords[j]);
+  return acc;
+}
+// sum_{i < n} eq(point, i) in O(|point|) (lincheck/union.rs:107-128); exactly one at n = 2^|point|.
+inline F128 eq_prefix_sum(const std::vector<F128>& point, uint64_t n) {
+  const size_t d = point.size();
+  if (n == (uint64_t(1) << d)) return F128::one();
+  F128 acc, high = F128::one();
+  for (size_t j = d; j-- > 0;) {
+    if ((n >> j) & 1) {
+      acc += high * (F128::one() + point[j]);
+      high = high * point[j];
+    } else {
+      high = high * (F128::one() + point[j]);
+    }
+  }
+  return acc;
+}
+
 inline F128 verify_anchor(Transcript& T, const std::vector<AssistStatement>& sts, const std::vector<F128>& point,
                           uint32_t m, const FrobeniusAssistProof& pf, uint32_t bits) {
   require(pf.rounds.size() == 2 * (size_t(m) + 1), "anchor: round count");
@@ -234,11 +256,13 @@ inline F128 verify_anchor(Transcript& T, const std::vector<AssistStatement>& sts
 
 // Multipoint twisted evaluation of the ring-switched claims at rho (jagged.rs:4418-4590):
 // returns V = sum_{i,j} c_ij A_ij^(2^j) once the dual values A are proven.
-inline F128 verify_multipoint(Transcript& T, const AlignedJagged& J, const std::vector<RsClaimPoint>& claims,
-                              const std::vector<F128>& rho, const MultipointTwistedProof& pf, uint32_t round_bits,
-                              uint32_t anchor_bits) {
+// make_stmt(z_row, z_col, coeff) builds a claim's anchor statement over the statement's
+// jagged layout (aligned or general).
+template <class MakeStmt>
+inline F128 verify_multipoint(Transcript& T, uint32_t m, const MakeStmt& make_stmt,
+                              const std::vector<RsClaimPoint>& claims, const std::vector<F128>& rho,
+                              const MultipointTwistedProof& pf, uint32_t round_bits, uint32_t anchor_bits) {
   const size_t R = claims.size();
-  const uint32_t m = J.m;
   require(pf.values.size() == R && pf.group_values.empty() && pf.rounds.size() == m, "multipoint: shape");
   for (auto& vs : pf.values) require(vs.size() == 128, "multipoint: dual value count");
   require(pf.round_grinding_nonces.size() == (round_bits ? m : 0), "multipoint: nonce count");
@@ -272,7 +296,7 @@ inline F128 verify_multipoint(Transcript& T, const AlignedJagged& J, const std::
     g_at += prod;
   }
   std::vector<AssistStatement> sts;
-  for (size_t i = 0; i < R; ++i) sts.push_back(aligned_statement(J, claims[i].z_row, claims[i].z_col, gpow[128 * i] * g_at));
+  for (size_t i = 0; i < R; ++i) sts.push_back(make_stmt(claims[i].z_row, claims[i].z_col, gpow[128 * i] * g_at));
   F128 s_at = verify_anchor(T, sts, point, m, pf.anchor, anchor_bits);
   require(running == s_at, "multipoint: sumcheck endpoint");
   F128 total;
@@ -621,9 +645,11 @@ inline void verify_bundle(const Statement& S, const Bundle& B, const uint8_t* do
   T.observe_label("flock-mixed-v1");
   T.observe_bytes(S.registry_digest.data(), 32);
   {
-    uint8_t counts[8];
-    for (int i = 0; i < 8; ++i) counts[i] = (uint8_t)((uint64_t)S.n_blocks >> (8 * i));
-    T.observe_bytes(counts, 8);
+    // the counts vector, one u64 LE per slot (union.rs:619-628)
+    std::vector<uint8_t> counts;
+    for (const SlotInfo& t : S.slots)
+      for (int i = 0; i < 8; ++i) counts.push_back((uint8_t)(t.count >> (8 * i)));
+    T.observe_bytes(counts);
     std::vector<uint8_t> capb;
     for (auto& h : B.cap) capb.insert(capb.end(), h.begin(), h.end());
     T.observe_bytes(capb);
@@ -676,48 +702,62 @@ inline void verify_bundle(const Statement& S, const Bundle& B, const uint8_t* do
   x_inner_rest.insert(x_inner_rest.end(), mlv.begin() + 1 + nu, mlv.end());
   const LincheckProof& lc = P.lincheck;
   const uint32_t inner_rest_len = k_log - 6;
-  require(lc.rounds.size() == inner_rest_len && lc.z_partial.size() == 64 && lc.matrix_evals.size() == 1 &&
-              lc.grinding_nonces.size() == inner_rest_len + 3,
+  const size_t n_slots = S.slots.size();
+  require(lc.rounds.size() == inner_rest_len && lc.z_partial.size() == 64 && lc.matrix_evals.size() == n_slots &&
+              lc.grinding_nonces.size() == inner_rest_len + 2 + n_slots,
           "lincheck: shape");
   T.observe_label("flock-lincheck-v0");
   require(T.verify_pow(lc.grinding_nonces[0], 1), "lincheck: alpha grinding");
   const F128 alpha = T.sample_f128();
-  require(T.verify_pow(lc.grinding_nonces[1], 1), "lincheck: beta grinding");
-  const F128 beta = T.sample_f128();
-  // const-pin target: beta * sum_{row < n} eq(x_outer, row) = beta at full utilisation
-  F128 lrun = alpha * zc.final_a_eval + zc.final_b_eval + beta;
+  // one const-pin challenge per slot; the target gains beta_t * sum_{row < n_t}
+  // eq(x_outer, row), exactly beta_t at full utilisation (lincheck/union.rs:800-830)
+  F128 lrun = alpha * zc.final_a_eval + zc.final_b_eval;
+  std::vector<F128> betas;
+  for (size_t t = 0; t < n_slots; ++t) {
+    require(T.verify_pow(lc.grinding_nonces[1 + t], 1), "lincheck: beta grinding");
+    betas.push_back(T.sample_f128());
+    lrun += betas[t] * eq_prefix_sum(x_outer, S.slots[t].count);
+  }
   std::vector<F128> r_rounds;
   for (uint32_t t = 0; t < inner_rest_len; ++t) {
     const F128 e1 = lc.rounds[t].first, ei = lc.rounds[t].second;
     T.observe_f128(e1);
     T.observe_f128(ei);
-    require(T.verify_pow(lc.grinding_nonces[2 + t], 2), "lincheck: round grinding");
+    require(T.verify_pow(lc.grinding_nonces[1 + n_slots + t], 2), "lincheck: round grinding");
     const F128 rt = T.sample_f128();
     const F128 e0 = lrun + e1, c1 = e0 + e1 + ei;
     lrun = ei * rt * rt + c1 * rt + e0;
     r_rounds.push_back(rt);
   }
   T.observe_f128_slice(lc.z_partial);
-  require(T.verify_pow(lc.grinding_nonces[2 + inner_rest_len], 6), "lincheck: skip grinding");
+  require(T.verify_pow(lc.grinding_nonces[1 + n_slots + inner_rest_len], 6), "lincheck: skip grinding");
   const F128 r_inner_skip = T.sample_f128();
   const std::vector<F128> rr(r_rounds.rbegin(), r_rounds.rend());
   {
-    // matrix discharge: the comb collapse at the bound column point
-    std::vector<F128> ca, cb;
-    if (S.slots.size() != 1) throw std::runtime_error("the restated verifier checks single-slot statements");
-    lincheck_combs(S.slots[0], lagrange_weights64(zskip, 0), x_inner_rest, ca, cb);
-    auto er = build_eq(rr);
-    F128 acc;
-    for (size_t c = 0; c < ca.size(); ++c) {
-      F128 comb = alpha * ca[c] + cb[c];
-      if (c == S.const_pin) comb += beta;
-      acc += er[c >> 6] * comb * lc.z_partial[c & 63];
+    // matrix discharge: the union comb collapse at the bound column point
+    // (lincheck/union.rs:540-625): per slot t with inner_t = k_log_t - 6 own column
+    // coordinates, w_t = eq weight of its prefix at the row point, P_t at the bound point
+    F128 acc, reported;
+    for (size_t t = 0; t < n_slots; ++t) {
+      const SlotInfo& T_ = S.slots[t];
+      const size_t inner = T_.k_log - 6;
+      std::vector<F128> ca, cb;
+      lincheck_combs(T_, lagrange_weights64(zskip, 0), slot_inner(T_, x_inner_rest), ca, cb);
+      const F128 w_t = eq_prefix_weight(std::vector<F128>(x_inner_rest.begin() + inner, x_inner_rest.end()), T_.prefix);
+      const F128 p_t = eq_prefix_weight(std::vector<F128>(rr.begin() + inner, rr.end()), T_.prefix);
+      auto er = build_eq(std::vector<F128>(rr.begin(), rr.begin() + inner));
+      F128 slot_acc;
+      for (size_t c = 0; c < ca.size(); ++c) {
+        F128 comb = w_t * (alpha * ca[c] + cb[c]);
+        if (c == T_.const_pin) comb += betas[t];
+        slot_acc += er[c >> 6] * comb * lc.z_partial[c & 63];
+      }
+      acc += p_t * slot_acc;
+      const F128 w_pin = er[T_.const_pin >> 6] * lc.z_partial[T_.const_pin & 63];
+      reported += p_t * (w_t * (alpha * lc.matrix_evals[t].first + lc.matrix_evals[t].second) + betas[t] * w_pin);
     }
     require(acc == lrun, "lincheck: matrix consistency");
-    // reported evaluations
-    const F128 w_pin = er[S.const_pin >> 6] * lc.z_partial[S.const_pin & 63];
-    require(alpha * lc.matrix_evals[0].first + lc.matrix_evals[0].second + beta * w_pin == lrun,
-            "lincheck: reported matrix evaluations");
+    require(reported == lrun, "lincheck: reported matrix evaluations");
   }
   F128 w_ab;
   {
@@ -771,8 +811,10 @@ inline void verify_bundle(const Statement& S, const Bundle& B, const uint8_t* do
     mrun = fold_round_claim(mrun, mo.merged_rounds[rd].first, mo.merged_rounds[rd].second, rt);
     rho.push_back(rt);
   }
-  AlignedJagged J{nu, S.geo.col_log, dense_log, S.geo.used_cols};
-  require(J.n + J.k == J.m, "merged open: jagged split");
+  const bool aligned = S.slots.size() == 1 && S.identity;
+  AlignedJagged J{nu, S.geo.col_log, dense_log, aligned ? S.slots[0].used_cols : 0};
+  JaggedLayout JL{nu, S.geo.col_log, dense_log, S.col_prefix};
+  require(aligned ? J.n + J.k == J.m : J.n + J.k >= J.m, "merged open: jagged split");
   std::vector<RsClaimPoint> fcl(2);
   for (int i = 0; i < 2; ++i) {
     const std::vector<F128>& x = *xs[i];
@@ -784,7 +826,10 @@ inline void verify_bundle(const Statement& S, const Bundle& B, const uint8_t* do
     fcl[i].coeffs = linearized_coefficients(fold_byte_table(scaled));
   }
   Transcript ch_a = T.fork("flock-par-assist-v1");
-  const F128 v = verify_multipoint(ch_a, J, fcl, rho, mo.frobenius, 2, 2);
+  auto stmt = [&](const std::vector<F128>& zr, const std::vector<F128>& zc, F128 coeff) {
+    return aligned ? aligned_statement(J, zr, zc, coeff) : jagged_statement(JL, zr, zc, coeff);
+  };
+  const F128 v = verify_multipoint(ch_a, dense_log, stmt, fcl, rho, mo.frobenius, 2, 2);
 
   // ---- inner opening of q_hat(rho) = q_eval
   const BatchOpeningProofLigerito& in = mo.inner;

@@ -1,7 +1,8 @@
 """Mixed multi-type union proofs on the GPU (flock_gb300_prove_union): the reference's four
 pinned BLAKE3 + SHA-256 nu = 10 digests through the proof-IO wire bytes
 (crates/flock-prover/tests/union_m6_fixtures.rs:196-281), byte identity with the oracle,
-and unions with Keccak-f slots and partial counts."""
+and unions with Keccak-f slots and partial counts, whose proofs the restated verifier
+accepts."""
 import hashlib
 
 import pytest
@@ -57,6 +58,8 @@ def test_union_with_keccak_matches_oracle(types, nu, counts):
         dom = b"gpu-union-%d" % nu
         bundle = u.prove_bytes(counts, recs, dom)
         assert bundle == oracle.prove_union_bytes(u.slot_kinds, nu, counts, recs, dom)
+        ok, why = oracle.verify_union(u.slot_kinds, nu, counts, bundle, dom)
+        assert ok, why
         with pytest.raises(FlockError):
             u.mixed_proof_io(counts, bundle)  # not a built-in tier
 

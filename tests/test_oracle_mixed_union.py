@@ -31,3 +31,24 @@ def test_oracle_reproduces_mixed_union_digest(anchors, idx):
     wire = oracle.mixed_proof_io(kinds, mx["nu"], [n_sha2, n_b3], bundle)
     assert wire[:7] == b"FLOCK\x15\x04"
     assert mixed_digest(bundle, wire) == fx["digest"], fx["name"]
+
+
+@pytest.mark.parametrize("idx", [1, 3])
+def test_restated_verifier_accepts_union_proofs_and_rejects_tampering(anchors, idx):
+    """The restated verifier replays a union bundle: per-slot const-pin challenges with
+    their count-derived targets, the per-slot matrix discharge under the slot prefix
+    weights, and the general jagged multipoint assist of the compacted stack."""
+    mx = anchors["mixed"]
+    n_sha2, n_b3 = mx["fixtures"][idx]["counts"]
+    sha, b3 = inputs.mixed_fixture(n_sha2, n_b3, mx["seed_base"] ^ (n_sha2 << 16) ^ n_b3)
+    kinds, counts, dom = [SHA256, BLAKE3], [n_sha2, n_b3], anchors["domain"].encode()
+    bundle = oracle.prove_union_bytes(kinds, mx["nu"], counts, [sha, b3], dom)
+    ok, why = oracle.verify_union(kinds, mx["nu"], counts, bundle, dom)
+    assert ok, why
+    for pos in (100, len(bundle) // 2, len(bundle) - 40):
+        bad = bytearray(bundle)
+        bad[pos] ^= 0x04
+        assert not oracle.verify_union(kinds, mx["nu"], counts, bytes(bad), dom)[0]
+    # the same bytes under different declared counts are a different statement
+    other = [n_sha2 + 1, n_b3] if n_sha2 < 1024 else [n_sha2, n_b3 - 1]
+    assert not oracle.verify_union(kinds, mx["nu"], other, bundle, dom)[0]
