@@ -6,6 +6,7 @@
 // in any order.
 #pragma once
 #include <algorithm>
+#include <cstdlib>
 #include <atomic>
 #include <condition_variable>
 #include <deque>
@@ -76,9 +77,15 @@ class ThreadPool {
     std::condition_variable cv;
   };
 
+  // Workers: all but two of the host's hardware threads (at most 15), or
+  // FLOCK_GB300_HOST_THREADS - 1 when that variable is set (the caller is the last one).
   ThreadPool() {
     unsigned hc = std::thread::hardware_concurrency();
     unsigned n = hc > 2 ? std::min(hc - 2, 15u) : 0u;
+    if (const char* e = std::getenv("FLOCK_GB300_HOST_THREADS")) {
+      const long v = std::strtol(e, nullptr, 10);
+      if (v >= 1 && v <= 256) n = (unsigned)(v - 1);
+    }
     for (unsigned i = 0; i < n; ++i) threads_.emplace_back([this] { loop(); });
   }
   static void work_on(Job& j) {

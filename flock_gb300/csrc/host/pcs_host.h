@@ -83,15 +83,13 @@ inline std::vector<F128> tensor_transpose128(const std::vector<F128>& v) {
   }
   return u;
 }
-// 16 x 256 byte tables: tab[k*256 + v] = sum of eq[8k + bit] over set bits of v.
+// 16 x 256 byte tables: tab[k*256 + v] = sum of eq[8k + bit] over set bits of v (each
+// entry one XOR from the entry without v's lowest set bit).
 inline std::vector<F128> fold_byte_table(const std::vector<F128>& eq128) {
   std::vector<F128> t(16 * 256);
   for (int k = 0; k < 16; ++k)
-    for (int v = 0; v < 256; ++v) {
-      F128 acc;
-      for (int b = 0; b < 8; ++b) if ((v >> b) & 1) acc += eq128[8 * k + b];
-      t[k * 256 + v] = acc;
-    }
+    for (int v = 1; v < 256; ++v)
+      t[k * 256 + v] = t[k * 256 + (v & (v - 1))] + eq128[8 * k + __builtin_ctz((unsigned)v)];
   return t;
 }
 inline F128 fold_one_slot(const F128& x, const F128* tab) {
@@ -148,7 +146,14 @@ inline std::vector<F128> linearized_coefficients(const std::vector<F128>& tab) {
 struct RingSwitchOut {
   RingSwitchProof proof;
   F128 sumcheck_claim;
-  std::vector<F128> table;
+  std::vector<F128> eq;     // eq(r'') over the 128 packing positions
+  std::vector<F128> table;  // fold_byte_table(eq)
+  // The table of gamma * eq: the table is linear in eq, so this is gamma times every
+  // entry, built from 128 products instead of 4096.
+  void scale(F128 gamma) {
+    for (auto& e : eq) e = e * gamma;
+    table = fold_byte_table(eq);
+  }
 };
 inline RingSwitchOut ring_switch_claim(Transcript& T, const std::vector<F128>& s_hat_v, uint32_t bits) {
   RingSwitchOut o;
@@ -163,6 +168,7 @@ inline RingSwitchOut ring_switch_claim(Transcript& T, const std::vector<F128>& s
   for (int i = 0; i < 128; ++i) acc += u[i] * eq[i];
   o.sumcheck_claim = acc;
   o.table = fold_byte_table(eq);
+  o.eq = std::move(eq);
   o.proof.s_hat_v = s_hat_v;
   return o;
 }

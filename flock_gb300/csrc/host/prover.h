@@ -339,8 +339,8 @@ inline ProveResult prove_fast(const Statement& S, ProverBackend& B, const std::v
   auto pg = T.grind_pow_and_sample_f128_vec(batch_bits, 2);
   mo.batching_nonces.push_back(pg.first);
   F128 g_ab = pg.second[0], g_c = pg.second[1];
-  for (auto& v : rs_ab.table) v = v * g_ab;
-  for (auto& v : rs_c.table) v = v * g_c;
+  rs_ab.scale(g_ab);
+  rs_c.scale(g_c);
   // The assist's linearised fold coefficients depend only on the scaled tables: compute
   // them on another host thread while the merged sumcheck runs on the backend.
   auto coeffs = std::async(std::launch::async, [&rs_ab, &rs_c] {
