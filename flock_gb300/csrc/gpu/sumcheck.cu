@@ -505,18 +505,35 @@ __device__ void publish_if_last(const F128d* part, uint32_t width, const FusedPu
 }
 
 // ------------------------------------------------------------------ pair fold + message
+// Folds of at least this many pairs take their products by r from byte tables. A block's
+// table build costs about as much shared-memory traffic as 300 table products, so the
+// table form also keeps at least PAIR_FOLD_TABLE_MIN_BLOCK_PAIRS pairs (4 table products
+// each) per block.
+constexpr uint64_t PAIR_FOLD_TABLE_MIN_PAIRS = uint64_t(1) << 17;
+constexpr uint64_t PAIR_FOLD_TABLE_MIN_BLOCK_PAIRS = 512;
 // Fold the low variable of two vectors at r (out[i] = in[2i] + r (in[2i+1] + in[2i]))
 // and, unless `msg` is false, emit the pair message over the folded vectors:
 //   g1 = sum_j eq(j) A1 B1, ginf = sum_j eq(j) (A0 + A1)(B0 + B1), (A0, A1) = out[2j..2j+2).
 // eq_lo == nullptr means eq = 1. n_pairs = output length / 2 (>= 1).
+// TBL: the four products by r come from byte tables of r in shared memory (load/store
+// pipe) while the message's products of two variables stay integer multiplies; the
+// block builds its table first, so this form is used where each block folds enough pairs
+// to pay for that. Otherwise r is split once per block for mul_split.
+template <bool TBL>
 __global__ void __launch_bounds__(256, 2)
 pair_fold_kernel(const F128d* __restrict__ ain, const F128d* __restrict__ bin, uint64_t n_pairs, F128d r,
                  const F128d* __restrict__ r_dev, const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F128d* __restrict__ eq_hi,
                  F128d* __restrict__ aout, F128d* __restrict__ bout, F128d* __restrict__ part, int msg, FusedPublish pub) {
+  extern __shared__ __align__(16) F128d rtab[];  // TBL: build_byte_table's BYTE_TABLE_SMEM_ENTRIES
   __shared__ F128d sh[32];
   __shared__ F128split rs;  // the fold challenge, split once
-  if (threadIdx.x == 0) rs = split_factor(r_dev ? *r_dev : r);
-  __syncthreads();
+  if (TBL) {
+    build_byte_table(r_dev ? *r_dev : r, rtab);
+  } else {
+    if (threadIdx.x == 0) rs = split_factor(r_dev ? *r_dev : r);
+    __syncthreads();
+  }
+  auto by_r = [&](F128d v) { return TBL ? mul_table(v, rtab) : mul_split_call(v, &rs); };
   const uint64_t chunk = 1ull << lo_bits;
   const uint64_t n_chunks = (n_pairs + chunk - 1) / chunk;
   F128d G1 = f128_zero(), GI = f128_zero();
@@ -526,8 +543,8 @@ pair_fold_kernel(const F128d* __restrict__ ain, const F128d* __restrict__ bin, u
     for (uint64_t j = ch * chunk + threadIdx.x; j < end; j += blockDim.x) {
       F128d x0 = ain[4 * j], x1 = ain[4 * j + 1], x2 = ain[4 * j + 2], x3 = ain[4 * j + 3];
       F128d y0 = bin[4 * j], y1 = bin[4 * j + 1], y2 = bin[4 * j + 2], y3 = bin[4 * j + 3];
-      F128d A0 = x0 + mul_split_call(x1 + x0, &rs), A1 = x2 + mul_split_call(x3 + x2, &rs);
-      F128d B0 = y0 + mul_split_call(y1 + y0, &rs), B1 = y2 + mul_split_call(y3 + y2, &rs);
+      F128d A0 = x0 + by_r(x1 + x0), A1 = x2 + by_r(x3 + x2);
+      F128d B0 = y0 + by_r(y1 + y0), B1 = y2 + by_r(y3 + y2);
       aout[2 * j] = A0; aout[2 * j + 1] = A1;
       bout[2 * j] = B0; bout[2 * j + 1] = B1;
       if (msg) {
@@ -558,9 +575,21 @@ uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, 
                           const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* aout, F128d* bout,
                           F128d* part, bool msg, cudaStream_t s, FusedPublish pub) {
   uint64_t n_chunks = (n_pairs + (1ull << lo_bits) - 1) >> lo_bits;
+  if (n_pairs >= PAIR_FOLD_TABLE_MIN_PAIRS) {
+    // two resident blocks per SM (74 KB of shared memory each), each building its table
+    // once for its share of the chunks
+    const int smem = (int)(BYTE_TABLE_SMEM_ENTRIES * sizeof(F128d));
+    set_dynamic_smem((const void*)pair_fold_kernel<true>, smem);
+    uint32_t blocks = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 4),
+                                                   n_pairs / PAIR_FOLD_TABLE_MIN_BLOCK_PAIRS);
+    pair_fold_kernel<true><<<blocks, 256, smem, s>>>(ain, bin, n_pairs, r, r_dev, eq_lo, lo_bits, eq_hi, aout, bout,
+                                                     part, msg ? 1 : 0, pub);
+    LAUNCH_OK();
+    return blocks;
+  }
   uint32_t blocks = (uint32_t)std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 8);
-  pair_fold_kernel<<<blocks, 256, 0, s>>>(ain, bin, n_pairs, r, r_dev, eq_lo, lo_bits, eq_hi, aout, bout, part,
-                                          msg ? 1 : 0, pub);
+  pair_fold_kernel<false><<<blocks, 256, 0, s>>>(ain, bin, n_pairs, r, r_dev, eq_lo, lo_bits, eq_hi, aout, bout, part,
+                                                 msg ? 1 : 0, pub);
   LAUNCH_OK();
   return blocks;
 }
@@ -1063,21 +1092,31 @@ uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64
   LAUNCH_OK();
   return blocks;
 }
-// o[i] = v[lo] + r (v[hi] + v[lo]), i = blk d + k, lo = 2 d blk + k.
-__global__ void lg_fold128_kernel(const F128d* __restrict__ f, const F128d* __restrict__ b, uint64_t n_out, F256d r,
-                                  const F256d* __restrict__ r_dev, uint32_t d_log, F256d* __restrict__ fo,
-                                  F256d* __restrict__ bo) {
-  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_out) return;
-  const uint64_t lo = pair_lo(i, d_log), hi = lo + (1ull << d_log);
-  F128d f0 = f[lo], df = f[hi] + f0, b0 = b[lo], db = b[hi] + b0;
+// o[i] = v[lo] + r (v[hi] + v[lo]), i = blk d + k, lo = 2 d blk + k. The products by r.c0
+// come from byte tables of r.c0 (load/store pipe), those by r.c1 from its split form
+// (multiply pipe); grid-stride, so each block's table serves many elements.
+__global__ void __launch_bounds__(256, 2)
+lg_fold128_kernel(const F128d* __restrict__ f, const F128d* __restrict__ b, uint64_t n_out, F256d r,
+                  const F256d* __restrict__ r_dev, uint32_t d_log, F256d* __restrict__ fo, F256d* __restrict__ bo) {
+  extern __shared__ __align__(16) F128d rtab[];  // build_byte_table's BYTE_TABLE_SMEM_ENTRIES
+  __shared__ F128split r1s;
   const F256d rv = r_dev ? *r_dev : r;
-  fo[i] = f256(f0 + mul_call(rv.c0, df), mul_call(rv.c1, df));
-  bo[i] = f256(b0 + mul_call(rv.c0, db), mul_call(rv.c1, db));
+  if (threadIdx.x == 0) r1s = split_factor(rv.c1);
+  build_byte_table(rv.c0, rtab);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_out; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t lo = pair_lo(i, d_log), hi = lo + (1ull << d_log);
+    F128d f0 = f[lo], df = f[hi] + f0, b0 = b[lo], db = b[hi] + b0;
+    fo[i] = f256(f0 + mul_table(df, rtab), mul_split_call(df, &r1s));
+    bo[i] = f256(b0 + mul_table(db, rtab), mul_split_call(db, &r1s));
+  }
 }
 void launch_lg_fold128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, const F256d* r_dev, uint64_t d,
                        F256d* fo, F256d* bo, cudaStream_t s) {
-  lg_fold128_kernel<<<(unsigned)((n_out + 255) / 256), 256, 0, s>>>(f, b, n_out, r, r_dev, log2_distance(d), fo, bo);
+  const int smem = (int)(BYTE_TABLE_SMEM_ENTRIES * sizeof(F128d));
+  set_dynamic_smem((const void*)lg_fold128_kernel, smem);
+  // at least 2048 elements per block (two table products each) for one table build
+  const uint64_t blocks = std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sm_count() * 2, n_out / 2048));
+  lg_fold128_kernel<<<(unsigned)blocks, 256, smem, s>>>(f, b, n_out, r, r_dev, log2_distance(d), fo, bo);
   LAUNCH_OK();
 }
 __global__ void lg_fold256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n_out, F256d r,
