@@ -845,7 +845,7 @@ void GpuBackend::lg_basis_eq(F128 gamma, const std::vector<F128>& rho) {
   lg_flush_fold();
   scr_off_ = 0;
   if ((uint64_t(1) << rho.size()) != Q_) throw std::runtime_error("Ligerito basis size mismatch");
-  EqSplit e = eq_split(rho, gamma, 10);
+  EqSplit e = eq_split(rho, gamma, 13);  // chunks of 2^13 entries: one eq_hi table each
   { Mark mk(this, ST_LIGERITO); launch_lg_eq_fill(e.lo, e.lo_bits, e.hi, Q_, lb128_, false, st_); }
   lg_base_ = true;
   lg_n_ = Q_;
@@ -866,7 +866,7 @@ void GpuBackend::lg_add_eq(F128 beta, const std::vector<F128>& zp) {
   lg_flush_fold();
   scr_off_ = 0;
   if (!lg_base_) throw std::runtime_error("basis update expects the base stage");
-  EqSplit e = eq_split(zp, beta, 10);
+  EqSplit e = eq_split(zp, beta, 13);
   { Mark mk(this, ST_LIGERITO); launch_lg_eq_fill(e.lo, e.lo_bits, e.hi, Q_, lb128_, true, st_); }
 }
 

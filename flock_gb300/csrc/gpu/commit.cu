@@ -64,6 +64,110 @@ __global__ void ntt_layer_kernel(F128d* __restrict__ data, uint32_t lanes, uint3
   data[i1 * lanes + l] = v + nu;
 }
 
+// Table layers: butterfly layers whose twiddle blocks are large. Each block of a launch
+// handles a contiguous share of one twiddle block's butterflies (2^cpb_log launch blocks
+// per twiddle block), builds that twiddle's byte tables once and takes half of its
+// products from them (load/store pipe), the other half from split twiddles (multiply
+// pipe). The butterflies of twiddle block b of a layer are the contiguous element ranges
+// u = [b 2^(sh+1) lanes, + 2^sh lanes) and v = u + 2^sh lanes, sh = log_d - layer - 1
+// (lane-minor layout); the first twiddle block's twiddle is zero in every layer.
+//
+// Two layers per pass: twiddle block b of `layer` spans the quarters x0..x3 of
+// Q = lanes 2^(sh-1) elements each; `layer` pairs (x0, x2) and (x1, x3) by t_b (table),
+// layer + 1 pairs (x0, x1) by t_2b and (x2, x3) by t_2b+1 (split). One read and one write
+// of the data per two layers.
+__global__ void __launch_bounds__(256, 3)
+ntt_layer2_tbl_kernel(F128d* __restrict__ data, uint32_t lanes, uint32_t log_d, uint32_t layer,
+                      const F128d* __restrict__ tw, uint32_t cpb_log) {
+  extern __shared__ __align__(16) F128d ttab[];  // build_byte_table's BYTE_TABLE_SMEM_ENTRIES
+  __shared__ F128split s0, s1;
+  const uint64_t b = blockIdx.x >> cpb_log, part = blockIdx.x & ((1ull << cpb_log) - 1);
+  const uint32_t sh = log_d - layer - 1;
+  const uint64_t Q = ((uint64_t)lanes) << (sh - 1);
+  const uint64_t per = Q >> cpb_log;
+  F128d* x = data + ((b << (sh + 1)) * lanes) + part * per;
+  const bool zero = (b == 0);  // block-uniform: t_b and t_2b are zero
+  if (threadIdx.x == 0) {
+    s0 = split_factor(tw[(2ull << layer) - 1 + 2 * b]);
+    s1 = split_factor(tw[(2ull << layer) - 1 + 2 * b + 1]);
+  }
+  if (!zero) build_byte_table(tw[(1ull << layer) - 1 + b], ttab);
+  else __syncthreads();
+  for (uint64_t k = threadIdx.x; k < per; k += blockDim.x) {
+    F128d a0 = x[k], a1 = x[Q + k], a2 = x[2 * Q + k], a3 = x[3 * Q + k];
+    if (!zero) {
+      a0 += mul_table(a2, ttab);
+      a1 += mul_table(a3, ttab);
+    }
+    a2 += a0;
+    a3 += a1;
+    if (!zero) a0 += mul_split_call(a1, &s0);
+    a1 += a0;
+    a2 += mul_split_call(a3, &s1);
+    a3 += a2;
+    x[k] = a0;
+    x[Q + k] = a1;
+    x[2 * Q + k] = a2;
+    x[3 * Q + k] = a3;
+  }
+}
+// One layer per pass (for an odd table layer): per thread and iteration one butterfly by
+// table and one by the split twiddle, the next iteration's operands loaded before this
+// one's products.
+__global__ void __launch_bounds__(256, 2)
+ntt_layer_tbl_kernel(F128d* __restrict__ data, uint32_t lanes, uint32_t log_d, uint32_t layer,
+                     const F128d* __restrict__ tw, uint32_t cpb_log) {
+  extern __shared__ __align__(16) F128d ttab[];  // build_byte_table's BYTE_TABLE_SMEM_ENTRIES
+  __shared__ F128split ts;
+  const uint64_t b = blockIdx.x >> cpb_log, part = blockIdx.x & ((1ull << cpb_log) - 1);
+  const uint32_t sh = log_d - layer - 1;
+  const uint64_t M = ((uint64_t)lanes) << sh;  // butterflies of twiddle block b
+  const uint64_t per = M >> cpb_log;           // this block's share (even: cpb_log < sh)
+  F128d* u = data + ((b << (sh + 1)) * lanes) + part * per;
+  F128d* v = u + M;
+  const bool zero = (b == 0);  // block-uniform
+  if (!zero) {
+    const F128d t = tw[(1ull << layer) - 1 + b];
+    if (threadIdx.x == 0) ts = split_factor(t);
+    build_byte_table(t, ttab);
+  }
+  const uint64_t half = per / 2;
+  uint64_t k = threadIdx.x;
+  F128d u0, v0, u1, v1;
+  if (k < half) {
+    u0 = u[k];
+    v0 = v[k];
+    u1 = u[half + k];
+    v1 = v[half + k];
+  }
+  for (; k < half; k += blockDim.x) {
+    const uint64_t kn = k + blockDim.x;
+    F128d p0, q0, p1, q1;
+    if (kn < half) {
+      p0 = u[kn];
+      q0 = v[kn];
+      p1 = u[half + kn];
+      q1 = v[half + kn];
+    }
+    const F128d n0 = zero ? u0 : u0 + mul_table(v0, ttab);
+    const F128d n1 = zero ? u1 : u1 + mul_split_call(v1, &ts);
+    u[k] = n0;
+    v[k] = v0 + n0;
+    u[half + k] = n1;
+    v[half + k] = v1 + n1;
+    u0 = p0;
+    v0 = q0;
+    u1 = p1;
+    v1 = q1;
+  }
+}
+// A layer is a table layer while its twiddle blocks hold at least this many butterflies
+// (a table build costs about as much shared-memory traffic as 300 table products), each
+// launch block getting at least NTT_TBL_MIN_BLOCK_BUTTERFLIES of them, and while the
+// transform is large enough to give every SM two such launch blocks.
+constexpr uint64_t NTT_TBL_MIN_TWIDDLE_BUTTERFLIES = uint64_t(1) << 12;
+constexpr uint64_t NTT_TBL_MIN_BLOCK_BUTTERFLIES = uint64_t(1) << 12;
+
 // Several consecutive layers [layer, layer + nl) fused through shared memory. A block
 // owns 2^nl positions spaced 2^(log_d - layer - nl) apart (one residue class inside a
 // block of the first fused layer) for a slice of lanes; each fused layer pairs positions
@@ -168,6 +272,40 @@ void launch_ntt(F128d* data, uint32_t lanes, uint32_t log_d, uint32_t start_laye
   uint32_t layer = start_layer;
   uint32_t lane_tile = lanes < 64 ? lanes : 64;
   const size_t tw_bytes = ((1u << NL) - 1) * sizeof(F128split);
+  // the top layers, whose twiddles are each shared by many butterflies: table layers, two
+  // per launch
+  const uint64_t butterflies = (uint64_t)lanes << (log_d - 1);
+  const bool tables = butterflies >= (uint64_t)sm_count() * 2 * NTT_TBL_MIN_BLOCK_BUTTERFLIES;
+  auto table_layer = [&](uint32_t l) {
+    return tables && l + 1 < log_d && ((uint64_t)lanes << (log_d - l - 1)) >= NTT_TBL_MIN_TWIDDLE_BUTTERFLIES;
+  };
+  // launch blocks per twiddle block: about eight per SM in all, and each with at least
+  // NTT_TBL_MIN_BLOCK_BUTTERFLIES of the `share` butterflies of its twiddle block
+  auto blocks_log = [&](uint32_t l, uint64_t share, uint32_t max_log) {
+    uint32_t c = 0;
+    while (c < max_log && ((uint64_t)1 << (l + c + 1)) <= (uint64_t)sm_count() * 8 &&
+           (share >> (c + 1)) >= NTT_TBL_MIN_BLOCK_BUTTERFLIES)
+      ++c;
+    return c;
+  };
+  const int tbl_smem = (int)(BYTE_TABLE_SMEM_ENTRIES * sizeof(F128d));
+  while (table_layer(layer)) {
+    const uint32_t sh = log_d - layer - 1;
+    if (table_layer(layer + 1) && sh >= 2) {
+      // radix-4 units of 4 elements; a block's share counted in butterflies (2 per unit)
+      const uint32_t c = blocks_log(layer, (uint64_t)lanes << sh, sh - 1);
+      set_dynamic_smem((const void*)ntt_layer2_tbl_kernel, tbl_smem);
+      ntt_layer2_tbl_kernel<<<(unsigned)(1ull << (layer + c)), 256, tbl_smem, s>>>(data, lanes, log_d, layer, tw, c);
+      LAUNCH_OK();
+      layer += 2;
+    } else {
+      const uint32_t c = blocks_log(layer, (uint64_t)lanes << sh, sh - 1);
+      set_dynamic_smem((const void*)ntt_layer_tbl_kernel, tbl_smem);
+      ntt_layer_tbl_kernel<<<(unsigned)(1ull << (layer + c)), 256, tbl_smem, s>>>(data, lanes, log_d, layer, tw, c);
+      LAUNCH_OK();
+      layer += 1;
+    }
+  }
   while (layer < log_d) {
     uint32_t remaining = log_d - layer;
     if (remaining >= (uint32_t)NL) {

@@ -1002,8 +1002,50 @@ __global__ void lg_eq_fill_kernel(const F128d* __restrict__ eq_lo, uint32_t lo_b
   if (add) out[i] += e;
   else out[i] = e;
 }
+// The same fill one chunk (2^lo_bits entries sharing eq_hi[chunk]) per block iteration:
+// the first half of a chunk takes its products by eq_hi[chunk] from the chunk's byte
+// tables, the second half from its split form; each thread forms one of each per
+// iteration, so the load/store and multiply pipes share the products.
+__global__ void __launch_bounds__(256, 2)
+lg_eq_fill_tbl_kernel(const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F128d* __restrict__ eq_hi, uint64_t n,
+                      F128d* __restrict__ out, int add) {
+  extern __shared__ __align__(16) F128d htab[];  // build_byte_table's BYTE_TABLE_SMEM_ENTRIES
+  __shared__ F128split hs;
+  const uint64_t chunk = 1ull << lo_bits, n_chunks = n >> lo_bits;
+  for (uint64_t ch = blockIdx.x; ch < n_chunks; ch += gridDim.x) {
+    __syncthreads();  // the previous chunk's table and split are no longer read
+    const F128d h = eq_hi[ch];
+    if (threadIdx.x == 0) hs = split_factor(h);
+    build_byte_table(h, htab);
+    F128d* o = out + ch * chunk;
+    const uint64_t half = chunk / 2;
+    for (uint64_t i = threadIdx.x; i < half; i += blockDim.x) {
+      const F128d e0 = mul_table(eq_lo[i], htab);
+      const F128d e1 = mul_split_call(eq_lo[half + i], &hs);
+      if (add) {
+        o[i] += e0;
+        o[half + i] += e1;
+      } else {
+        o[i] = e0;
+        o[half + i] = e1;
+      }
+    }
+  }
+}
+// Chunks of at least 2^12 entries (one table build per chunk), and enough of them to give
+// every SM two blocks, use the table form.
+constexpr uint32_t LG_EQ_FILL_TABLE_MIN_LO_BITS = 12;
 void launch_lg_eq_fill(const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, uint64_t n, F128d* out, bool add,
                        cudaStream_t s) {
+  if (eq_hi && lo_bits >= LG_EQ_FILL_TABLE_MIN_LO_BITS && (n >> lo_bits) >= (uint64_t)sm_count() * 2 &&
+      (n & ((1ull << lo_bits) - 1)) == 0) {
+    const int smem = (int)(BYTE_TABLE_SMEM_ENTRIES * sizeof(F128d));
+    set_dynamic_smem((const void*)lg_eq_fill_tbl_kernel, smem);
+    const uint32_t blocks = (uint32_t)std::min<uint64_t>(n >> lo_bits, (uint64_t)sm_count() * 2);
+    lg_eq_fill_tbl_kernel<<<blocks, 256, smem, s>>>(eq_lo, lo_bits, eq_hi, n, out, add ? 1 : 0);
+    LAUNCH_OK();
+    return;
+  }
   lg_eq_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(eq_lo, lo_bits, eq_hi, n, out, add ? 1 : 0);
   LAUNCH_OK();
 }
@@ -1146,20 +1188,49 @@ __device__ __forceinline__ void lg_fold_at(const F256d* __restrict__ f, const F2
   fi = f0 + f256_mul_call(r, f[hi] + f0);
   bi = b0 + f256_mul_call(r, b[hi] + b0);
 }
-__global__ void __launch_bounds__(256, 2)
+// TBL: the products by r come from byte tables of r.c0 and r.c1 plus the split form of
+// r.c0 + r.c1 (the Karatsuba terms of F256 product, see operator* in field.cuh): per pair
+// 8 table products on the load/store pipe beside 4 + 6 integer-multiply products. One
+// 512-thread block per SM holds the two tables (141 KB).
+template <bool TBL>
+__global__ void __launch_bounds__(TBL ? 512 : 256, TBL ? 1 : 2)
 lg_fold_msg256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n_out, F256d r,
                       uint32_t dlog_fold, uint32_t dlog_msg, F256d* __restrict__ fo, F256d* __restrict__ bo,
                       F128d* __restrict__ part, FusedPublish pub) {
+  extern __shared__ __align__(16) F128d rtab[];  // TBL: tables of r.c0 and r.c1
   __shared__ F128d sh[32];
+  __shared__ F128split rsum;
+  if (TBL) {
+    if (threadIdx.x == 0) rsum = split_factor(r.c0 + r.c1);
+    build_byte_table(r.c0, rtab);
+    build_byte_table(r.c1, rtab + BYTE_TABLE_ENTRIES);  // its scratch follows the second table
+  }
+  // fold of entry i (see lg_fold_at)
+  auto fold_at = [&](uint64_t i, F256d& fi, F256d& bi) {
+    if (TBL) {
+      const uint64_t lo = pair_lo(i, dlog_fold), hi = lo + (1ull << dlog_fold);
+      const F256d f0 = f[lo], b0 = b[lo], df = f[hi] + f0, db = b[hi] + b0;
+      const F128d* T0 = rtab;
+      const F128d* T1 = rtab + BYTE_TABLE_ENTRIES;
+      F128d p0 = mul_table(df.c0, T0), p1 = mul_table(df.c1, T1), p2 = mul_split_call(df.c0 + df.c1, &rsum);
+      fi = f0 + f256(p0 + mul_by_x_inv(p1), p2 + p0);
+      p0 = mul_table(db.c0, T0);
+      p1 = mul_table(db.c1, T1);
+      p2 = mul_split_call(db.c0 + db.c1, &rsum);
+      bi = b0 + f256(p0 + mul_by_x_inv(p1), p2 + p0);
+    } else {
+      lg_fold_at(f, b, r, dlog_fold, i, fi, bi);
+    }
+  };
   F256d u0 = f256(f128_zero(), f128_zero()), u2 = u0;
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_out / 2; p += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t olo = pair_lo(p, dlog_msg), ohi = olo + (1ull << dlog_msg);
     F256d fl, bl, fh, bh;
-    lg_fold_at(f, b, r, dlog_fold, olo, fl, bl);
+    fold_at(olo, fl, bl);
     fo[olo] = fl;
     bo[olo] = bl;
     u0 += f256_mul_call(fl, bl);
-    lg_fold_at(f, b, r, dlog_fold, ohi, fh, bh);
+    fold_at(ohi, fh, bh);
     fo[ohi] = fh;
     bo[ohi] = bh;
     u2 += f256_mul_call(fl + fh, bl + bh);
@@ -1171,11 +1242,25 @@ lg_fold_msg256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, 
   }
   if (pub.out) publish_if_last(part, 4, pub, sh);
 }
+// Folds of at least this many output entries use the table form, with at least
+// LG_FOLD_TABLE_MIN_BLOCK_PAIRS message pairs per block for its two table builds.
+constexpr uint64_t LG_FOLD_TABLE_MIN_OUT = uint64_t(1) << 17;
+constexpr uint64_t LG_FOLD_TABLE_MIN_BLOCK_PAIRS = 512;
 uint32_t launch_lg_fold_msg256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, uint64_t d_fold, uint64_t d_msg,
                                F256d* fo, F256d* bo, F128d* part, cudaStream_t s, FusedPublish pub) {
+  if (n_out >= LG_FOLD_TABLE_MIN_OUT) {
+    const int smem = (int)((BYTE_TABLE_ENTRIES + BYTE_TABLE_SMEM_ENTRIES) * sizeof(F128d));
+    set_dynamic_smem((const void*)lg_fold_msg256_kernel<true>, smem);
+    const uint32_t blocks = (uint32_t)std::max<uint64_t>(
+        1, std::min<uint64_t>((uint64_t)sm_count(), n_out / 2 / LG_FOLD_TABLE_MIN_BLOCK_PAIRS));
+    lg_fold_msg256_kernel<true><<<blocks, 512, smem, s>>>(f, b, n_out, r, log2_distance(d_fold), log2_distance(d_msg),
+                                                          fo, bo, part, pub);
+    LAUNCH_OK();
+    return blocks;
+  }
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n_out / 2 + 255) / 256, (uint64_t)sm_count() * 8));
-  lg_fold_msg256_kernel<<<blocks, 256, 0, s>>>(f, b, n_out, r, log2_distance(d_fold), log2_distance(d_msg), fo, bo,
-                                               part, pub);
+  lg_fold_msg256_kernel<false><<<blocks, 256, 0, s>>>(f, b, n_out, r, log2_distance(d_fold), log2_distance(d_msg), fo,
+                                                      bo, part, pub);
   LAUNCH_OK();
   return blocks;
 }
