@@ -856,7 +856,8 @@ F128 GpuBackend::lg_eval_eq(const std::vector<F128>& zp) {
   lg_flush_fold();
   scr_off_ = 0;
   if (!lg_base_) throw std::runtime_error("OOD evaluation expects the committed base vector");
-  EqSplit e = eq_split(zp, F128::one(), 10);
+  // chunks of 2^13 words (one eq_hi table each) where there are enough of them for every SM
+  EqSplit e = eq_split(zp, F128::one(), (Q_ >> 13) >= (uint64_t)sm_count() ? 13 : 10);
   uint32_t nb;
   { Mark mk(this, ST_LIGERITO); nb = launch_lg_dot_eq(q_, 1, e.lo, e.lo_bits, e.hi, Q_, part_, st_); }
   return reduce(nb, 1)[0];

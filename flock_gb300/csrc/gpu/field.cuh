@@ -177,16 +177,18 @@ constexpr uint32_t BYTE_TABLE_ENTRIES = 16 * 256;
 // 128 power entries of scratch.
 constexpr uint32_t BYTE_TABLE_SMEM_ENTRIES = BYTE_TABLE_ENTRIES + 512 + 128;
 
-// Every thread of the block calls this; T has BYTE_TABLE_SMEM_ENTRIES entries. The table
-// is complete when it returns. Built in three steps: E[i] = c x^i (128 products), nibble
-// tables N[4-bit position j][u] = sum of u's bits times E[4j + bit], then each byte entry
-// as the XOR of its two nibble entries.
-__device__ __forceinline__ void build_byte_table(F128d c, F128d* T) {
+// The same tables serve any GF(2)-linear map f of GF(2^128): T[256 k + v] = f(v x^(8k)),
+// built from the 128 images E[i] = f(x^i).
+__device__ __forceinline__ F128d unit_power(uint32_t i) { return i < 64 ? f128(1ull << i, 0) : f128(0, 1ull << (i - 64)); }
+// Every thread of the block calls this; T has BYTE_TABLE_SMEM_ENTRIES entries and its
+// scratch already holds the images (byte_table_images(T)[i] = f(x^i), written before a
+// block barrier). The table is complete when it returns. Nibble tables N[4-bit position
+// j][u] = sum of u's bits times E[4j + bit], then each byte entry as the XOR of its two
+// nibble entries.
+__device__ __forceinline__ F128d* byte_table_images(F128d* T) { return T + BYTE_TABLE_ENTRIES + 512; }
+__device__ __forceinline__ void byte_table_from_images(F128d* T) {
   F128d* N = T + BYTE_TABLE_ENTRIES;
-  F128d* E = N + 512;
-  for (uint32_t i = threadIdx.x; i < 128; i += blockDim.x)
-    E[i] = mul_call(c, i < 64 ? f128(1ull << i, 0) : f128(0, 1ull << (i - 64)));
-  __syncthreads();
+  const F128d* E = byte_table_images(T);
   for (uint32_t e = threadIdx.x; e < 512; e += blockDim.x) {
     const uint32_t j = e >> 4, u = e & 15;
     F128d acc = f128_zero();
@@ -205,6 +207,13 @@ __device__ __forceinline__ void build_byte_table(F128d c, F128d* T) {
     T[e] = N[32 * k + (v & 15)] + N[32 * k + 16 + (v >> 4)];
   }
   __syncthreads();
+}
+// The tables of the product by c: E[i] = c x^i (128 products), then as above.
+__device__ __forceinline__ void build_byte_table(F128d c, F128d* T) {
+  F128d* E = byte_table_images(T);
+  for (uint32_t i = threadIdx.x; i < 128; i += blockDim.x) E[i] = mul_call(c, unit_power(i));
+  __syncthreads();
+  byte_table_from_images(T);
 }
 __device__ __forceinline__ F128d mul_table(F128d a, const F128d* __restrict__ T) {
   F128d acc = f128_zero();

@@ -975,9 +975,69 @@ mo_build_w_kernel(const F128d* __restrict__ q, const F128d* __restrict__ er0, co
   u2 = block_xor(u2, sh);
   if (threadIdx.x == 0) { part[blockIdx.x * 2] = u0; part[blockIdx.x * 2 + 1] = u2; }
 }
+// The same weight under identity compaction with tall columns (col = d >> nu): in column c
+// the map x -> fold_slot(x ec_i[c], table_i) is GF(2)-linear, so the block builds its byte
+// tables once per (column, part) work item and W[d] = M0_c(er0[row]) + M1_c(er1[row]) is
+// 32 table lookups and no multiply; only the message's products stay integer multiplies.
+// Work item = 2^(nu - part_log) consecutive rows of one column.
+__global__ void __launch_bounds__(512, 1)
+mo_build_w_cols_kernel(const F128d* __restrict__ q, const F128d* __restrict__ er0, const F128d* __restrict__ ec0,
+                       const F128d* __restrict__ er1, const F128d* __restrict__ ec1, const F128d* __restrict__ tables,
+                       uint32_t nu, uint32_t part_log, uint64_t area, uint64_t n, F128d* __restrict__ w,
+                       F128d* __restrict__ part) {
+  extern __shared__ __align__(16) F128d ct[];  // column tables M0, M1, then M1's scratch
+  __shared__ F128d sh[32];
+  F128d* T0 = ct;
+  F128d* T1 = ct + BYTE_TABLE_ENTRIES;
+  const uint64_t items = (n >> nu) << part_log, rows = 1ull << (nu - part_log);
+  F128d u0 = f128_zero(), u2 = f128_zero();
+  for (uint64_t it = blockIdx.x; it < items; it += gridDim.x) {
+    const uint64_t col = it >> part_log, d0 = (col << nu) + ((it & ((1ull << part_log) - 1)) << (nu - part_log));
+    const bool used = d0 < area;  // block-uniform
+    __syncthreads();  // the previous item's tables are no longer read
+    if (used) {
+      // M0's images (its scratch lies inside M1's table), then M1's
+      if (threadIdx.x < 128) byte_table_images(T0)[threadIdx.x] = fold_slot(mul_call(ec0[col], unit_power(threadIdx.x)), tables);
+      __syncthreads();
+      byte_table_from_images(T0);
+      if (threadIdx.x < 128)
+        byte_table_images(T1)[threadIdx.x] = fold_slot(mul_call(ec1[col], unit_power(threadIdx.x)), tables + 16 * 256);
+      __syncthreads();
+      byte_table_from_images(T1);
+    }
+    for (uint64_t j = threadIdx.x; j < rows / 2; j += blockDim.x) {
+      const uint64_t d = d0 + 2 * j, row = d & ((1ull << nu) - 1);
+      F128d W0 = f128_zero(), W1 = f128_zero();
+      if (used && d < area) W0 = mul_table(er0[row], T0) + mul_table(er1[row], T1);
+      if (used && d + 1 < area) W1 = mul_table(er0[row + 1], T0) + mul_table(er1[row + 1], T1);
+      w[d] = W0;
+      w[d + 1] = W1;
+      const F128d q0 = q[d], q1 = q[d + 1];
+      u0 += mul_call(q0, W0);
+      u2 += mul_call(q0 + q1, W0 + W1);
+    }
+  }
+  u0 = block_xor(u0, sh);
+  u2 = block_xor(u2, sh);
+  if (threadIdx.x == 0) { part[blockIdx.x * 2] = u0; part[blockIdx.x * 2 + 1] = u2; }
+}
+// Columns of at least 2^MO_COLS_MIN_NU rows take the column-table form.
+constexpr uint32_t MO_COLS_MIN_NU = 14;
 uint32_t launch_mo_build_w(const F128d* q, const F128d* er0, const F128d* ec0, const F128d* er1, const F128d* ec1,
                            const F128d* tables, uint32_t nu, uint64_t area, uint64_t n, F128d* w, F128d* part,
                            cudaStream_t s, const JaggedSegs* segs) {
+  if (!segs && nu >= MO_COLS_MIN_NU && (n >> nu) >= 1 && (n & ((1ull << nu) - 1)) == 0) {
+    // work items of at least 2^13 rows, about eight per SM in all
+    uint32_t part_log = 0;
+    while (nu - part_log > 13 && ((n >> nu) << part_log) < (uint64_t)sm_count() * 8) ++part_log;
+    const uint64_t items = (n >> nu) << part_log;
+    const uint32_t blocks = (uint32_t)std::min<uint64_t>(items, (uint64_t)sm_count());
+    const int smem = (int)((BYTE_TABLE_ENTRIES + BYTE_TABLE_SMEM_ENTRIES) * sizeof(F128d));
+    set_dynamic_smem((const void*)mo_build_w_cols_kernel, smem);
+    mo_build_w_cols_kernel<<<blocks, 512, smem, s>>>(q, er0, ec0, er1, ec1, tables, nu, part_log, area, n, w, part);
+    LAUNCH_OK();
+    return blocks;
+  }
   size_t smem = 2 * 16 * 256 * sizeof(F128d);
   uint32_t blocks = (uint32_t)std::min<uint64_t>((n / 2 + 511) / 512, (uint64_t)sm_count());
   if (segs) {
@@ -1066,8 +1126,52 @@ __global__ void lg_dot_eq_kernel(const F128d* __restrict__ f, uint32_t stride, c
   }
   if (threadIdx.x == 0) part[blockIdx.x] = G;
 }
+// The same sum with chunks of 2^13 words and unit stride, reordered so that every
+// per-word product is by a block constant:
+//   sum_i f[i] eq(i) = sum_a eq_lo[a] h[a],  h[a] = sum_chunks eq_hi[chunk] f[chunk 2^13 + a].
+// Thread t of the 512 owns the 16 low indices a = t + 512 k and accumulates its block's
+// share of h[a] chunk by chunk; the products by the chunk's eq_hi come half from its byte
+// tables, half from its split form. Then 16 products by eq_lo[a] and the block reduction.
+constexpr uint32_t DOT_EQ_TBL_LO_BITS = 13;
+__global__ void __launch_bounds__(512, 1)
+lg_dot_eq_tbl_kernel(const F128d* __restrict__ f, const F128d* __restrict__ eq_lo, const F128d* __restrict__ eq_hi,
+                     uint64_t n_chunks, F128d* __restrict__ part) {
+  extern __shared__ __align__(16) F128d htab[];  // build_byte_table's BYTE_TABLE_SMEM_ENTRIES
+  __shared__ F128split hs;
+  __shared__ F128d sh[32];
+  F128d h[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) h[k] = f128_zero();
+  for (uint64_t ch = blockIdx.x; ch < n_chunks; ch += gridDim.x) {
+    __syncthreads();  // the previous chunk's table and split are no longer read
+    const F128d e = eq_hi[ch];
+    if (threadIdx.x == 0) hs = split_factor(e);
+    build_byte_table(e, htab);
+    const F128d* fc = f + (ch << DOT_EQ_TBL_LO_BITS) + threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const F128d x = fc[512 * k];
+      h[k] += (k & 1) ? mul_split_call(x, &hs) : mul_table(x, htab);
+    }
+  }
+  F128d g = f128_zero();
+#pragma unroll
+  for (int k = 0; k < 16; ++k) g += mul_call(h[k], eq_lo[threadIdx.x + 512 * k]);
+  g = block_xor(g, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = g;
+}
 uint32_t launch_lg_dot_eq(const F128d* f, uint32_t stride, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi,
                           uint64_t n, F128d* part, cudaStream_t s) {
+  if (stride == 1 && eq_hi && lo_bits == DOT_EQ_TBL_LO_BITS && (n & ((1ull << lo_bits) - 1)) == 0 &&
+      (n >> lo_bits) >= (uint64_t)sm_count()) {
+    const uint64_t n_chunks = n >> lo_bits;
+    const uint32_t blocks = (uint32_t)sm_count();
+    const int smem = (int)(BYTE_TABLE_SMEM_ENTRIES * sizeof(F128d));
+    set_dynamic_smem((const void*)lg_dot_eq_tbl_kernel, smem);
+    lg_dot_eq_tbl_kernel<<<blocks, 512, smem, s>>>(f, eq_lo, eq_hi, n_chunks, part);
+    LAUNCH_OK();
+    return blocks;
+  }
   uint64_t n_chunks = (n + (1ull << lo_bits) - 1) >> lo_bits;
   uint32_t blocks = (uint32_t)std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 8);
   lg_dot_eq_kernel<<<blocks, 256, 0, s>>>(f, stride, eq_lo, lo_bits, eq_hi, n, part);
