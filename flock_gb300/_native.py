@@ -40,6 +40,7 @@ EXPORTS = (
     "flock_gb300_prove_union",
     "flock_gb300_mixed_proof_io",
     "flock_gb300_f128_mul_rate",
+    "flock_gb300_f128_table_mix_rate",
     "flock_gb300_proof_io",
     "flock_gb300_server_free",
     "flock_gb300_free",
@@ -153,6 +154,8 @@ def load() -> ctypes.CDLL:
         lib.flock_gb300_mixed_proof_io.restype = c.c_int
         lib.flock_gb300_f128_mul_rate.argtypes = [c.c_int, c.POINTER(c.c_double)]
         lib.flock_gb300_f128_mul_rate.restype = c.c_int
+        lib.flock_gb300_f128_table_mix_rate.argtypes = [c.c_int, c.POINTER(c.c_double)]
+        lib.flock_gb300_f128_table_mix_rate.restype = c.c_int
         lib.flock_gb300_server_free.argtypes = [c.c_void_p]
         lib.flock_gb300_server_free.restype = None
         lib.flock_gb300_free.argtypes = [c.POINTER(c.c_uint8)]

@@ -165,7 +165,7 @@ ntt_layer_tbl_kernel(F128d* __restrict__ data, uint32_t lanes, uint32_t log_d, u
 // (a table build costs about as much shared-memory traffic as 300 table products), each
 // launch block getting at least NTT_TBL_MIN_BLOCK_BUTTERFLIES of them, and while the
 // transform is large enough to give every SM two such launch blocks.
-constexpr uint64_t NTT_TBL_MIN_TWIDDLE_BUTTERFLIES = uint64_t(1) << 12;
+constexpr uint64_t NTT_TBL_MIN_TWIDDLE_BUTTERFLIES = uint64_t(1) << 11;
 constexpr uint64_t NTT_TBL_MIN_BLOCK_BUTTERFLIES = uint64_t(1) << 12;
 
 // Several consecutive layers [layer, layer + nl) fused through shared memory. A block

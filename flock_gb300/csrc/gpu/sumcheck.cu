@@ -381,8 +381,75 @@ zc_fold_skip_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, co
   }
   if (threadIdx.x == 0) { part[blockIdx.x * 2] = G1; part[blockIdx.x * 2 + 1] = GI; }
 }
+// The same message with the eq factors applied in the other order, for chunks of 1024
+// words (lo_bits = 10) and 256 threads: thread t sees the four low indices l = t + 256 k of
+// every chunk, so
+//   g1 = sum_k eq_lo[l_k] S1_k,  S1_k = sum_chunks eq_hi[chunk] (a1 b1)[chunk 1024 + l_k]
+// (ginf alike), and each per-word product by eq_lo becomes a product by the chunk's eq_hi,
+// taken from the chunk's byte tables on the load/store pipe; eq_lo enters in eight
+// products per thread at the end. Per word two products of variables stay on the multiply
+// pipe instead of four.
+constexpr uint32_t ZC_SKIP_DEFER_LO_BITS = 10;
+__global__ void __launch_bounds__(256, 2)
+zc_fold_skip_defer_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, const F128d* __restrict__ w64,
+                          uint64_t n_chunks, const F128d* __restrict__ eq_lo, const F128d* __restrict__ eq_hi,
+                          F128d* __restrict__ part) {
+  __shared__ F128d T[8][256];
+  __shared__ F128d sh[32];
+  extern __shared__ __align__(16) F128d htab[];  // build_byte_table's BYTE_TABLE_SMEM_ENTRIES
+  for (uint32_t e = threadIdx.x; e < 2048; e += blockDim.x) {
+    uint32_t c = e >> 8, v = e & 255;
+    F128d acc = f128_zero();
+    for (int k = 0; k < 8; ++k)
+      if ((v >> k) & 1) acc += w64[8 * c + k];
+    T[c][v] = acc;
+  }
+  F128d S1[4], SI[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) S1[k] = SI[k] = f128_zero();
+  for (uint64_t ch = blockIdx.x; ch < n_chunks; ch += gridDim.x) {
+    __syncthreads();  // T is complete; the previous chunk's table is no longer read
+    build_byte_table(eq_hi[ch], htab);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint64_t wi = (ch << ZC_SKIP_DEFER_LO_BITS) + threadIdx.x + 256 * k;
+      const F128d av = a[wi], bv = b[wi];
+      F128d a0 = f128_zero(), a1 = f128_zero(), b0 = f128_zero(), b1 = f128_zero();
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        a0 += T[c][(av.lo >> (8 * c)) & 255];
+        a1 += T[c][(av.hi >> (8 * c)) & 255];
+        b0 += T[c][(bv.lo >> (8 * c)) & 255];
+        b1 += T[c][(bv.hi >> (8 * c)) & 255];
+      }
+      S1[k] += mul_table(mul_call(a1, b1), htab);
+      SI[k] += mul_table(mul_call(a0 + a1, b0 + b1), htab);
+    }
+  }
+  F128d G1 = f128_zero(), GI = f128_zero();
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const F128d e = eq_lo[threadIdx.x + 256 * k];
+    G1 += mul_call(e, S1[k]);
+    GI += mul_call(e, SI[k]);
+  }
+  G1 = block_xor(G1, sh);
+  GI = block_xor(GI, sh);
+  if (threadIdx.x == 0) { part[blockIdx.x * 2] = G1; part[blockIdx.x * 2 + 1] = GI; }
+}
 uint32_t launch_zc_fold_skip(const F128d* a, const F128d* b, const F128d* w64, uint64_t n_words, const F128d* eq_lo,
                              uint32_t lo_bits, const F128d* eq_hi, F128d* part, cudaStream_t s) {
+  if (eq_hi && lo_bits == ZC_SKIP_DEFER_LO_BITS && (n_words & ((1ull << lo_bits) - 1)) == 0 &&
+      (n_words >> lo_bits) >= (uint64_t)sm_count() * 8) {
+    // two resident blocks per SM, each looping over its share of the chunks
+    const uint64_t n_chunks = n_words >> lo_bits;
+    const uint32_t blocks = (uint32_t)sm_count() * 2;
+    const int smem = (int)(BYTE_TABLE_SMEM_ENTRIES * sizeof(F128d));
+    set_dynamic_smem((const void*)zc_fold_skip_defer_kernel, smem);
+    zc_fold_skip_defer_kernel<<<blocks, 256, smem, s>>>(a, b, w64, n_chunks, eq_lo, eq_hi, part);
+    LAUNCH_OK();
+    return blocks;
+  }
   uint64_t n_chunks = (n_words + (1ull << lo_bits) - 1) >> lo_bits;
   uint32_t blocks = (uint32_t)std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 8);
   zc_fold_skip_kernel<<<blocks, 256, 0, s>>>(a, b, w64, n_words, eq_lo, lo_bits, eq_hi, part);

@@ -215,6 +215,13 @@ int flock_gb300_mixed_proof_io(const flock_gb300_union_setup* setup, const uint6
  * the multiply-bound kernels are compared against. Allocates and frees its own buffers. */
 int flock_gb300_f128_mul_rate(int iters, double* muls_per_s);
 
+/* Measurement helper (no reference counterpart): products per second by a per-block
+ * constant in the mixed form the table kernels use (half the products from the constant's
+ * shared-memory byte tables, half from its split form), `iters` chained products per
+ * thread on a full grid. The peak that the constant-operand kernels (NTT table layers,
+ * challenge folds) are compared against. Allocates and frees its own buffers. */
+int flock_gb300_f128_table_mix_rate(int iters, double* products_per_s);
+
 /* Releases a bundle returned by flock_gb300_prove_fast (cuda-ghash/prove_ffi.cu:417 flock_cuda_free). */
 void flock_gb300_free(uint8_t* p);
 
