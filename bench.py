@@ -285,8 +285,8 @@ def run_gpu(args, world, rank, local):
                 continue
             o = measure(wl, args, world, rank, local)
             others[wl] = {k: o[k] for k in ("value", "unit", "ms_per_step", "config", "latency_ms", "e2e",
-                                            "roofline", "stages_ms_per_prove", "gpu_launches", "clocks",
-                                            "cpu_baseline")}
+                                            "roofline", "stages_ms_per_prove", "host_phase_ms", "gpu_launches",
+                                            "clocks", "cpu_baseline")}
         line["other_workloads"] = others
     print(json.dumps(line), flush=True)
     return 0

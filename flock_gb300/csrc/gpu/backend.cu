@@ -280,6 +280,7 @@ GpuBackend::Mark::~Mark() {
 }
 void GpuBackend::begin_prove(const void* d_inputs) {
   lg_pend_fold_.active = false;
+  lg_pend_switch_ = false;
   d_user_inputs_ = d_inputs;
   h2d_ = d2h_ = 0;
   spans_.clear();
@@ -872,6 +873,24 @@ void GpuBackend::lg_add_eq(F128 beta, const std::vector<F128>& zp) {
 }
 
 Msg256 GpuBackend::lg_message(size_t d) {
+  if (lg_pend_switch_ && (d == 1 || 2 * lg_n_ == d)) {
+    // code switch and the message over its pairs (2i, 2i + 1) in one pass
+    lg_pend_switch_ = false;
+    const int nx = lg_cur_ ^ 1;
+    FusedPublish fp = fused_publish();
+    {
+      Mark mk(this, ST_LIGERITO);
+      launch_lg_switch_msg(lf_[lg_cur_], lb_[lg_cur_], lg_n_, lf_[nx], lb_[nx], part_, st_, fp);
+    }
+    lg_cur_ = nx;
+    lg_n_ *= 2;
+    auto v = read_published(fp.seq, 4);
+    Msg256 m;
+    m.u0 = F256(v[0], v[1]);
+    m.u2 = F256(v[2], v[3]);
+    return m;
+  }
+  if (lg_pend_switch_) lg_flush_fold();  // a code switch followed by a message with other pairs
   if (lg_pend_fold_.active) {
     // fold and message in one pass over the F256 vectors
     const uint64_t n_out = lg_n_ / 2;
@@ -912,6 +931,16 @@ Msg256 GpuBackend::lg_message(size_t d) {
 }
 
 void GpuBackend::lg_flush_fold() {
+  if (lg_pend_switch_) {
+    lg_pend_switch_ = false;
+    const int nx = lg_cur_ ^ 1;
+    {
+      Mark mk(this, ST_LIGERITO);
+      launch_lg_code_switch(lf_[lg_cur_], lb_[lg_cur_], lg_n_, lf_[nx], lb_[nx], st_);
+    }
+    lg_cur_ = nx;
+    lg_n_ *= 2;
+  }
   if (!lg_pend_fold_.active) return;
   lg_pend_fold_.active = false;
   const uint64_t n_out = lg_n_ / 2;
@@ -951,11 +980,7 @@ void GpuBackend::lg_code_switch() {
   lg_flush_fold();
   if (lg_base_) throw std::runtime_error("code switch before the first fold");
   if (2 * lg_n_ > W_ / 2) throw std::runtime_error("code switch exceeds the Ligerito buffers");
-  int nx = lg_cur_ ^ 1;
-  Mark mk(this, ST_LIGERITO);
-  launch_lg_code_switch(lf_[lg_cur_], lb_[lg_cur_], lg_n_, lf_[nx], lb_[nx], st_);
-  lg_cur_ = nx;
-  lg_n_ *= 2;
+  lg_pend_switch_ = true;  // performed by the next message, or by lg_flush_fold
 }
 
 void GpuBackend::lg_commit(uint32_t level, uint32_t log_cols, uint32_t log_lanes, uint32_t log_rate,

@@ -179,6 +179,9 @@ class GpuBackend : public ProverBackend {
     size_t d = 0;
   };
   PendingFold lg_pend_fold_;
+  // A code switch is held back the same way: the next message (pairs one apart) runs fused
+  // with it; any other call first performs it on its own (lg_flush_fold does both).
+  bool lg_pend_switch_ = false;
   void lg_flush_fold();
   uint64_t lg_n_ = 0;
   F128d* pend_ = nullptr;

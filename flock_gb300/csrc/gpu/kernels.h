@@ -139,6 +139,10 @@ uint32_t launch_lg_fold_msg256(const F256d* f, const F256d* b, uint64_t n_out, F
 void launch_lg_fold256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, const F256d* r_dev, uint64_t d,
                        F256d* fo, F256d* bo, cudaStream_t s);
 void launch_lg_code_switch(const F256d* f, const F256d* b, uint64_t n, F256d* fo, F256d* bo, cudaStream_t s);
+// The code switch and the round message over the switched vectors with pairs one apart,
+// in one pass; published like launch_lg_message256 (four words).
+uint32_t launch_lg_switch_msg(const F256d* f, const F256d* b, uint64_t n, F256d* fo, F256d* bo, F128d* part,
+                              cudaStream_t s, FusedPublish pub);
 void launch_lg_replicate(const F256d* f, uint64_t msg, uint64_t total, F128d* mat, cudaStream_t s);
 uint32_t launch_lg_intro_eq(const F256d* f, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, uint64_t n,
                             F128d* pend, F128d* part, cudaStream_t s,

@@ -1450,6 +1450,44 @@ void launch_lg_code_switch(const F256d* f, const F256d* b, uint64_t n, F256d* fo
   lg_code_switch_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(f, b, n, fo, bo);
   LAUNCH_OK();
 }
+// The code switch fused with the next message (pairs (2i, 2i + 1) of the switched vectors).
+// The switched f entries are base-field, so both products of pair i are base x F256, two
+// F128 products each instead of three:
+//   u0 += f.c0 b = (f.c0 b.c0, f.c0 b.c1),
+//   u2 += (f.c0 + f.c1)(b + u b) = s (b.c0 + x^-1 b.c1, b.c0),  s = f.c0 + f.c1,
+// with u b = (x^-1 b.c1, b.c0 + b.c1) as the switch writes it.
+__global__ void lg_switch_msg_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n,
+                                     F256d* __restrict__ fo, F256d* __restrict__ bo, F128d* __restrict__ part,
+                                     FusedPublish pub) {
+  __shared__ F128d sh[32];
+  F128d u00 = f128_zero(), u01 = f128_zero(), u20 = f128_zero(), u21 = f128_zero();
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const F256d fv = f[i], bv = b[i];
+    const F128d ub0 = mul_by_x_inv(bv.c1);
+    fo[2 * i] = f256_base(fv.c0);
+    fo[2 * i + 1] = f256_base(fv.c1);
+    bo[2 * i] = bv;
+    bo[2 * i + 1] = f256(ub0, bv.c0 + bv.c1);
+    const F128d sv = fv.c0 + fv.c1;
+    u00 += mul_call(fv.c0, bv.c0);
+    u01 += mul_call(fv.c0, bv.c1);
+    u20 += mul_call(sv, bv.c0 + ub0);
+    u21 += mul_call(sv, bv.c0);
+  }
+  F128d r0 = block_xor(u00, sh), r1 = block_xor(u01, sh), r2 = block_xor(u20, sh), r3 = block_xor(u21, sh);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x * 4] = r0; part[blockIdx.x * 4 + 1] = r1;
+    part[blockIdx.x * 4 + 2] = r2; part[blockIdx.x * 4 + 3] = r3;
+  }
+  if (pub.out) publish_if_last(part, 4, pub, sh);
+}
+uint32_t launch_lg_switch_msg(const F256d* f, const F256d* b, uint64_t n, F256d* fo, F256d* bo, F128d* part,
+                              cudaStream_t s, FusedPublish pub) {
+  uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, (uint64_t)sm_count() * 8));
+  lg_switch_msg_kernel<<<blocks, 256, 0, s>>>(f, b, n, fo, bo, part, pub);
+  LAUNCH_OK();
+  return blocks;
+}
 // mat[i] = f[i mod msg].c0
 __global__ void lg_replicate_kernel(const F256d* __restrict__ f, uint64_t msg, uint64_t total, F128d* __restrict__ mat) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
