@@ -892,16 +892,21 @@ Msg256 GpuBackend::lg_message(size_t d) {
   }
   if (lg_pend_switch_) lg_flush_fold();  // a code switch followed by a message with other pairs
   if (lg_pend_fold_.active) {
-    // fold and message in one pass over the F256 vectors
+    // fold and message in one pass (over the base vectors for the first fold)
     const uint64_t n_out = lg_n_ / 2;
     const size_t dm = (d == 1 || n_out == d) ? 1 : d;
-    const int nx = lg_cur_ ^ 1;
+    const int nx = lg_pend_fold_.base ? 0 : lg_cur_ ^ 1;
     FusedPublish fp = fused_publish();
     {
       Mark mk(this, ST_LIGERITO);
-      launch_lg_fold_msg256(lf_[lg_cur_], lb_[lg_cur_], n_out, dev(lg_pend_fold_.r), lg_pend_fold_.d, dm, lf_[nx],
-                            lb_[nx], part_, st_, fp);
+      if (lg_pend_fold_.base)
+        launch_lg_fold_msg128(q_, lb128_, n_out, dev(lg_pend_fold_.r), lg_pend_fold_.d, dm, lf_[0], lb_[0], part_, st_,
+                              fp);
+      else
+        launch_lg_fold_msg256(lf_[lg_cur_], lb_[lg_cur_], n_out, dev(lg_pend_fold_.r), lg_pend_fold_.d, dm, lf_[nx],
+                              lb_[nx], part_, st_, fp);
     }
+    if (lg_pend_fold_.base) lg_base_ = false;
     lg_pend_fold_.active = false;
     lg_cur_ = nx;
     lg_n_ = n_out;
@@ -944,6 +949,16 @@ void GpuBackend::lg_flush_fold() {
   if (!lg_pend_fold_.active) return;
   lg_pend_fold_.active = false;
   const uint64_t n_out = lg_n_ / 2;
+  if (lg_pend_fold_.base) {
+    {
+      Mark mk(this, ST_LIGERITO);
+      launch_lg_fold128(q_, lb128_, n_out, dev(lg_pend_fold_.r), nullptr, lg_pend_fold_.d, lf_[0], lb_[0], st_);
+    }
+    lg_cur_ = 0;
+    lg_base_ = false;
+    lg_n_ = n_out;
+    return;
+  }
   const int nx = lg_cur_ ^ 1;
   {
     Mark mk(this, ST_LIGERITO);
@@ -956,24 +971,11 @@ void GpuBackend::lg_flush_fold() {
 
 void GpuBackend::lg_fold(F256 r, size_t d) {
   lg_flush_fold();
-  if (!lg_base_) {
-    lg_pend_fold_.active = true;
-    lg_pend_fold_.r = r;
-    lg_pend_fold_.d = d;
-    return;
-  }
-  uint64_t n_out = lg_n_ / 2;
-  Mark mk(this, ST_LIGERITO);
-  if (lg_base_) {
-    launch_lg_fold128(q_, lb128_, n_out, dev(r), nullptr, d, lf_[0], lb_[0], st_);
-    lg_cur_ = 0;
-    lg_base_ = false;
-  } else {
-    int nx = lg_cur_ ^ 1;
-    launch_lg_fold256(lf_[lg_cur_], lb_[lg_cur_], n_out, dev(r), nullptr, d, lf_[nx], lb_[nx], st_);
-    lg_cur_ = nx;
-  }
-  lg_n_ = n_out;
+  // held back: the next message runs fused with it, any other call performs it first
+  lg_pend_fold_.active = true;
+  lg_pend_fold_.base = lg_base_;
+  lg_pend_fold_.r = r;
+  lg_pend_fold_.d = d;
 }
 
 void GpuBackend::lg_code_switch() {

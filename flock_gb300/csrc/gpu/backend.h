@@ -175,6 +175,7 @@ class GpuBackend : public ProverBackend {
   // runs fused with it (one pass); any other call first performs it on its own.
   struct PendingFold {
     bool active = false;
+    bool base = false;  // the first fold: of the base vectors q_ and lb128_ into lf_[0], lb_[0]
     F256 r;
     size_t d = 0;
   };

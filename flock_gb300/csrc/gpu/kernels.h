@@ -133,6 +133,10 @@ uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64
                               FusedPublish pub = FusedPublish());
 void launch_lg_fold128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, const F256d* r_dev, uint64_t d,
                        F256d* fo, F256d* bo, cudaStream_t s);
+// The first fold (of the base vectors into F256 vectors) fused with the next message,
+// like launch_lg_fold_msg256.
+uint32_t launch_lg_fold_msg128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, uint64_t d_fold, uint64_t d_msg,
+                               F256d* fo, F256d* bo, F128d* part, cudaStream_t s, FusedPublish pub);
 uint32_t launch_lg_fold_msg256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, uint64_t d_fold, uint64_t d_msg,
                                F256d* fo, F256d* bo, F128d* part, cudaStream_t s,
                                FusedPublish pub = FusedPublish());                                  // width 4

@@ -1413,6 +1413,59 @@ lg_fold_msg256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, 
   }
   if (pub.out) publish_if_last(part, 4, pub, sh);
 }
+// The first fold, of the base (F128) vectors at r, fused with the next message: the
+// products r.c0 (f[hi] + f[lo]) and r.c1 (f[hi] + f[lo]) come from byte tables of r.c0 and
+// r.c1 (8 table products per message pair on the load/store pipe) and the message's two
+// F256 products of variables (6 F128 products) from integer multiplies. One 512-thread
+// block per SM holds the two tables.
+__global__ void __launch_bounds__(512, 1)
+lg_fold_msg128_kernel(const F128d* __restrict__ f, const F128d* __restrict__ b, uint64_t n_out, F256d r,
+                      uint32_t dlog_fold, uint32_t dlog_msg, F256d* __restrict__ fo, F256d* __restrict__ bo,
+                      F128d* __restrict__ part, FusedPublish pub) {
+  extern __shared__ __align__(16) F128d rtab[];  // tables of r.c0 and r.c1
+  __shared__ F128d sh[32];
+  const F128d* T0 = rtab;
+  const F128d* T1 = rtab + BYTE_TABLE_ENTRIES;
+  build_byte_table(r.c0, rtab);
+  build_byte_table(r.c1, rtab + BYTE_TABLE_ENTRIES);  // its scratch follows the second table
+  auto fold_at = [&](uint64_t i, F256d& fi, F256d& bi) {
+    const uint64_t lo = pair_lo(i, dlog_fold), hi = lo + (1ull << dlog_fold);
+    const F128d f0 = f[lo], df = f[hi] + f0, b0 = b[lo], db = b[hi] + b0;
+    fi = f256(f0 + mul_table(df, T0), mul_table(df, T1));
+    bi = f256(b0 + mul_table(db, T0), mul_table(db, T1));
+  };
+  F256d u0 = f256(f128_zero(), f128_zero()), u2 = u0;
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_out / 2; p += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t olo = pair_lo(p, dlog_msg), ohi = olo + (1ull << dlog_msg);
+    F256d fl, bl, fh, bh;
+    fold_at(olo, fl, bl);
+    fo[olo] = fl;
+    bo[olo] = bl;
+    u0 += f256_mul_call(fl, bl);
+    fold_at(ohi, fh, bh);
+    fo[ohi] = fh;
+    bo[ohi] = bh;
+    u2 += f256_mul_call(fl + fh, bl + bh);
+  }
+  F128d r0 = block_xor(u0.c0, sh), r1 = block_xor(u0.c1, sh), r2 = block_xor(u2.c0, sh), r3 = block_xor(u2.c1, sh);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x * 4] = r0; part[blockIdx.x * 4 + 1] = r1;
+    part[blockIdx.x * 4 + 2] = r2; part[blockIdx.x * 4 + 3] = r3;
+  }
+  if (pub.out) publish_if_last(part, 4, pub, sh);
+}
+uint32_t launch_lg_fold_msg128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, uint64_t d_fold, uint64_t d_msg,
+                               F256d* fo, F256d* bo, F128d* part, cudaStream_t s, FusedPublish pub) {
+  const int smem = (int)((BYTE_TABLE_ENTRIES + BYTE_TABLE_SMEM_ENTRIES) * sizeof(F128d));
+  set_dynamic_smem((const void*)lg_fold_msg128_kernel, smem);
+  // at least 512 message pairs per block for its two table builds
+  const uint32_t blocks =
+      (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sm_count(), n_out / 2 / 512));
+  lg_fold_msg128_kernel<<<blocks, 512, smem, s>>>(f, b, n_out, r, log2_distance(d_fold), log2_distance(d_msg), fo, bo,
+                                                   part, pub);
+  LAUNCH_OK();
+  return blocks;
+}
 // Folds of at least this many output entries use the table form, with at least
 // LG_FOLD_TABLE_MIN_BLOCK_PAIRS message pairs per block for its two table builds.
 constexpr uint64_t LG_FOLD_TABLE_MIN_OUT = uint64_t(1) << 17;
