@@ -1148,7 +1148,7 @@ lg_eq_fill_tbl_kernel(const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F
     const uint64_t half = chunk / 2;
     for (uint64_t i = threadIdx.x; i < half; i += blockDim.x) {
       const F128d e0 = mul_table(eq_lo[i], htab);
-      const F128d e1 = mul_split_call(eq_lo[half + i], &hs);
+      const F128d e1 = mul_split(eq_lo[half + i], hs);
       if (add) {
         o[i] += e0;
         o[half + i] += e1;
@@ -1218,7 +1218,7 @@ lg_dot_eq_tbl_kernel(const F128d* __restrict__ f, const F128d* __restrict__ eq_l
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
       const F128d x = fc[512 * k];
-      h[k] += (k & 1) ? mul_split_call(x, &hs) : mul_table(x, htab);
+      h[k] += (k & 1) ? mul_split(x, hs) : mul_table(x, htab);
     }
   }
   F128d g = f128_zero();
@@ -1319,8 +1319,8 @@ lg_fold128_kernel(const F128d* __restrict__ f, const F128d* __restrict__ b, uint
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_out; i += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t lo = pair_lo(i, d_log), hi = lo + (1ull << d_log);
     F128d f0 = f[lo], df = f[hi] + f0, b0 = b[lo], db = b[hi] + b0;
-    fo[i] = f256(f0 + mul_table(df, rtab), mul_split_call(df, &r1s));
-    bo[i] = f256(b0 + mul_table(db, rtab), mul_split_call(db, &r1s));
+    fo[i] = f256(f0 + mul_table(df, rtab), mul_split(df, r1s));
+    bo[i] = f256(b0 + mul_table(db, rtab), mul_split(db, r1s));
   }
 }
 void launch_lg_fold128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, const F256d* r_dev, uint64_t d,
