@@ -587,7 +587,7 @@ constexpr uint64_t PAIR_FOLD_TABLE_MIN_BLOCK_PAIRS = 512;
 // block builds its table first, so this form is used where each block folds enough pairs
 // to pay for that. Otherwise r is split once per block for mul_split.
 template <bool TBL>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, TBL ? 3 : 2)
 pair_fold_kernel(const F128d* __restrict__ ain, const F128d* __restrict__ bin, uint64_t n_pairs, F128d r,
                  const F128d* __restrict__ r_dev, const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F128d* __restrict__ eq_hi,
                  F128d* __restrict__ aout, F128d* __restrict__ bout, F128d* __restrict__ part, int msg, FusedPublish pub) {
@@ -643,11 +643,11 @@ uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, 
                           F128d* part, bool msg, cudaStream_t s, FusedPublish pub) {
   uint64_t n_chunks = (n_pairs + (1ull << lo_bits) - 1) >> lo_bits;
   if (n_pairs >= PAIR_FOLD_TABLE_MIN_PAIRS) {
-    // two resident blocks per SM (74 KB of shared memory each), each building its table
+    // three resident blocks per SM (74 KB of shared memory each), each building its table
     // once for its share of the chunks
     const int smem = (int)(BYTE_TABLE_SMEM_ENTRIES * sizeof(F128d));
     set_dynamic_smem((const void*)pair_fold_kernel<true>, smem);
-    uint32_t blocks = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 4),
+    uint32_t blocks = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 6),
                                                    n_pairs / PAIR_FOLD_TABLE_MIN_BLOCK_PAIRS);
     pair_fold_kernel<true><<<blocks, 256, smem, s>>>(ain, bin, n_pairs, r, r_dev, eq_lo, lo_bits, eq_hi, aout, bout,
                                                      part, msg ? 1 : 0, pub);
@@ -1047,7 +1047,7 @@ mo_build_w_kernel(const F128d* __restrict__ q, const F128d* __restrict__ er0, co
 // tables once per (column, part) work item and W[d] = M0_c(er0[row]) + M1_c(er1[row]) is
 // 32 table lookups and no multiply; only the message's products stay integer multiplies.
 // Work item = 2^(nu - part_log) consecutive rows of one column.
-__global__ void __launch_bounds__(512, 1)
+__global__ void __launch_bounds__(768, 1)
 mo_build_w_cols_kernel(const F128d* __restrict__ q, const F128d* __restrict__ er0, const F128d* __restrict__ ec0,
                        const F128d* __restrict__ er1, const F128d* __restrict__ ec1, const F128d* __restrict__ tables,
                        uint32_t nu, uint32_t part_log, uint64_t area, uint64_t n, F128d* __restrict__ w,
@@ -1101,7 +1101,7 @@ uint32_t launch_mo_build_w(const F128d* q, const F128d* er0, const F128d* ec0, c
     const uint32_t blocks = (uint32_t)std::min<uint64_t>(items, (uint64_t)sm_count());
     const int smem = (int)((BYTE_TABLE_ENTRIES + BYTE_TABLE_SMEM_ENTRIES) * sizeof(F128d));
     set_dynamic_smem((const void*)mo_build_w_cols_kernel, smem);
-    mo_build_w_cols_kernel<<<blocks, 512, smem, s>>>(q, er0, ec0, er1, ec1, tables, nu, part_log, area, n, w, part);
+    mo_build_w_cols_kernel<<<blocks, 768, smem, s>>>(q, er0, ec0, er1, ec1, tables, nu, part_log, area, n, w, part);
     LAUNCH_OK();
     return blocks;
   }
