@@ -216,30 +216,48 @@ zc_round1_ab_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, ui
   for (int k = 0; k < 4; ++k) part[row * 64 + 4 * lane + k] = acc[k];
 }
 
+// Warp-wide 32 x 32 bit transpose: lane r holds word x_r; afterwards lane c holds the word
+// whose bit r is bit c of x_r (five exchange stages of halving block size).
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t masks[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+  for (int s = 0; s < 5; ++s) {
+    const uint32_t j = 16u >> s, m = masks[s];
+    const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
+    x = (lane & j) ? ((x & ~m) | ((y & ~m) >> j)) : ((x & m) | ((y & m) << j));
+  }
+  return x;
+}
+
 // s_hat_v_c[t] = sum_xo eq_o(xo) sum_w wconst[w] bit_t(z[64 xo + w]). The word constants
 // and the eq_hi factor are applied once per eq_hi chunk, not per xo:
 //   part[t] = sum_chunks eq_hi(chunk) * sum_{w in group} wconst[w] * U[w][t],
 //   U[w][t] = sum_{xo in chunk} eq_lo(xo) bit_t(z[64 xo + w]),
-// so the inner loop is a masked XOR per (xo, word, bit) and no multiply. Block = 128
-// threads (one per bit t) x one group of 8 words (blockIdx.y) x a run of xo_per_block
-// consecutive xo (blockIdx.x); runs and chunks are powers of two.
+// so the inner loop has no multiply. Block = 128 threads (one per bit t; warp = 32-bit
+// limb) x one group of 8 words (blockIdx.y) x a run of xo_per_block consecutive xo
+// (blockIdx.x); runs and chunks are powers of two. Per tile of 32 xo and word w, the warp
+// transposes the 32 xo's limb words (lane r loads xo r), so thread t holds bit t of all 32
+// xo in one register; each byte of it indexes the 256 subset sums of eight xo's eq weights.
 constexpr uint32_t SVC_WORDS = 8;
-constexpr uint32_t SVC_TILE = 32;  // xo staged in shared memory per step
+constexpr uint32_t SVC_TILE = 32;  // xo staged in shared memory per step (one warp's lanes)
+constexpr uint32_t SVC_ZS_STRIDE = SVC_WORDS * 4 + 1;  // 32-bit words per staged xo, padded
 __global__ void __launch_bounds__(128)
 zc_svc_kernel(const F128d* __restrict__ z, uint64_t xo_per_block, const ZcConsts* __restrict__ gconst,
               const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F128d* __restrict__ eq_hi,
               F128d* __restrict__ part) {
-  __shared__ uint4 zt[SVC_TILE * SVC_WORDS];
+  __shared__ uint32_t zs[SVC_TILE * SVC_ZS_STRIDE];  // zs[xo * stride + 4 w + limb]
   __shared__ F128d et[SVC_TILE];
-  __shared__ F128d et4[SVC_TILE / 4][16];  // et4[q][v] = sum of et[4 q + k] over the bits k of v
-  const uint32_t t = threadIdx.x, limb = t >> 5, bit = t & 31;
+  __shared__ F128d et4[SVC_TILE / 4][16];   // et4[q][v] = sum of et[4 q + k] over the bits k of v
+  __shared__ F128d et8[SVC_TILE / 8][256];  // et8[q][v] = sum of et[8 q + k] over the bits k of v
+  const uint32_t t = threadIdx.x, limb = t >> 5, lane = t & 31;
   const uint32_t g = blockIdx.y;
   const uint64_t xo0 = (uint64_t)blockIdx.x * xo_per_block;
   const uint64_t chunk = 1ull << lo_bits;
   const uint64_t seg = xo_per_block < chunk ? xo_per_block : chunk;
   const uint32_t tile = seg < SVC_TILE ? (uint32_t)seg : SVC_TILE;
   const F128d* wc = gconst->wconst + g * SVC_WORDS;
-  const uint4* z4 = reinterpret_cast<const uint4*>(z);
+  const uint32_t* z32 = reinterpret_cast<const uint32_t*>(z);
   F128d acc = f128_zero();
   for (uint64_t s0 = xo0; s0 < xo0 + xo_per_block; s0 += seg) {
     F128d U[SVC_WORDS];
@@ -247,38 +265,38 @@ zc_svc_kernel(const F128d* __restrict__ z, uint64_t xo_per_block, const ZcConsts
     for (uint32_t w = 0; w < SVC_WORDS; ++w) U[w] = f128_zero();
     for (uint64_t xt = s0; xt < s0 + seg; xt += tile) {
       __syncthreads();
-      for (uint32_t i = t; i < tile * SVC_WORDS; i += blockDim.x)
-        zt[i] = z4[(xt + (i / SVC_WORDS)) * 64 + g * SVC_WORDS + (i % SVC_WORDS)];
-      if (t < tile) et[t] = eq_lo[(xt + t) & (chunk - 1)];
+      // xo past a short tile are staged as zero words with zero weight: they add nothing
+      for (uint32_t i = t; i < SVC_TILE * SVC_WORDS * 4; i += blockDim.x) {
+        const uint32_t xl = i / (SVC_WORDS * 4), rem = i % (SVC_WORDS * 4);
+        zs[xl * SVC_ZS_STRIDE + rem] = xl < tile ? z32[((xt + xl) * 64 + g * SVC_WORDS) * 4 + rem] : 0u;
+      }
+      if (t < SVC_TILE) et[t] = t < tile ? eq_lo[(xt + t) & (chunk - 1)] : f128_zero();
       __syncthreads();
-      // four xo at a time: their bits t form a 4-bit index into the subset sums of their eq
-      // weights (one lookup instead of four masked additions). A tile of fewer than four xo
-      // leaves rows past the tile out of every subset sum, whatever bits they hold.
-      const uint32_t groups = (tile + 3) / 4;
-      for (uint32_t i = t; i < groups * 16; i += blockDim.x) {
-        const uint32_t q = i >> 4, v = i & 15;
-        F128d acc = f128_zero();
+      {
+        const uint32_t q = t >> 4, v = t & 15;  // 128 threads: one nibble-table entry each
+        F128d a = f128_zero();
 #pragma unroll
         for (uint32_t k = 0; k < 4; ++k)
-          if (((v >> k) & 1) && 4 * q + k < tile) acc += et[4 * q + k];
-        et4[q][v] = acc;
+          if ((v >> k) & 1) a += et[4 * q + k];
+        et4[q][v] = a;
       }
       __syncthreads();
-      for (uint32_t q = 0; q < groups; ++q) {
-        const uint32_t* r0 = reinterpret_cast<const uint32_t*>(zt + (4 * q) * SVC_WORDS) + limb;
+      for (uint32_t i = t; i < (SVC_TILE / 8) * 256; i += blockDim.x) {
+        const uint32_t q = i >> 8, v = i & 255;
+        et8[q][v] = et4[2 * q][v & 15] + et4[2 * q + 1][v >> 4];
+      }
+      __syncthreads();
 #pragma unroll
-        for (uint32_t w = 0; w < SVC_WORDS; ++w) {
-          const uint32_t v = ((r0[4 * w] >> bit) & 1) | (((r0[4 * SVC_WORDS + 4 * w] >> bit) & 1) << 1) |
-                             (((r0[8 * SVC_WORDS + 4 * w] >> bit) & 1) << 2) |
-                             (((r0[12 * SVC_WORDS + 4 * w] >> bit) & 1) << 3);
-          U[w] += et4[q][v];
-        }
+      for (uint32_t w = 0; w < SVC_WORDS; ++w) {
+        const uint32_t bits = warp_transpose32(zs[lane * SVC_ZS_STRIDE + 4 * w + limb]);  // bit r: xo r
+#pragma unroll
+        for (uint32_t q = 0; q < SVC_TILE / 8; ++q) U[w] += et8[q][(bits >> (8 * q)) & 255];
       }
     }
     F128d v = f128_zero();
 #pragma unroll
-    for (uint32_t w = 0; w < SVC_WORDS; ++w) v += wc[w] * U[w];
-    acc += eq_hi ? eq_hi[s0 >> lo_bits] * v : v;
+    for (uint32_t w = 0; w < SVC_WORDS; ++w) v += mul_call(wc[w], U[w]);
+    acc += eq_hi ? mul_call(eq_hi[s0 >> lo_bits], v) : v;
   }
   part[((uint64_t)blockIdx.y * gridDim.x + blockIdx.x) * 128 + t] = acc;
 }
