@@ -119,6 +119,9 @@ GpuBackend::GpuBackend(const Statement& s) : S(s) {
   upload_constants_once();
   W_ = uint64_t(1) << (S.m - 7);
   K_ = 1u << S.k_log;
+  zc_live_words_ = (S.slots.size() == 1 && S.slots[0].offset == 0)
+                       ? std::min<uint64_t>(W_, S.slots[0].used_cols << S.nu)
+                       : W_;
   const uint64_t W = W_;
   in_bytes_ = 0;
   for (const SlotInfo& t : S.slots) in_bytes_ += (size_t)t.count * input_record_bytes(t.hash);
@@ -525,7 +528,7 @@ void GpuBackend::zc_round1(const std::vector<F128>& r, std::vector<F128>& ab, st
   F128d* part_svc = part_ + part_cap_ / 2;
   {
     Mark mk(this, ST_ZC_ROUND1);
-    launch_zc_round1(a_, b_, z_, m, e.lo, e.lo_bits, e.hi, part_, &nab, part_svc, &nsvc, st_);
+    launch_zc_round1(a_, b_, z_, m, zc_live_words_, e.lo, e.lo_bits, e.hi, part_, &nab, part_svc, &nsvc, st_);
   }
   if ((uint64_t)nab * 64 > part_cap_ / 2 || (uint64_t)nsvc * 128 > part_cap_ / 2)
     throw std::runtime_error("round-1 partials exceed the partials buffer");
@@ -598,7 +601,8 @@ void GpuBackend::zc_fold_skip(const std::vector<F128>& w, const std::vector<F128
   {
     Mark mk(this, ST_ZC_FOLD_SKIP);
     launch_eq_tables(dp, ddesc, (uint32_t)zc_desc_.size(), total, zc_tabs_, st_);
-    nb = launch_zc_fold_skip(a_, b_, dw, W_, zc_tabs_, 10, zc_tabs_ + zc_desc_[1].out_off, part_, st_);
+    // words from zc_live_words_ on are zero and add nothing to the message
+    nb = launch_zc_fold_skip(a_, b_, dw, zc_live_words_, zc_tabs_, 10, zc_tabs_ + zc_desc_[1].out_off, part_, st_);
     CUDA_OK(cudaMemcpyAsync(zc_w64_, dw, 64 * sizeof(F128d), cudaMemcpyDeviceToDevice, st_));
   }
   auto v = reduce(nb, 2);
@@ -607,6 +611,7 @@ void GpuBackend::zc_fold_skip(const std::vector<F128>& w, const std::vector<F128
   zc_cur_a_ = nullptr;  // the skip-folded vectors live only implicitly (a, b bits and the weights)
   zc_cur_b_ = nullptr;
   zc_len_ = 2 * W_;
+  zc_live_ = 2 * zc_live_words_;
   zc_round_ = 0;
 }
 
@@ -618,6 +623,8 @@ void GpuBackend::zc_fold(F128 rho, const std::vector<F128>& eq_point, F128& g1, 
     throw std::runtime_error("zerocheck fold: round tables out of step");
   const EqDesc& lo = zc_desc_[k];
   const EqDesc& hi = zc_desc_[k + 1];
+  // pairs (4 entries in, 2 out) from live_pairs on read only the zero tail
+  const uint64_t live_pairs = std::min<uint64_t>(n_pairs, (zc_live_ + 3) / 4);
   // round 0 writes W words per vector into zc2; later rounds alternate zc1 <-> zc2
   F128d* oa = (zc_round_ == 0 || zc_cur_a_ == zc1a_) ? zc2a_ : zc1a_;
   F128d* ob = (zc_round_ == 0 || zc_cur_a_ == zc1a_) ? zc2b_ : zc1b_;
@@ -626,11 +633,11 @@ void GpuBackend::zc_fold(F128 rho, const std::vector<F128>& eq_point, F128& g1, 
     Mark mk(this, ST_ZC_FOLDS);
     if (zc_round_ == 0) {
       F128d* tabs = static_cast<F128d*>(scratch(4096 * sizeof(F128d)));
-      nb = launch_zc_fold2(a_, b_, zc_w64_, dev(rho), tabs, n_pairs, zc_tabs_ + lo.out_off, lo.n, zc_tabs_ + hi.out_off,
-                           oa, ob, part_, st_);
+      nb = launch_zc_fold2(a_, b_, zc_w64_, dev(rho), tabs, n_pairs, live_pairs, zc_tabs_ + lo.out_off, lo.n,
+                           zc_tabs_ + hi.out_off, oa, ob, part_, st_);
     } else {
       FusedPublish fp = fused_publish();
-      launch_pair_fold(zc_cur_a_, zc_cur_b_, n_pairs, dev(rho), nullptr, zc_tabs_ + lo.out_off, lo.n,
+      launch_pair_fold(zc_cur_a_, zc_cur_b_, n_pairs, live_pairs, dev(rho), nullptr, zc_tabs_ + lo.out_off, lo.n,
                        zc_tabs_ + hi.out_off, oa, ob, part_, true, st_, fp);
       nb = 0;
       pub_seq = fp.seq;
@@ -642,6 +649,7 @@ void GpuBackend::zc_fold(F128 rho, const std::vector<F128>& eq_point, F128& g1, 
   zc_cur_a_ = oa;
   zc_cur_b_ = ob;
   zc_len_ /= 2;
+  zc_live_ = std::min(zc_len_, 2 * live_pairs);
   zc_round_++;
 }
 
@@ -824,7 +832,8 @@ void GpuBackend::mo_round(F128 r, bool last, F128& g1, F128& gi) {
   if (!last) fp = fused_publish();
   {
     Mark mk(this, ST_MO_ROUNDS);
-    launch_pair_fold(mo_q_, mo_w_, n_pairs, dev(r), nullptr, nullptr, chunk_bits, nullptr, oq, ow, part_, !last, st_, fp);
+    launch_pair_fold(mo_q_, mo_w_, n_pairs, n_pairs, dev(r), nullptr, nullptr, chunk_bits, nullptr, oq, ow, part_, !last,
+                     st_, fp);
   }
   mo_q_ = oq;
   mo_w_ = ow;

@@ -153,6 +153,12 @@ class GpuBackend : public ProverBackend {
   F128d *zc1a_ = nullptr, *zc1b_ = nullptr, *zc2a_ = nullptr, *zc2b_ = nullptr;
   F128d *zc_cur_a_ = nullptr, *zc_cur_b_ = nullptr;
   uint64_t zc_len_ = 0;
+  // Words of z, a and b that can be nonzero (a single slot's witness fills chunk-columns
+  // c < used_cols of word (c << nu) + instance; the tail is cleared at allocation and never
+  // written), and the live entries of the current zerocheck vectors: the zerocheck kernels
+  // skip the zero tail.
+  uint64_t zc_live_words_ = 0;
+  uint64_t zc_live_ = 0;
   uint32_t zc_round_ = 0;
   F128d* zc_w64_ = nullptr;  // skip-point Lagrange weights (device)
 

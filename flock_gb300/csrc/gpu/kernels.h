@@ -60,16 +60,20 @@ void launch_reduce_parts(const F128d* part, uint32_t n_blocks, uint32_t width, F
 
 void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t mulk[8][256], const F128d* wconst);
 // Round-1 partials: P_ab rows of width 64 into part_ab, s_hat_v_c rows of width 128 into part_svc.
-void launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32_t m, const F128d* eq_lo, uint32_t lo_bits,
-                      const F128d* eq_hi, F128d* part_ab, uint32_t* nrows_ab, F128d* part_svc, uint32_t* nrows_svc,
-                      cudaStream_t s);
+// Words of z, a and b from live_words on are zero (the zero tail of a single slot's chunk
+// columns) and are not read.
+void launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32_t m, uint64_t live_words,
+                      const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* part_ab, uint32_t* nrows_ab,
+                      F128d* part_svc, uint32_t* nrows_svc, cudaStream_t s);
 uint32_t launch_zc_fold_skip(const F128d* a, const F128d* b, const F128d* w64, uint64_t n_words, const F128d* eq_lo,
                              uint32_t lo_bits, const F128d* eq_hi, F128d* part, cudaStream_t s);       // width 2
 // First multilinear fold (at rho) of the skip-folded a, b, computed from the bits; writes
 // n_pairs * 2 words of each folded vector and the next message. tabs: 4096-word scratch.
+// Pairs from live_pairs on have zero inputs: their outputs are written as zeros and they
+// add nothing to the message.
 uint32_t launch_zc_fold2(const F128d* a, const F128d* b, const F128d* w64, F128d rho, F128d* tabs, uint64_t n_pairs,
-                         const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* aout, F128d* bout, F128d* part,
-                         cudaStream_t s);                                                              // width 2
+                         uint64_t live_pairs, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* aout,
+                         F128d* bout, F128d* part, cudaStream_t s);                                     // width 2
 // In-kernel publication of a round message: the last block to finish (a device-wide
 // ticket counter) XOR-reduces every block's partials, writes the message to mapped host
 // memory and then the sequence number, as launch_reduce_publish does in a launch of its
@@ -80,10 +84,12 @@ struct FusedPublish {
   uint32_t* counter = nullptr; // device memory
   uint32_t seq = 0;
 };
-// r_dev (when not null) is the device address of the challenge, read by the kernel.
-uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, F128d r, const F128d* r_dev,
-                          const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* aout, F128d* bout,
-                          F128d* part, bool msg, cudaStream_t s, FusedPublish pub = FusedPublish());  // width 2
+// r_dev (when not null) is the device address of the challenge, read by the kernel. Pairs
+// from live_pairs on have zero inputs (zeros written, nothing added to the message).
+uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, uint64_t live_pairs, F128d r,
+                          const F128d* r_dev, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* aout,
+                          F128d* bout, F128d* part, bool msg, cudaStream_t s,
+                          FusedPublish pub = FusedPublish());  // width 2
 
 void launch_lc_eq_inner(const F128d* w64, const F128d* er, uint32_t K, F128d* eqi, cudaStream_t s);
 void launch_csc_fold(const uint32_t* col_ptr, const uint32_t* rows, uint32_t K, const F128d* eqi, F128d* out,

@@ -243,7 +243,7 @@ constexpr uint32_t SVC_WORDS = 8;
 constexpr uint32_t SVC_TILE = 32;  // xo staged in shared memory per step (one warp's lanes)
 constexpr uint32_t SVC_ZS_STRIDE = SVC_WORDS * 4 + 1;  // 32-bit words per staged xo, padded
 __global__ void __launch_bounds__(128)
-zc_svc_kernel(const F128d* __restrict__ z, uint64_t xo_per_block, const ZcConsts* __restrict__ gconst,
+zc_svc_kernel(const F128d* __restrict__ z, uint64_t xo_per_block, uint64_t xo_live, const ZcConsts* __restrict__ gconst,
               const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F128d* __restrict__ eq_hi,
               F128d* __restrict__ part) {
   __shared__ uint32_t zs[SVC_TILE * SVC_ZS_STRIDE];  // zs[xo * stride + 4 w + limb]
@@ -258,19 +258,24 @@ zc_svc_kernel(const F128d* __restrict__ z, uint64_t xo_per_block, const ZcConsts
   const uint32_t tile = seg < SVC_TILE ? (uint32_t)seg : SVC_TILE;
   const F128d* wc = gconst->wconst + g * SVC_WORDS;
   const uint32_t* z32 = reinterpret_cast<const uint32_t*>(z);
+  // xo from xo_live on hold zero words: the block stops there (a block wholly past it
+  // writes a zero partial)
+  const uint64_t xo_end = xo0 + xo_per_block < xo_live ? xo0 + xo_per_block : xo_live;
   F128d acc = f128_zero();
-  for (uint64_t s0 = xo0; s0 < xo0 + xo_per_block; s0 += seg) {
+  for (uint64_t s0 = xo0; s0 < xo_end; s0 += seg) {
     F128d U[SVC_WORDS];
 #pragma unroll
     for (uint32_t w = 0; w < SVC_WORDS; ++w) U[w] = f128_zero();
-    for (uint64_t xt = s0; xt < s0 + seg; xt += tile) {
+    const uint64_t s_end = s0 + seg < xo_end ? s0 + seg : xo_end;
+    for (uint64_t xt = s0; xt < s_end; xt += tile) {
+      const uint32_t cur = xt + tile <= s_end ? tile : (uint32_t)(s_end - xt);
       __syncthreads();
       // xo past a short tile are staged as zero words with zero weight: they add nothing
       for (uint32_t i = t; i < SVC_TILE * SVC_WORDS * 4; i += blockDim.x) {
         const uint32_t xl = i / (SVC_WORDS * 4), rem = i % (SVC_WORDS * 4);
-        zs[xl * SVC_ZS_STRIDE + rem] = xl < tile ? z32[((xt + xl) * 64 + g * SVC_WORDS) * 4 + rem] : 0u;
+        zs[xl * SVC_ZS_STRIDE + rem] = xl < cur ? z32[((xt + xl) * 64 + g * SVC_WORDS) * 4 + rem] : 0u;
       }
-      if (t < SVC_TILE) et[t] = t < tile ? eq_lo[(xt + t) & (chunk - 1)] : f128_zero();
+      if (t < SVC_TILE) et[t] = t < cur ? eq_lo[(xt + t) & (chunk - 1)] : f128_zero();
       __syncthreads();
       {
         const uint32_t q = t >> 4, v = t & 15;  // 128 threads: one nibble-table entry each
@@ -329,23 +334,26 @@ void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t mulk[
   g_zc_consts_dev[dev] = d;
 }
 
-void launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32_t m, const F128d* eq_lo, uint32_t lo_bits,
-                      const F128d* eq_hi, F128d* part_ab, uint32_t* nrows_ab, F128d* part_svc, uint32_t* nrows_svc,
-                      cudaStream_t s) {
+void launch_zc_round1(const F128d* a, const F128d* b, const F128d* z, uint32_t m, uint64_t live_words,
+                      const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* part_ab, uint32_t* nrows_ab,
+                      F128d* part_svc, uint32_t* nrows_svc, cudaStream_t s) {
   ZcConsts* g_zc_consts = zc_consts();
   if (!g_zc_consts) throw std::runtime_error("zerocheck constants not uploaded");
   uint64_t n_xo = 1ull << (m - 13);
+  // xo past the live words hold zero rows of z, a and b and add nothing to any sum
+  const uint64_t xo_live = std::min<uint64_t>(n_xo, (live_words + 63) / 64);
   size_t smem = ZC_CONST_BYTES;
   set_dynamic_smem((const void*)zc_round1_ab_kernel, (int)smem);
-  uint32_t blocks = (uint32_t)std::min<uint64_t>((n_xo + ZC_TEAMS - 1) / ZC_TEAMS, (uint64_t)sm_count());
-  zc_round1_ab_kernel<<<blocks, 16 * ZC_TEAMS, smem, s>>>(a, b, n_xo, g_zc_consts, eq_lo, lo_bits, eq_hi, part_ab);
+  uint32_t blocks = (uint32_t)std::max<uint64_t>(
+      1, std::min<uint64_t>((xo_live + ZC_TEAMS - 1) / ZC_TEAMS, (uint64_t)sm_count()));
+  zc_round1_ab_kernel<<<blocks, 16 * ZC_TEAMS, smem, s>>>(a, b, xo_live, g_zc_consts, eq_lo, lo_bits, eq_hi, part_ab);
   LAUNCH_OK();
   *nrows_ab = blocks * ZC_TEAMS;
   // at most 256 runs of xo per word group (n_xo and the chunks are powers of two)
   const uint64_t runs = std::min<uint64_t>(n_xo, 256);
   const uint64_t run = n_xo / runs;
-  zc_svc_kernel<<<dim3((uint32_t)runs, 64 / SVC_WORDS), 128, 0, s>>>(z, run, g_zc_consts, eq_lo, lo_bits, eq_hi,
-                                                                   part_svc);
+  zc_svc_kernel<<<dim3((uint32_t)runs, 64 / SVC_WORDS), 128, 0, s>>>(z, run, xo_live, g_zc_consts, eq_lo, lo_bits,
+                                                                   eq_hi, part_svc);
   LAUNCH_OK();
   *nrows_svc = (uint32_t)(runs * (64 / SVC_WORDS));
 }
@@ -498,8 +506,9 @@ __global__ void zc_scaled_tables_kernel(const F128d* __restrict__ w64, F128d rho
 }
 __global__ void __launch_bounds__(256)
 zc_fold2_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, const F128d* __restrict__ tabs,
-                uint64_t n_pairs, const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F128d* __restrict__ eq_hi,
-                F128d* __restrict__ aout, F128d* __restrict__ bout, F128d* __restrict__ part) {
+                uint64_t n_pairs, uint64_t live_pairs, const F128d* __restrict__ eq_lo, uint32_t lo_bits,
+                const F128d* __restrict__ eq_hi, F128d* __restrict__ aout, F128d* __restrict__ bout,
+                F128d* __restrict__ part) {
   extern __shared__ __align__(16) F128d T[];  // [2][8][256]: (1 + rho) w tables, then rho w tables
   __shared__ F128d sh[32];
   for (uint32_t e = threadIdx.x; e < 4096; e += blockDim.x) T[e] = tabs[e];
@@ -513,6 +522,10 @@ zc_fold2_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, const 
     F128d g1 = f128_zero(), gi = f128_zero();
     uint64_t end = min(n_pairs, (ch + 1) * chunk);
     for (uint64_t j = ch * chunk + threadIdx.x; j < end; j += blockDim.x) {
+      if (j >= live_pairs) {  // zero words: zero outputs, nothing added to the message
+        aout[2 * j] = aout[2 * j + 1] = bout[2 * j] = bout[2 * j + 1] = f128_zero();
+        continue;
+      }
       F128d A[2], B[2];
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
@@ -543,14 +556,16 @@ zc_fold2_kernel(const F128d* __restrict__ a, const F128d* __restrict__ b, const 
   if (threadIdx.x == 0) { part[blockIdx.x * 2] = G1; part[blockIdx.x * 2 + 1] = GI; }
 }
 uint32_t launch_zc_fold2(const F128d* a, const F128d* b, const F128d* w64, F128d rho, F128d* tabs, uint64_t n_pairs,
-                         const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* aout, F128d* bout, F128d* part,
-                         cudaStream_t s) {
+                         uint64_t live_pairs, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* aout,
+                         F128d* bout, F128d* part, cudaStream_t s) {
+  live_pairs = std::min(live_pairs, n_pairs);
   zc_scaled_tables_kernel<<<16, 256, 0, s>>>(w64, rho, tabs);
   LAUNCH_OK();
   set_dynamic_smem((const void*)zc_fold2_kernel, 4096 * 16);
   uint64_t n_chunks = (n_pairs + (1ull << lo_bits) - 1) >> lo_bits;
   uint32_t blocks = (uint32_t)std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 3);
-  zc_fold2_kernel<<<blocks, 256, 4096 * 16, s>>>(a, b, tabs, n_pairs, eq_lo, lo_bits, eq_hi, aout, bout, part);
+  zc_fold2_kernel<<<blocks, 256, 4096 * 16, s>>>(a, b, tabs, n_pairs, live_pairs, eq_lo, lo_bits, eq_hi, aout, bout,
+                                                  part);
   LAUNCH_OK();
   return blocks;
 }
@@ -606,9 +621,10 @@ constexpr uint64_t PAIR_FOLD_TABLE_MIN_BLOCK_PAIRS = 512;
 // to pay for that. Otherwise r is split once per block for mul_split.
 template <bool TBL>
 __global__ void __launch_bounds__(256, TBL ? 3 : 2)
-pair_fold_kernel(const F128d* __restrict__ ain, const F128d* __restrict__ bin, uint64_t n_pairs, F128d r,
-                 const F128d* __restrict__ r_dev, const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F128d* __restrict__ eq_hi,
-                 F128d* __restrict__ aout, F128d* __restrict__ bout, F128d* __restrict__ part, int msg, FusedPublish pub) {
+pair_fold_kernel(const F128d* __restrict__ ain, const F128d* __restrict__ bin, uint64_t n_pairs, uint64_t live_pairs,
+                 F128d r, const F128d* __restrict__ r_dev, const F128d* __restrict__ eq_lo, uint32_t lo_bits,
+                 const F128d* __restrict__ eq_hi, F128d* __restrict__ aout, F128d* __restrict__ bout,
+                 F128d* __restrict__ part, int msg, FusedPublish pub) {
   extern __shared__ __align__(16) F128d rtab[];  // TBL: build_byte_table's BYTE_TABLE_SMEM_ENTRIES
   __shared__ F128d sh[32];
   __shared__ F128split rs;  // the fold challenge, split once
@@ -626,6 +642,10 @@ pair_fold_kernel(const F128d* __restrict__ ain, const F128d* __restrict__ bin, u
     F128d g1 = f128_zero(), gi = f128_zero();
     uint64_t end = min(n_pairs, (ch + 1) * chunk);
     for (uint64_t j = ch * chunk + threadIdx.x; j < end; j += blockDim.x) {
+      if (j >= live_pairs) {  // zero inputs: zero outputs, nothing added to the message
+        aout[2 * j] = aout[2 * j + 1] = bout[2 * j] = bout[2 * j + 1] = f128_zero();
+        continue;
+      }
       F128d x0 = ain[4 * j], x1 = ain[4 * j + 1], x2 = ain[4 * j + 2], x3 = ain[4 * j + 3];
       F128d y0 = bin[4 * j], y1 = bin[4 * j + 1], y2 = bin[4 * j + 2], y3 = bin[4 * j + 3];
       F128d A0 = x0 + by_r(x1 + x0), A1 = x2 + by_r(x3 + x2);
@@ -656,9 +676,10 @@ pair_fold_kernel(const F128d* __restrict__ ain, const F128d* __restrict__ bin, u
   if (msg && threadIdx.x == 0) { part[blockIdx.x * 2] = G1; part[blockIdx.x * 2 + 1] = GI; }
   if (msg && pub.out) publish_if_last(part, 2, pub, sh);
 }
-uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, F128d r, const F128d* r_dev,
-                          const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* aout, F128d* bout,
-                          F128d* part, bool msg, cudaStream_t s, FusedPublish pub) {
+uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, uint64_t live_pairs, F128d r,
+                          const F128d* r_dev, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, F128d* aout,
+                          F128d* bout, F128d* part, bool msg, cudaStream_t s, FusedPublish pub) {
+  live_pairs = std::min(live_pairs, n_pairs);
   uint64_t n_chunks = (n_pairs + (1ull << lo_bits) - 1) >> lo_bits;
   if (n_pairs >= PAIR_FOLD_TABLE_MIN_PAIRS) {
     // three resident blocks per SM (74 KB of shared memory each), each building its table
@@ -667,14 +688,14 @@ uint32_t launch_pair_fold(const F128d* ain, const F128d* bin, uint64_t n_pairs, 
     set_dynamic_smem((const void*)pair_fold_kernel<true>, smem);
     uint32_t blocks = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 6),
                                                    n_pairs / PAIR_FOLD_TABLE_MIN_BLOCK_PAIRS);
-    pair_fold_kernel<true><<<blocks, 256, smem, s>>>(ain, bin, n_pairs, r, r_dev, eq_lo, lo_bits, eq_hi, aout, bout,
-                                                     part, msg ? 1 : 0, pub);
+    pair_fold_kernel<true><<<blocks, 256, smem, s>>>(ain, bin, n_pairs, live_pairs, r, r_dev, eq_lo, lo_bits, eq_hi,
+                                                     aout, bout, part, msg ? 1 : 0, pub);
     LAUNCH_OK();
     return blocks;
   }
   uint32_t blocks = (uint32_t)std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 8);
-  pair_fold_kernel<false><<<blocks, 256, 0, s>>>(ain, bin, n_pairs, r, r_dev, eq_lo, lo_bits, eq_hi, aout, bout, part,
-                                                 msg ? 1 : 0, pub);
+  pair_fold_kernel<false><<<blocks, 256, 0, s>>>(ain, bin, n_pairs, live_pairs, r, r_dev, eq_lo, lo_bits, eq_hi, aout,
+                                                 bout, part, msg ? 1 : 0, pub);
   LAUNCH_OK();
   return blocks;
 }
