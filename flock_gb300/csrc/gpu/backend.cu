@@ -815,6 +815,7 @@ void GpuBackend::mo_build_w(const std::vector<WeightClaim>& cl, uint32_t nu, uin
   mo_q_ = q_;
   mo_w_ = mw_;
   mo_len_ = Q_;
+  mo_live_ = std::min<uint64_t>(Q_, area);
 }
 
 void GpuBackend::mo_round(F128 r, bool last, F128& g1, F128& gi) {
@@ -827,17 +828,19 @@ void GpuBackend::mo_round(F128 r, bool last, F128& g1, F128& gi) {
   F128d* oq = (mo_q_ == moAq_) ? moBq_ : moAq_;
   F128d* ow = (mo_q_ == moAq_) ? moBw_ : moAw_;
   uint64_t n_pairs = mo_len_ / 4;
+  const uint64_t live_pairs = std::min<uint64_t>(n_pairs, (mo_live_ + 3) / 4);
   uint32_t chunk_bits = std::min<uint32_t>(10, ceil_log2(n_pairs));  // chunking only sets the work split
   FusedPublish fp;
   if (!last) fp = fused_publish();
   {
     Mark mk(this, ST_MO_ROUNDS);
-    launch_pair_fold(mo_q_, mo_w_, n_pairs, n_pairs, dev(r), nullptr, nullptr, chunk_bits, nullptr, oq, ow, part_, !last,
-                     st_, fp);
+    launch_pair_fold(mo_q_, mo_w_, n_pairs, live_pairs, dev(r), nullptr, nullptr, chunk_bits, nullptr, oq, ow, part_,
+                     !last, st_, fp);
   }
   mo_q_ = oq;
   mo_w_ = ow;
   mo_len_ /= 2;
+  mo_live_ = std::min(mo_len_, 2 * live_pairs);
   if (!last) {
     auto v = read_published(fp.seq, 2);
     g1 = v[0];
@@ -869,7 +872,8 @@ F128 GpuBackend::lg_eval_eq(const std::vector<F128>& zp) {
   // chunks of 2^13 words (one eq_hi table each) where there are enough of them for every SM
   EqSplit e = eq_split(zp, F128::one(), (Q_ >> 13) >= (uint64_t)sm_count() ? 13 : 10);
   uint32_t nb;
-  { Mark mk(this, ST_LIGERITO); nb = launch_lg_dot_eq(q_, 1, e.lo, e.lo_bits, e.hi, Q_, part_, st_); }
+  // q is zero from the dense words on (the zero tail of the committed vector)
+  { Mark mk(this, ST_LIGERITO); nb = launch_lg_dot_eq(q_, 1, e.lo, e.lo_bits, e.hi, Q_, S.dense_words, part_, st_); }
   return reduce(nb, 1)[0];
 }
 

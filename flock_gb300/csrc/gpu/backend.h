@@ -170,6 +170,7 @@ class GpuBackend : public ProverBackend {
   const F128d* mo_q_ = nullptr;
   const F128d* mo_w_ = nullptr;
   uint64_t mo_len_ = 0;
+  uint64_t mo_live_ = 0;  // entries of q and W that can be nonzero (both are zero from the area on)
   F128 mo_final_;
 
   F128d* lb128_ = nullptr;

@@ -132,7 +132,7 @@ uint32_t launch_mo_build_w(const F128d* q, const F128d* er0, const F128d* ec0, c
 void launch_lg_eq_fill(const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, uint64_t n, F128d* out, bool add,
                        cudaStream_t s);
 uint32_t launch_lg_dot_eq(const F128d* f, uint32_t stride, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi,
-                          uint64_t n, F128d* part, cudaStream_t s);                                    // width 1
+                          uint64_t n, uint64_t live, F128d* part, cudaStream_t s);  // f zero from `live` on                                    // width 1
 uint32_t launch_lg_message128(const F128d* f, const F128d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s,
                               FusedPublish pub = FusedPublish());
 uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s,

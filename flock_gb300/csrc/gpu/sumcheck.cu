@@ -1062,6 +1062,10 @@ mo_build_w_kernel(const F128d* __restrict__ q, const F128d* __restrict__ er0, co
   const uint64_t rmask = (1ull << nu) - 1;
   F128d u0 = f128_zero(), u2 = f128_zero();
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n / 2; i += (uint64_t)gridDim.x * blockDim.x) {
+    if (2 * i >= area) {  // q and W are zero from the area on
+      w[2 * i] = w[2 * i + 1] = f128_zero();
+      continue;
+    }
     F128d W[2];
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
@@ -1100,8 +1104,12 @@ mo_build_w_cols_kernel(const F128d* __restrict__ q, const F128d* __restrict__ er
   for (uint64_t it = blockIdx.x; it < items; it += gridDim.x) {
     const uint64_t col = it >> part_log, d0 = (col << nu) + ((it & ((1ull << part_log) - 1)) << (nu - part_log));
     const bool used = d0 < area;  // block-uniform
+    if (!used) {  // q and W are zero from the area on: zero weights, nothing added to the message
+      for (uint64_t j = threadIdx.x; j < rows; j += blockDim.x) w[d0 + j] = f128_zero();
+      continue;
+    }
     __syncthreads();  // the previous item's tables are no longer read
-    if (used) {
+    {
       // M0's images (its scratch lies inside M1's table), then M1's
       if (threadIdx.x < 128) byte_table_images(T0)[threadIdx.x] = fold_slot(mul_call(ec0[col], unit_power(threadIdx.x)), tables);
       __syncthreads();
@@ -1114,8 +1122,8 @@ mo_build_w_cols_kernel(const F128d* __restrict__ q, const F128d* __restrict__ er
     for (uint64_t j = threadIdx.x; j < rows / 2; j += blockDim.x) {
       const uint64_t d = d0 + 2 * j, row = d & ((1ull << nu) - 1);
       F128d W0 = f128_zero(), W1 = f128_zero();
-      if (used && d < area) W0 = mul_table(er0[row], T0) + mul_table(er1[row], T1);
-      if (used && d + 1 < area) W1 = mul_table(er0[row + 1], T0) + mul_table(er1[row + 1], T1);
+      if (d < area) W0 = mul_table(er0[row], T0) + mul_table(er1[row], T1);
+      if (d + 1 < area) W1 = mul_table(er0[row + 1], T0) + mul_table(er1[row + 1], T1);
       w[d] = W0;
       w[d + 1] = W1;
       const F128d q0 = q[d], q1 = q[d + 1];
@@ -1267,10 +1275,11 @@ lg_dot_eq_tbl_kernel(const F128d* __restrict__ f, const F128d* __restrict__ eq_l
   if (threadIdx.x == 0) part[blockIdx.x] = g;
 }
 uint32_t launch_lg_dot_eq(const F128d* f, uint32_t stride, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi,
-                          uint64_t n, F128d* part, cudaStream_t s) {
+                          uint64_t n, uint64_t live, F128d* part, cudaStream_t s) {
+  live = std::min(live, n);  // f is zero from `live` on
   if (stride == 1 && eq_hi && lo_bits == DOT_EQ_TBL_LO_BITS && (n & ((1ull << lo_bits) - 1)) == 0 &&
       (n >> lo_bits) >= (uint64_t)sm_count()) {
-    const uint64_t n_chunks = n >> lo_bits;
+    const uint64_t n_chunks = std::max<uint64_t>(1, (live + (1ull << lo_bits) - 1) >> lo_bits);
     const uint32_t blocks = (uint32_t)sm_count();
     const int smem = (int)(BYTE_TABLE_SMEM_ENTRIES * sizeof(F128d));
     set_dynamic_smem((const void*)lg_dot_eq_tbl_kernel, smem);
@@ -1278,6 +1287,7 @@ uint32_t launch_lg_dot_eq(const F128d* f, uint32_t stride, const F128d* eq_lo, u
     LAUNCH_OK();
     return blocks;
   }
+  n = std::max<uint64_t>(live, 1);
   uint64_t n_chunks = (n + (1ull << lo_bits) - 1) >> lo_bits;
   uint32_t blocks = (uint32_t)std::min<uint64_t>(n_chunks, (uint64_t)sm_count() * 8);
   lg_dot_eq_kernel<<<blocks, 256, 0, s>>>(f, stride, eq_lo, lo_bits, eq_hi, n, part);
