@@ -862,6 +862,7 @@ void GpuBackend::lg_basis_eq(F128 gamma, const std::vector<F128>& rho) {
   { Mark mk(this, ST_LIGERITO); launch_lg_eq_fill(e.lo, e.lo_bits, e.hi, Q_, lb128_, false, st_); }
   lg_base_ = true;
   lg_n_ = Q_;
+  lg_live_ = std::min<uint64_t>(Q_, S.dense_words);  // q is zero from the dense words on
   lg_cur_ = 0;
 }
 
@@ -893,10 +894,11 @@ Msg256 GpuBackend::lg_message(size_t d) {
     FusedPublish fp = fused_publish();
     {
       Mark mk(this, ST_LIGERITO);
-      launch_lg_switch_msg(lf_[lg_cur_], lb_[lg_cur_], lg_n_, lf_[nx], lb_[nx], part_, st_, fp);
+      launch_lg_switch_msg(lf_[lg_cur_], lb_[lg_cur_], lg_n_, lg_live_, lf_[nx], lb_[nx], part_, st_, fp);
     }
     lg_cur_ = nx;
     lg_n_ *= 2;
+    lg_live_ = std::min(lg_n_, 2 * lg_live_);
     auto v = read_published(fp.seq, 4);
     Msg256 m;
     m.u0 = F256(v[0], v[1]);
@@ -913,16 +915,17 @@ Msg256 GpuBackend::lg_message(size_t d) {
     {
       Mark mk(this, ST_LIGERITO);
       if (lg_pend_fold_.base)
-        launch_lg_fold_msg128(q_, lb128_, n_out, dev(lg_pend_fold_.r), lg_pend_fold_.d, dm, lf_[0], lb_[0], part_, st_,
-                              fp);
+        launch_lg_fold_msg128(q_, lb128_, n_out, lg_live_, dev(lg_pend_fold_.r), lg_pend_fold_.d, dm, lf_[0], lb_[0],
+                              part_, st_, fp);
       else
-        launch_lg_fold_msg256(lf_[lg_cur_], lb_[lg_cur_], n_out, dev(lg_pend_fold_.r), lg_pend_fold_.d, dm, lf_[nx],
-                              lb_[nx], part_, st_, fp);
+        launch_lg_fold_msg256(lf_[lg_cur_], lb_[lg_cur_], n_out, lg_live_, dev(lg_pend_fold_.r), lg_pend_fold_.d, dm,
+                              lf_[nx], lb_[nx], part_, st_, fp);
     }
     if (lg_pend_fold_.base) lg_base_ = false;
     lg_pend_fold_.active = false;
     lg_cur_ = nx;
     lg_n_ = n_out;
+    lg_live_ = fold_live(lg_live_, lg_pend_fold_.d);
     auto v = read_published(fp.seq, 4);
     Msg256 m;
     m.u0 = F256(v[0], v[1]);
@@ -934,13 +937,13 @@ Msg256 GpuBackend::lg_message(size_t d) {
   Msg256 m;
   if (lg_base_) {
     FusedPublish fp = fused_publish();
-    { Mark mk(this, ST_LIGERITO); launch_lg_message128(q_, lb128_, n, d, part_, st_, fp); }
+    { Mark mk(this, ST_LIGERITO); launch_lg_message128(q_, lb128_, n, lg_live_, d, part_, st_, fp); }
     auto v = read_published(fp.seq, 2);
     m.u0 = F256(v[0]);
     m.u2 = F256(v[1]);
   } else {
     FusedPublish fp = fused_publish();
-    { Mark mk(this, ST_LIGERITO); launch_lg_message256(lf_[lg_cur_], lb_[lg_cur_], n, d, part_, st_, fp); }
+    { Mark mk(this, ST_LIGERITO); launch_lg_message256(lf_[lg_cur_], lb_[lg_cur_], n, lg_live_, d, part_, st_, fp); }
     auto v = read_published(fp.seq, 4);
     m.u0 = F256(v[0], v[1]);
     m.u2 = F256(v[2], v[3]);
@@ -958,6 +961,7 @@ void GpuBackend::lg_flush_fold() {
     }
     lg_cur_ = nx;
     lg_n_ *= 2;
+    lg_live_ = std::min(lg_n_, 2 * lg_live_);
   }
   if (!lg_pend_fold_.active) return;
   lg_pend_fold_.active = false;
@@ -970,6 +974,7 @@ void GpuBackend::lg_flush_fold() {
     lg_cur_ = 0;
     lg_base_ = false;
     lg_n_ = n_out;
+    lg_live_ = fold_live(lg_live_, lg_pend_fold_.d);
     return;
   }
   const int nx = lg_cur_ ^ 1;
@@ -980,6 +985,7 @@ void GpuBackend::lg_flush_fold() {
   }
   lg_cur_ = nx;
   lg_n_ = n_out;
+  lg_live_ = fold_live(lg_live_, lg_pend_fold_.d);
 }
 
 void GpuBackend::lg_fold(F256 r, size_t d) {

@@ -192,6 +192,12 @@ class GpuBackend : public ProverBackend {
   bool lg_pend_switch_ = false;
   void lg_flush_fold();
   uint64_t lg_n_ = 0;
+  // f (the folded committed vector) is zero from entry lg_live_ on: the committed vector's
+  // zero tail, halved through the folds, doubled by the code switch
+  uint64_t lg_live_ = 0;
+  static uint64_t fold_live(uint64_t live, uint64_t d) {  // output i is live when f[pair_lo(i, d)] may be nonzero
+    return (live / (2 * d)) * d + std::min<uint64_t>(d, live % (2 * d));
+  }
   F128d* pend_ = nullptr;
   bool pend_induced_ = false;
   uint64_t pend_n_ = 0;

@@ -133,26 +133,29 @@ void launch_lg_eq_fill(const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi,
                        cudaStream_t s);
 uint32_t launch_lg_dot_eq(const F128d* f, uint32_t stride, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi,
                           uint64_t n, uint64_t live, F128d* part, cudaStream_t s);  // f zero from `live` on                                    // width 1
-uint32_t launch_lg_message128(const F128d* f, const F128d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s,
-                              FusedPublish pub = FusedPublish());
-uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s,
-                              FusedPublish pub = FusedPublish());
+// f_live: f is zero from that entry on (pairs wholly past it add nothing and are skipped).
+uint32_t launch_lg_message128(const F128d* f, const F128d* b, uint64_t n, uint64_t f_live, uint64_t d, F128d* part,
+                              cudaStream_t s, FusedPublish pub = FusedPublish());
+uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64_t f_live, uint64_t d, F128d* part,
+                              cudaStream_t s, FusedPublish pub = FusedPublish());
 void launch_lg_fold128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, const F256d* r_dev, uint64_t d,
                        F256d* fo, F256d* bo, cudaStream_t s);
 // The first fold (of the base vectors into F256 vectors) fused with the next message,
 // like launch_lg_fold_msg256.
-uint32_t launch_lg_fold_msg128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, uint64_t d_fold, uint64_t d_msg,
-                               F256d* fo, F256d* bo, F128d* part, cudaStream_t s, FusedPublish pub);
-uint32_t launch_lg_fold_msg256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, uint64_t d_fold, uint64_t d_msg,
-                               F256d* fo, F256d* bo, F128d* part, cudaStream_t s,
+// f_live: the input f is zero from that entry on; message pairs whose inputs all lie past
+// it fold only b (their f outputs are written as zero) and add nothing to the message.
+uint32_t launch_lg_fold_msg128(const F128d* f, const F128d* b, uint64_t n_out, uint64_t f_live, F256d r, uint64_t d_fold,
+                               uint64_t d_msg, F256d* fo, F256d* bo, F128d* part, cudaStream_t s, FusedPublish pub);
+uint32_t launch_lg_fold_msg256(const F256d* f, const F256d* b, uint64_t n_out, uint64_t f_live, F256d r, uint64_t d_fold,
+                               uint64_t d_msg, F256d* fo, F256d* bo, F128d* part, cudaStream_t s,
                                FusedPublish pub = FusedPublish());                                  // width 4
 void launch_lg_fold256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, const F256d* r_dev, uint64_t d,
                        F256d* fo, F256d* bo, cudaStream_t s);
 void launch_lg_code_switch(const F256d* f, const F256d* b, uint64_t n, F256d* fo, F256d* bo, cudaStream_t s);
 // The code switch and the round message over the switched vectors with pairs one apart,
 // in one pass; published like launch_lg_message256 (four words).
-uint32_t launch_lg_switch_msg(const F256d* f, const F256d* b, uint64_t n, F256d* fo, F256d* bo, F128d* part,
-                              cudaStream_t s, FusedPublish pub);
+uint32_t launch_lg_switch_msg(const F256d* f, const F256d* b, uint64_t n, uint64_t f_live, F256d* fo, F256d* bo,
+                              F128d* part, cudaStream_t s, FusedPublish pub);
 void launch_lg_replicate(const F256d* f, uint64_t msg, uint64_t total, F128d* mat, cudaStream_t s);
 uint32_t launch_lg_intro_eq(const F256d* f, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, uint64_t n,
                             F128d* pend, F128d* part, cudaStream_t s,

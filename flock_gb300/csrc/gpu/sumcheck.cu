@@ -1308,12 +1308,13 @@ static uint32_t log2_distance(uint64_t d) {
 __device__ __forceinline__ uint64_t pair_lo(uint64_t i, uint32_t d_log) {
   return ((i >> d_log) << (d_log + 1)) | (i & ((1ull << d_log) - 1));
 }
-__global__ void lg_message128_kernel(const F128d* __restrict__ f, const F128d* __restrict__ b, uint64_t n, uint32_t d_log,
-                                     F128d* __restrict__ part, FusedPublish pub) {
+__global__ void lg_message128_kernel(const F128d* __restrict__ f, const F128d* __restrict__ b, uint64_t n, uint64_t f_live,
+                                     uint32_t d_log, F128d* __restrict__ part, FusedPublish pub) {
   __shared__ F128d sh[32];
   F128d u0 = f128_zero(), u2 = f128_zero();
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n / 2; p += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t lo = pair_lo(p, d_log), hi = lo + (1ull << d_log);
+    if (lo >= f_live) continue;  // f[lo] = f[hi] = 0: the pair adds nothing
     F128d f0 = f[lo], f1 = f[hi], b0 = b[lo], b1 = b[hi];
     u0 += f0 * b0;
     u2 += (f0 + f1) * (b0 + b1);
@@ -1323,19 +1324,20 @@ __global__ void lg_message128_kernel(const F128d* __restrict__ f, const F128d* _
   if (threadIdx.x == 0) { part[blockIdx.x * 2] = u0; part[blockIdx.x * 2 + 1] = u2; }
   if (pub.out) publish_if_last(part, 2, pub, sh);
 }
-uint32_t launch_lg_message128(const F128d* f, const F128d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s,
-                              FusedPublish pub) {
+uint32_t launch_lg_message128(const F128d* f, const F128d* b, uint64_t n, uint64_t f_live, uint64_t d, F128d* part,
+                              cudaStream_t s, FusedPublish pub) {
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n / 2 + 255) / 256, (uint64_t)sm_count() * 8));
-  lg_message128_kernel<<<blocks, 256, 0, s>>>(f, b, n, log2_distance(d), part, pub);
+  lg_message128_kernel<<<blocks, 256, 0, s>>>(f, b, n, f_live, log2_distance(d), part, pub);
   LAUNCH_OK();
   return blocks;
 }
-__global__ void lg_message256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n, uint32_t d_log,
-                                     F128d* __restrict__ part, FusedPublish pub) {
+__global__ void lg_message256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n, uint64_t f_live,
+                                     uint32_t d_log, F128d* __restrict__ part, FusedPublish pub) {
   __shared__ F128d sh[32];
   F256d u0 = f256(f128_zero(), f128_zero()), u2 = u0;
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n / 2; p += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t lo = pair_lo(p, d_log), hi = lo + (1ull << d_log);
+    if (lo >= f_live) continue;  // f[lo] = f[hi] = 0: the pair adds nothing
     F256d f0 = f[lo], f1 = f[hi], b0 = b[lo], b1 = b[hi];
     u0 += f256_mul_call(f0, b0);
     u2 += f256_mul_call(f0 + f1, b0 + b1);
@@ -1347,10 +1349,10 @@ __global__ void lg_message256_kernel(const F256d* __restrict__ f, const F256d* _
   }
   if (pub.out) publish_if_last(part, 4, pub, sh);
 }
-uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64_t d, F128d* part, cudaStream_t s,
-                              FusedPublish pub) {
+uint32_t launch_lg_message256(const F256d* f, const F256d* b, uint64_t n, uint64_t f_live, uint64_t d, F128d* part,
+                              cudaStream_t s, FusedPublish pub) {
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n / 2 + 255) / 256, (uint64_t)sm_count() * 8));
-  lg_message256_kernel<<<blocks, 256, 0, s>>>(f, b, n, log2_distance(d), part, pub);
+  lg_message256_kernel<<<blocks, 256, 0, s>>>(f, b, n, f_live, log2_distance(d), part, pub);
   LAUNCH_OK();
   return blocks;
 }
@@ -1414,7 +1416,7 @@ __device__ __forceinline__ void lg_fold_at(const F256d* __restrict__ f, const F2
 // 512-thread block per SM holds the two tables (141 KB).
 template <bool TBL>
 __global__ void __launch_bounds__(TBL ? 512 : 256, TBL ? 1 : 2)
-lg_fold_msg256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n_out, F256d r,
+lg_fold_msg256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n_out, uint64_t f_live, F256d r,
                       uint32_t dlog_fold, uint32_t dlog_msg, F256d* __restrict__ fo, F256d* __restrict__ bo,
                       F128d* __restrict__ part, FusedPublish pub) {
   extern __shared__ __align__(16) F128d rtab[];  // TBL: tables of r.c0 and r.c1
@@ -1442,9 +1444,26 @@ lg_fold_msg256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, 
       lg_fold_at(f, b, r, dlog_fold, i, fi, bi);
     }
   };
+  auto fold_b_at = [&](uint64_t i) {  // f is zero at both inputs of i: only b folds
+    const uint64_t lo = pair_lo(i, dlog_fold), hi = lo + (1ull << dlog_fold);
+    const F256d b0 = b[lo], db = b[hi] + b0;
+    fo[i] = f256(f128_zero(), f128_zero());
+    if (TBL) {
+      const F128d p0 = mul_table(db.c0, rtab), p1 = mul_table(db.c1, rtab + BYTE_TABLE_ENTRIES),
+                  p2 = mul_split_call(db.c0 + db.c1, &rsum);
+      bo[i] = b0 + f256(p0 + mul_by_x_inv(p1), p2 + p0);
+    } else {
+      bo[i] = b0 + f256_mul_call(r, db);
+    }
+  };
   F256d u0 = f256(f128_zero(), f128_zero()), u2 = u0;
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_out / 2; p += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t olo = pair_lo(p, dlog_msg), ohi = olo + (1ull << dlog_msg);
+    if (pair_lo(olo, dlog_fold) >= f_live) {  // f is zero at every input of both entries
+      fold_b_at(olo);
+      fold_b_at(ohi);
+      continue;
+    }
     F256d fl, bl, fh, bh;
     fold_at(olo, fl, bl);
     fo[olo] = fl;
@@ -1468,7 +1487,7 @@ lg_fold_msg256_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, 
 // F256 products of variables (6 F128 products) from integer multiplies. One 512-thread
 // block per SM holds the two tables.
 __global__ void __launch_bounds__(512, 1)
-lg_fold_msg128_kernel(const F128d* __restrict__ f, const F128d* __restrict__ b, uint64_t n_out, F256d r,
+lg_fold_msg128_kernel(const F128d* __restrict__ f, const F128d* __restrict__ b, uint64_t n_out, uint64_t f_live, F256d r,
                       uint32_t dlog_fold, uint32_t dlog_msg, F256d* __restrict__ fo, F256d* __restrict__ bo,
                       F128d* __restrict__ part, FusedPublish pub) {
   extern __shared__ __align__(16) F128d rtab[];  // tables of r.c0 and r.c1
@@ -1483,9 +1502,20 @@ lg_fold_msg128_kernel(const F128d* __restrict__ f, const F128d* __restrict__ b, 
     fi = f256(f0 + mul_table(df, T0), mul_table(df, T1));
     bi = f256(b0 + mul_table(db, T0), mul_table(db, T1));
   };
+  auto fold_b_at = [&](uint64_t i) {  // f is zero at both inputs of i: only b folds
+    const uint64_t lo = pair_lo(i, dlog_fold), hi = lo + (1ull << dlog_fold);
+    const F128d b0 = b[lo], db = b[hi] + b0;
+    fo[i] = f256(f128_zero(), f128_zero());
+    bo[i] = f256(b0 + mul_table(db, T0), mul_table(db, T1));
+  };
   F256d u0 = f256(f128_zero(), f128_zero()), u2 = u0;
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_out / 2; p += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t olo = pair_lo(p, dlog_msg), ohi = olo + (1ull << dlog_msg);
+    if (pair_lo(olo, dlog_fold) >= f_live) {  // f is zero at every input of both entries
+      fold_b_at(olo);
+      fold_b_at(ohi);
+      continue;
+    }
     F256d fl, bl, fh, bh;
     fold_at(olo, fl, bl);
     fo[olo] = fl;
@@ -1503,15 +1533,15 @@ lg_fold_msg128_kernel(const F128d* __restrict__ f, const F128d* __restrict__ b, 
   }
   if (pub.out) publish_if_last(part, 4, pub, sh);
 }
-uint32_t launch_lg_fold_msg128(const F128d* f, const F128d* b, uint64_t n_out, F256d r, uint64_t d_fold, uint64_t d_msg,
-                               F256d* fo, F256d* bo, F128d* part, cudaStream_t s, FusedPublish pub) {
+uint32_t launch_lg_fold_msg128(const F128d* f, const F128d* b, uint64_t n_out, uint64_t f_live, F256d r, uint64_t d_fold,
+                               uint64_t d_msg, F256d* fo, F256d* bo, F128d* part, cudaStream_t s, FusedPublish pub) {
   const int smem = (int)((BYTE_TABLE_ENTRIES + BYTE_TABLE_SMEM_ENTRIES) * sizeof(F128d));
   set_dynamic_smem((const void*)lg_fold_msg128_kernel, smem);
   // at least 512 message pairs per block for its two table builds
   const uint32_t blocks =
       (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sm_count(), n_out / 2 / 512));
-  lg_fold_msg128_kernel<<<blocks, 512, smem, s>>>(f, b, n_out, r, log2_distance(d_fold), log2_distance(d_msg), fo, bo,
-                                                   part, pub);
+  lg_fold_msg128_kernel<<<blocks, 512, smem, s>>>(f, b, n_out, f_live, r, log2_distance(d_fold), log2_distance(d_msg),
+                                                   fo, bo, part, pub);
   LAUNCH_OK();
   return blocks;
 }
@@ -1519,21 +1549,21 @@ uint32_t launch_lg_fold_msg128(const F128d* f, const F128d* b, uint64_t n_out, F
 // LG_FOLD_TABLE_MIN_BLOCK_PAIRS message pairs per block for its two table builds.
 constexpr uint64_t LG_FOLD_TABLE_MIN_OUT = uint64_t(1) << 17;
 constexpr uint64_t LG_FOLD_TABLE_MIN_BLOCK_PAIRS = 512;
-uint32_t launch_lg_fold_msg256(const F256d* f, const F256d* b, uint64_t n_out, F256d r, uint64_t d_fold, uint64_t d_msg,
-                               F256d* fo, F256d* bo, F128d* part, cudaStream_t s, FusedPublish pub) {
+uint32_t launch_lg_fold_msg256(const F256d* f, const F256d* b, uint64_t n_out, uint64_t f_live, F256d r, uint64_t d_fold,
+                               uint64_t d_msg, F256d* fo, F256d* bo, F128d* part, cudaStream_t s, FusedPublish pub) {
   if (n_out >= LG_FOLD_TABLE_MIN_OUT) {
     const int smem = (int)((BYTE_TABLE_ENTRIES + BYTE_TABLE_SMEM_ENTRIES) * sizeof(F128d));
     set_dynamic_smem((const void*)lg_fold_msg256_kernel<true>, smem);
     const uint32_t blocks = (uint32_t)std::max<uint64_t>(
         1, std::min<uint64_t>((uint64_t)sm_count(), n_out / 2 / LG_FOLD_TABLE_MIN_BLOCK_PAIRS));
-    lg_fold_msg256_kernel<true><<<blocks, 512, smem, s>>>(f, b, n_out, r, log2_distance(d_fold), log2_distance(d_msg),
-                                                          fo, bo, part, pub);
+    lg_fold_msg256_kernel<true><<<blocks, 512, smem, s>>>(f, b, n_out, f_live, r, log2_distance(d_fold),
+                                                          log2_distance(d_msg), fo, bo, part, pub);
     LAUNCH_OK();
     return blocks;
   }
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n_out / 2 + 255) / 256, (uint64_t)sm_count() * 8));
-  lg_fold_msg256_kernel<false><<<blocks, 256, 0, s>>>(f, b, n_out, r, log2_distance(d_fold), log2_distance(d_msg), fo,
-                                                      bo, part, pub);
+  lg_fold_msg256_kernel<false><<<blocks, 256, 0, s>>>(f, b, n_out, f_live, r, log2_distance(d_fold), log2_distance(d_msg),
+                                                      fo, bo, part, pub);
   LAUNCH_OK();
   return blocks;
 }
@@ -1558,7 +1588,7 @@ void launch_lg_code_switch(const F256d* f, const F256d* b, uint64_t n, F256d* fo
 //   u0 += f.c0 b = (f.c0 b.c0, f.c0 b.c1),
 //   u2 += (f.c0 + f.c1)(b + u b) = s (b.c0 + x^-1 b.c1, b.c0),  s = f.c0 + f.c1,
 // with u b = (x^-1 b.c1, b.c0 + b.c1) as the switch writes it.
-__global__ void lg_switch_msg_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n,
+__global__ void lg_switch_msg_kernel(const F256d* __restrict__ f, const F256d* __restrict__ b, uint64_t n, uint64_t f_live,
                                      F256d* __restrict__ fo, F256d* __restrict__ bo, F128d* __restrict__ part,
                                      FusedPublish pub) {
   __shared__ F128d sh[32];
@@ -1570,6 +1600,7 @@ __global__ void lg_switch_msg_kernel(const F256d* __restrict__ f, const F256d* _
     fo[2 * i + 1] = f256_base(fv.c1);
     bo[2 * i] = bv;
     bo[2 * i + 1] = f256(ub0, bv.c0 + bv.c1);
+    if (i >= f_live) continue;  // f[i] = 0: both products vanish
     const F128d sv = fv.c0 + fv.c1;
     u00 += mul_call(fv.c0, bv.c0);
     u01 += mul_call(fv.c0, bv.c1);
@@ -1583,10 +1614,10 @@ __global__ void lg_switch_msg_kernel(const F256d* __restrict__ f, const F256d* _
   }
   if (pub.out) publish_if_last(part, 4, pub, sh);
 }
-uint32_t launch_lg_switch_msg(const F256d* f, const F256d* b, uint64_t n, F256d* fo, F256d* bo, F128d* part,
-                              cudaStream_t s, FusedPublish pub) {
+uint32_t launch_lg_switch_msg(const F256d* f, const F256d* b, uint64_t n, uint64_t f_live, F256d* fo, F256d* bo,
+                              F128d* part, cudaStream_t s, FusedPublish pub) {
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, (uint64_t)sm_count() * 8));
-  lg_switch_msg_kernel<<<blocks, 256, 0, s>>>(f, b, n, fo, bo, part, pub);
+  lg_switch_msg_kernel<<<blocks, 256, 0, s>>>(f, b, n, f_live, fo, bo, part, pub);
   LAUNCH_OK();
   return blocks;
 }
