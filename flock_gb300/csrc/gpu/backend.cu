@@ -71,10 +71,16 @@ static T* dmalloc(size_t n, std::vector<void*>& owned, uint64_t& counter) {
 
 // Entries of the split eq tables of the skip fold (over L coordinates) and of every
 // later zerocheck fold round (over the suffixes of L - 1, L - 2, ..., 0 coordinates).
+// Round i splits its n = L - 1 - i coordinates as lo + hi with lo = zc_round_lo_bits(n).
+static uint32_t zc_round_lo_bits(uint32_t n) {
+  // chunks of 2^10 pairs where the round has enough of them for the table form, else of
+  // 2^8 (one pair per thread: four times the blocks of a small, latency-bound round)
+  return std::min(n, n >= 17 ? 10u : 8u);
+}
 static uint64_t zc_tables_entries(uint32_t L) {
   uint64_t total = (uint64_t(1) << 10) + (uint64_t(1) << (L - 10));
   for (uint32_t i = 0; i < L; ++i) {
-    uint32_t n = L - 1 - i, lo = std::min(n, 10u);
+    uint32_t n = L - 1 - i, lo = zc_round_lo_bits(n);
     total += (uint64_t(1) << lo) + (uint64_t(1) << (n - lo));
   }
   return total;
@@ -501,7 +507,7 @@ void GpuBackend::commit_l0(uint32_t cap_depth, std::vector<Hash>& cap) {
   }
   { Mark mk(this, ST_L0_FILL); launch_fill_lane_major(q_, cw0_, S.lanes, S.log_dim, S.k_code, st_); }
   { Mark mk(this, ST_L0_NTT); launch_ntt(cw0_, S.lanes, S.k_code, 1, tw0_, st_); }
-  { Mark mk(this, ST_L0_MERKLE); launch_merkle(cw0_, S.lanes, n_pos0_, tree0_, st_); }
+  { Mark mk(this, ST_L0_MERKLE); launch_merkle(cw0_, S.lanes, n_pos0_, cap_depth, tree0_, st_); }
   cap = read_cap(tree0_, n_pos0_, cap_depth);
 }
 
@@ -591,7 +597,7 @@ void GpuBackend::zc_fold_skip(const std::vector<F128>& w, const std::vector<F128
   add(0, 10);
   add(10, L - 10);
   for (uint32_t i = 0; i < L; ++i) {  // round i: eq over eq_point[1 + i ..), L - 1 - i coordinates
-    uint32_t n = L - 1 - i, lo = std::min(n, 10u);
+    uint32_t n = L - 1 - i, lo = zc_round_lo_bits(n);
     add(1 + i, lo);
     add(1 + i + lo, n - lo);
   }
@@ -829,7 +835,9 @@ void GpuBackend::mo_round(F128 r, bool last, F128& g1, F128& gi) {
   F128d* ow = (mo_q_ == moAq_) ? moBw_ : moAw_;
   uint64_t n_pairs = mo_len_ / 4;
   const uint64_t live_pairs = std::min<uint64_t>(n_pairs, (mo_live_ + 3) / 4);
-  uint32_t chunk_bits = std::min<uint32_t>(10, ceil_log2(n_pairs));  // chunking only sets the work split
+  // chunking only sets the work split: 2^10 pairs per chunk for the table form's rounds,
+  // 2^8 (one pair per thread) for the small, latency-bound ones
+  uint32_t chunk_bits = std::min<uint32_t>(n_pairs >= (uint64_t(1) << 17) ? 10 : 8, ceil_log2(n_pairs));
   FusedPublish fp;
   if (!last) fp = fused_publish();
   {
@@ -1027,7 +1035,7 @@ void GpuBackend::lg_commit(uint32_t level, uint32_t log_cols, uint32_t log_lanes
   const F128d* tw = twiddles(log_cols + log_rate);
   { Mark mk(this, ST_LIGERITO); launch_lg_replicate(lf_[lg_cur_], lg_n_, block_len * lanes, L.mat, st_); }
   { Mark mk(this, ST_LG_NTT); launch_ntt(L.mat, lanes, log_cols + log_rate, log_rate, tw, st_); }
-  { Mark mk(this, ST_LG_MERKLE); launch_merkle(L.mat, lanes, block_len, L.tree, st_); }
+  { Mark mk(this, ST_LG_MERKLE); launch_merkle(L.mat, lanes, block_len, cap_depth, L.tree, st_); }
   cap = read_cap(L.tree, block_len, cap_depth);
 }
 

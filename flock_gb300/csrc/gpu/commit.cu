@@ -348,12 +348,14 @@ __global__ void merkle_level_kernel(uint32_t* __restrict__ tree, uint64_t in_off
 #pragma unroll
   for (int k = 0; k < 8; ++k) tree[o * 8 + k] = out[k];
 }
-// The top of the tree, from a level of n_in <= MERKLE_TOP_NODES nodes up to the root, in
-// one block: each level's nodes are hashed by the block's threads, then a barrier.
+// The top of the tree, from a level of n_in <= MERKLE_TOP_NODES nodes up to the level of
+// n_cap nodes (the cap), in one block: each level's nodes are hashed by the block's
+// threads, then a barrier.
 constexpr uint32_t MERKLE_TOP_NODES = 2048;
-__global__ void __launch_bounds__(256) merkle_top_kernel(uint32_t* __restrict__ tree, uint64_t in_off, uint32_t n_in) {
+__global__ void __launch_bounds__(256) merkle_top_kernel(uint32_t* __restrict__ tree, uint64_t in_off, uint32_t n_in,
+                                                         uint32_t n_cap) {
   uint64_t off = in_off;
-  for (uint32_t len = n_in; len > 1; len /= 2) {
+  for (uint32_t len = n_in; len > n_cap; len /= 2) {
     const uint32_t nout = len / 2;
     for (uint32_t i = threadIdx.x; i < nout; i += blockDim.x) {
       const uint32_t* l = tree + (off + 2 * (uint64_t)i) * 8;
@@ -367,19 +369,23 @@ __global__ void __launch_bounds__(256) merkle_top_kernel(uint32_t* __restrict__ 
     off += len;
   }
 }
-void launch_merkle(const F128d* rows, uint32_t lanes, uint64_t n_leaves, uint8_t* tree, cudaStream_t s) {
+void launch_merkle(const F128d* rows, uint32_t lanes, uint64_t n_leaves, uint32_t cap_depth, uint8_t* tree,
+                   cudaStream_t s) {
+  // levels above the cap are never read (the cap is the commitment, paths stop below it)
+  const uint64_t n_cap = uint64_t(1) << cap_depth;
+  if (n_cap > n_leaves) throw std::runtime_error("Merkle cap wider than the leaf level");
   merkle_leaves_kernel<<<(unsigned)((n_leaves + 127) / 128), 128, 0, s>>>(rows, lanes, n_leaves, (uint32_t*)tree);
   LAUNCH_OK();
   uint64_t off = 0, len = n_leaves;
-  while (len > MERKLE_TOP_NODES) {
+  while (len > MERKLE_TOP_NODES && len > n_cap) {
     uint64_t nout = len / 2;
     merkle_level_kernel<<<(unsigned)((nout + 127) / 128), 128, 0, s>>>((uint32_t*)tree, off, nout);
     LAUNCH_OK();
     off += len;
     len = nout;
   }
-  if (len > 1) {
-    merkle_top_kernel<<<1, 256, 0, s>>>((uint32_t*)tree, off, (uint32_t)len);
+  if (len > n_cap) {
+    merkle_top_kernel<<<1, 256, 0, s>>>((uint32_t*)tree, off, (uint32_t)len, (uint32_t)n_cap);
     LAUNCH_OK();
   }
 }

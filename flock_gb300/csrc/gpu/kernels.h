@@ -45,7 +45,10 @@ void launch_witness(int hash, const void* d_inputs, uint32_t n_inst, uint32_t nu
 void launch_fill_lane_major(const F128d* q, F128d* cw, uint32_t lanes, uint32_t log_dim, uint32_t log_pos,
                             cudaStream_t s);
 void launch_ntt(F128d* data, uint32_t lanes, uint32_t log_d, uint32_t start_layer, const F128d* tw, cudaStream_t s);
-void launch_merkle(const F128d* rows, uint32_t lanes, uint64_t n_leaves, uint8_t* tree, cudaStream_t s);
+// Leaves and the levels up to the cap level (2^cap_depth nodes); the levels above it are
+// not computed.
+void launch_merkle(const F128d* rows, uint32_t lanes, uint64_t n_leaves, uint32_t cap_depth, uint8_t* tree,
+                   cudaStream_t s);
 void launch_pow(const uint32_t digest_le[8], uint32_t bits, uint64_t start, uint64_t count, unsigned long long* d_min,
                 uint32_t* d_counter, unsigned long long* out, uint32_t* flag, uint32_t seq, cudaStream_t s);
 void launch_gather_rows(const F128d* mat, uint32_t lanes, const uint64_t* d_pos, uint32_t n, F128d* out,

@@ -119,7 +119,7 @@ extern "C" int flock_gb300_commit_cap_noalloc(int hash_kind, const void* d_input
     launch_witness(hash_kind, d_inputs, (uint32_t)n_blocks, nu, z, a, b, (uint32_t)geo.used_cols, s);
     launch_fill_lane_major(z, cw, lanes, log_dim, k_code, s);
     launch_ntt(cw, lanes, k_code, 1, st.twiddles + (size_t(1) << k_code), s);
-    launch_merkle(cw, lanes, n_pos, tree, s);
+    launch_merkle(cw, lanes, n_pos, cap_depth, tree, s);
     CUDA_OK(cudaMemcpyAsync(cap_out, tree + (2 * n_pos - 2 * (uint64_t(1) << cap_depth)) * 32, cap_bytes,
                             cudaMemcpyDeviceToHost, s));
     CUDA_OK(cudaStreamSynchronize(s));
