@@ -417,8 +417,7 @@ GpuBackend::EqSplit GpuBackend::eq_split(const std::vector<F128>& point, F128 sc
   const F128d* dp = upload(point);
   F128d* lo = static_cast<F128d*>(scratch((size_t(16)) << e.lo_bits));
   F128d* hi = static_cast<F128d*>(scratch((size_t(16)) << hi_bits));
-  launch_eq_table(dp, e.lo_bits, dev(F128::one()), lo, st_);
-  launch_eq_table(dp + e.lo_bits, hi_bits, dev(scale), hi, st_);
+  launch_eq_split(dp, e.lo_bits, hi_bits, dev(scale), lo, hi, st_);
   e.lo = lo;
   e.hi = hi;
   return e;
@@ -430,8 +429,7 @@ GpuBackend::EqSplit GpuBackend::eq_split_dev(const F128d* dp, uint32_t n, F128 s
   uint32_t hi_bits = n - e.lo_bits;
   F128d* lo = static_cast<F128d*>(scratch((size_t(16)) << e.lo_bits));
   F128d* hi = static_cast<F128d*>(scratch((size_t(16)) << hi_bits));
-  launch_eq_table(dp, e.lo_bits, dev(F128::one()), lo, st_);
-  launch_eq_table(dp + e.lo_bits, hi_bits, dev(scale), hi, st_);
+  launch_eq_split(dp, e.lo_bits, hi_bits, dev(scale), lo, hi, st_);
   e.lo = lo;
   e.hi = hi;
   return e;
@@ -781,12 +779,14 @@ uint32_t GpuBackend::launch_build_w(const std::vector<WeightClaim>& cl, uint32_t
   F128d* er[2];
   F128d* ec[2];
   for (int i = 0; i < 2; ++i) {
-    const F128d* pr = upload(cl[i].z_row);
+    // the row and column tables of one claim in one launch, from the point (z_row | z_col)
+    std::vector<F128> rc(cl[i].z_row);
+    rc.insert(rc.end(), cl[i].z_col.begin(), cl[i].z_col.end());
+    const F128d* prc = upload(rc);
     er[i] = static_cast<F128d*>(scratch(size_t(16) << cl[i].z_row.size()));
-    launch_eq_table(pr, (uint32_t)cl[i].z_row.size(), dev(F128::one()), er[i], st_);
-    const F128d* pc = upload(cl[i].z_col);
     ec[i] = static_cast<F128d*>(scratch(size_t(16) << cl[i].z_col.size()));
-    launch_eq_table(pc, (uint32_t)cl[i].z_col.size(), dev(F128::one()), ec[i], st_);
+    launch_eq_split(prc, (uint32_t)cl[i].z_row.size(), (uint32_t)cl[i].z_col.size(), dev(F128::one()), er[i], ec[i],
+                    st_);
   }
   std::vector<F128> tabs(cl[0].table);
   tabs.insert(tabs.end(), cl[1].table.begin(), cl[1].table.end());

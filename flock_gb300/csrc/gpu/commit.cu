@@ -474,10 +474,11 @@ __global__ void gather_paths_kernel(const uint8_t* __restrict__ tree, uint64_t n
   while ((1ull << depth) < n_leaves) ++depth;
   uint32_t plen = depth - cap_depth;
   uint64_t start = 0, len = n_leaves, idx = pos[q];
-  for (uint32_t k = 0; k < plen; ++k) {
-    const uint8_t* src = tree + (start + (idx ^ 1)) * 32;
-    uint8_t* dst = out + ((uint64_t)q * plen + k) * 32;
-    for (int b = 0; b < 32; ++b) dst[b] = src[b];
+  for (uint32_t k = 0; k < plen; ++k) {  // 32-byte nodes: two 16-byte copies (tree and out are 16-byte aligned)
+    const uint4* src = reinterpret_cast<const uint4*>(tree + (start + (idx ^ 1)) * 32);
+    uint4* dst = reinterpret_cast<uint4*>(out + ((uint64_t)q * plen + k) * 32);
+    dst[0] = src[0];
+    dst[1] = src[1];
     start += len;
     len >>= 1;
     idx >>= 1;

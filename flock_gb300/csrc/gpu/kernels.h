@@ -59,6 +59,9 @@ void launch_gather_paths(const uint8_t* tree, uint64_t n_leaves, const uint64_t*
 // sumcheck.cu. Kernels returning a block count wrote per-block partials of the stated
 // width into `part`; launch_reduce_parts XORs them.
 void launch_eq_table(const F128d* d_point, uint32_t n, F128d scale, F128d* out, cudaStream_t s);
+// The lo and hi tables of an eq split (lo unscaled, hi times scale) in one launch.
+void launch_eq_split(const F128d* d_point, uint32_t lo_bits, uint32_t hi_bits, F128d scale, F128d* lo, F128d* hi,
+                     cudaStream_t s);
 void launch_reduce_parts(const F128d* part, uint32_t n_blocks, uint32_t width, F128d* out, cudaStream_t s);
 
 void upload_zc_consts(const uint8_t* ext, const F128d* phi8, const uint8_t mulk[8][256], const F128d* wconst);

@@ -53,6 +53,31 @@ void launch_eq_table(const F128d* d_point, uint32_t n, F128d scale, F128d* out, 
   eq_table_kernel<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(d_point, n, scale, out);
   LAUNCH_OK();
 }
+// Both tables of an eq split in one launch: lo = eq(p[0 .. lo_bits)) and
+// hi = scale * eq(p[lo_bits .. lo_bits + hi_bits)); entry e < 2^lo_bits is a lo entry.
+__global__ void eq_split_kernel(const F128d* __restrict__ p, uint32_t lo_bits, uint32_t hi_bits, F128d scale,
+                                F128d* __restrict__ lo, F128d* __restrict__ hi) {
+  const uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t n_lo = 1ull << lo_bits;
+  if (e >= n_lo + (1ull << hi_bits)) return;
+  const bool is_lo = e < n_lo;
+  const uint64_t i = is_lo ? e : e - n_lo;
+  const uint32_t n = is_lo ? lo_bits : hi_bits;
+  const F128d* q = is_lo ? p : p + lo_bits;
+  F128d v = is_lo ? f128_one() : scale;
+  for (uint32_t j = 0; j < n; ++j) {
+    F128d r = q[j];
+    if (!((i >> j) & 1)) r.lo ^= 1;
+    v = v * r;
+  }
+  (is_lo ? lo : hi)[i] = v;
+}
+void launch_eq_split(const F128d* d_point, uint32_t lo_bits, uint32_t hi_bits, F128d scale, F128d* lo, F128d* hi,
+                     cudaStream_t s) {
+  const uint64_t len = (1ull << lo_bits) + (1ull << hi_bits);
+  eq_split_kernel<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(d_point, lo_bits, hi_bits, scale, lo, hi);
+  LAUNCH_OK();
+}
 
 __global__ void reduce_parts_kernel(const F128d* __restrict__ part, uint32_t n_blocks, uint32_t width,
                                     F128d* __restrict__ out) {
