@@ -1587,8 +1587,8 @@ uint32_t launch_lg_fold_msg256(const F256d* f, const F256d* b, uint64_t n_out, u
     return blocks;
   }
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n_out / 2 + 255) / 256, (uint64_t)sm_count() * 8));
-  lg_fold_msg256_kernel<false><<<blocks, 256, 0, s>>>(f, b, n_out, f_live, r, log2_distance(d_fold), log2_distance(d_msg),
-                                                      fo, bo, part, pub);
+  lg_fold_msg256_kernel<false><<<blocks, 256, 0, s>>>(f, b, n_out, f_live, r, log2_distance(d_fold),
+                                                      log2_distance(d_msg), fo, bo, part, pub);
   LAUNCH_OK();
   return blocks;
 }

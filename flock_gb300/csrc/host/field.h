@@ -82,7 +82,7 @@ inline F128 ghash_reduce(uint64_t r0, uint64_t r1, uint64_t r2, uint64_t r3) {
   return F128(r0 ^ t_lo ^ corr, r1 ^ t_hi);
 }
 
-inline F128 mul(const F128& a, const F128& b) {
+static inline F128 mul_impl(const F128& a, const F128& b) {
   uint64_t l0, l1, h0, h1, m0, m1;
   clmul64(a.lo, b.lo, l0, l1);
   clmul64(a.hi, b.hi, h0, h1);
@@ -91,6 +91,15 @@ inline F128 mul(const F128& a, const F128& b) {
   m1 ^= l1 ^ h1;
   return ghash_reduce(l0, l1 ^ m0, h0 ^ m1, h1);
 }
+#if defined(__CUDACC__)
+// Host code that nvcc compiles cannot use the crypto intrinsics (the arm_neon.h route is
+// closed to it): its products go to host_accel.cc, which the host compiler builds with the
+// target's crypto extensions (PMULL on aarch64).
+F128 mul_host_accel(const F128& a, const F128& b);
+inline F128 mul(const F128& a, const F128& b) { return mul_host_accel(a, b); }
+#else
+inline F128 mul(const F128& a, const F128& b) { return mul_impl(a, b); }
+#endif
 inline F128 operator*(const F128& a, const F128& b) { return mul(a, b); }
 inline F128& operator*=(F128& a, const F128& b) { a = mul(a, b); return a; }
 inline F128 sqr(const F128& a) { return mul(a, a); }

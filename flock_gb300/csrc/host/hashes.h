@@ -25,6 +25,12 @@
 
 namespace flock {
 
+#if defined(__CUDACC__)
+// One SHA-256 compression for host code that nvcc compiles, in host_accel.cc (built by the
+// host compiler with the SHA-2 instructions where the target has them).
+void sha256_compress_host_accel(uint32_t st[8], const uint8_t* p);
+#endif
+
 // ------------------------------------------------------------------ SHA-256
 struct Sha256 {
   uint32_t h[8];
@@ -50,6 +56,13 @@ struct Sha256 {
 
   // One compression over a 64-byte block (big-endian words).
   static void compress(uint32_t st[8], const uint8_t* p) {
+#if defined(__CUDACC__)
+    sha256_compress_host_accel(st, p);
+#else
+    compress_impl(st, p);
+#endif
+  }
+  static void compress_impl(uint32_t st[8], const uint8_t* p) {
 #ifdef FLOCK_HOST_SHA2
     // four rounds per step: SHA256H / SHA256H2 on (abcd, efgh), the schedule by SHA256SU0/SU1
     uint32x4_t abcd = vld1q_u32(st), efgh = vld1q_u32(st + 4);

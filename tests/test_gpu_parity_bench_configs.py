@@ -49,7 +49,8 @@ def _build_lockstep() -> str:
     os.makedirs(out_dir, exist_ok=True)
     exe = os.path.join(out_dir, "lockstep")
     src = os.path.join(ROOT, "tests", "native", "lockstep.cu")
-    objs = [os.path.join(g.OBJ_DIR, f) for f in ("witness.o", "commit.o", "sumcheck.o", "rounds.o", "backend.o")]
+    objs = [os.path.join(g.OBJ_DIR, f)
+            for f in ("witness.o", "commit.o", "sumcheck.o", "rounds.o", "backend.o", "host_accel.o")]
     deps = [src] + objs + g._headers() + [os.path.join(ROOT, "oracle", "cpu_backend.h")]
     if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(p) for p in deps):
         g._run([g._nvcc(), *g.NVCC_FLAGS, src, *objs, "-o", exe, "-lpthread"])
