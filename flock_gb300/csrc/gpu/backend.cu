@@ -324,7 +324,9 @@ uint64_t GpuBackend::gpu_pow(const std::array<uint8_t, 32>& digest, uint32_t bit
 }
 PowSearchFn GpuBackend::pow_search() {
   return [this](const std::array<uint8_t, 32>& digest, uint32_t bits) -> uint64_t {
-    if (bits < 6) return pow_search_host(digest, bits);
+    // Up to 8 bits (256 compressions expected) the host search with the SHA-2 instructions
+    // (a few microseconds) beats a device launch and its round trip
+    if (bits <= 8) return pow_search_host(digest, bits);
     return gpu_pow(digest, bits);
   };
 }
