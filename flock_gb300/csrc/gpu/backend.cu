@@ -290,6 +290,7 @@ GpuBackend::Mark::~Mark() {
 void GpuBackend::begin_prove(const void* d_inputs) {
   lg_pend_fold_.active = false;
   lg_pend_switch_ = false;
+  lg_pend_basis_ = false;
   d_user_inputs_ = d_inputs;
   h2d_ = d2h_ = 0;
   spans_.clear();
@@ -868,8 +869,9 @@ void GpuBackend::lg_basis_eq(F128 gamma, const std::vector<F128>& rho) {
   lg_flush_fold();
   scr_off_ = 0;
   if ((uint64_t(1) << rho.size()) != Q_) throw std::runtime_error("Ligerito basis size mismatch");
-  EqSplit e = eq_split(rho, gamma, 13);  // chunks of 2^13 entries: one eq_hi table each
-  { Mark mk(this, ST_LIGERITO); launch_lg_eq_fill(e.lo, e.lo_bits, e.hi, Q_, lb128_, false, st_); }
+  lg_pend_basis_ = true;  // filled with the first OOD eq (lg_add_eq) or alone (lg_flush_basis)
+  lg_basis_gamma_ = gamma;
+  lg_basis_rho_ = rho;
   lg_base_ = true;
   lg_n_ = Q_;
   lg_live_ = std::min<uint64_t>(Q_, S.dense_words);  // q is zero from the dense words on
@@ -877,7 +879,7 @@ void GpuBackend::lg_basis_eq(F128 gamma, const std::vector<F128>& rho) {
 }
 
 F128 GpuBackend::lg_eval_eq(const std::vector<F128>& zp) {
-  lg_flush_fold();
+  lg_flush_pending();  // reads q only: a held-back basis fill stays held back
   scr_off_ = 0;
   if (!lg_base_) throw std::runtime_error("OOD evaluation expects the committed base vector");
   // chunks of 2^13 words (one eq_hi table each) where there are enough of them for every SM
@@ -889,14 +891,32 @@ F128 GpuBackend::lg_eval_eq(const std::vector<F128>& zp) {
 }
 
 void GpuBackend::lg_add_eq(F128 beta, const std::vector<F128>& zp) {
-  lg_flush_fold();
+  lg_flush_pending();
   scr_off_ = 0;
   if (!lg_base_) throw std::runtime_error("basis update expects the base stage");
   EqSplit e = eq_split(zp, beta, 13);
+  if (lg_pend_basis_) {
+    // b = gamma eq(rho) + beta eq(z) in one pass
+    lg_pend_basis_ = false;
+    EqSplit eb = eq_split(lg_basis_rho_, lg_basis_gamma_, 13);
+    if (eb.lo_bits != e.lo_bits) throw std::runtime_error("basis and OOD eq splits differ");
+    Mark mk(this, ST_LIGERITO);
+    launch_lg_eq_fill2(eb.lo, eb.hi, e.lo, e.hi, e.lo_bits, Q_, lb128_, st_);
+    return;
+  }
   { Mark mk(this, ST_LIGERITO); launch_lg_eq_fill(e.lo, e.lo_bits, e.hi, Q_, lb128_, true, st_); }
 }
 
+void GpuBackend::lg_flush_basis() {
+  if (!lg_pend_basis_) return;
+  lg_pend_basis_ = false;
+  EqSplit e = eq_split(lg_basis_rho_, lg_basis_gamma_, 13);  // chunks of 2^13 entries: one eq_hi table each
+  Mark mk(this, ST_LIGERITO);
+  launch_lg_eq_fill(e.lo, e.lo_bits, e.hi, Q_, lb128_, false, st_);
+}
+
 Msg256 GpuBackend::lg_message(size_t d) {
+  lg_flush_basis();  // the base message reads b
   if (lg_pend_switch_ && (d == 1 || 2 * lg_n_ == d)) {
     // code switch and the message over its pairs (2i, 2i + 1) in one pass
     lg_pend_switch_ = false;
@@ -962,6 +982,12 @@ Msg256 GpuBackend::lg_message(size_t d) {
 }
 
 void GpuBackend::lg_flush_fold() {
+  lg_flush_basis();
+  lg_flush_pending();
+}
+
+void GpuBackend::lg_flush_pending() {
+  if (lg_pend_fold_.active && lg_pend_fold_.base) lg_flush_basis();  // the base fold reads b
   if (lg_pend_switch_) {
     lg_pend_switch_ = false;
     const int nx = lg_cur_ ^ 1;

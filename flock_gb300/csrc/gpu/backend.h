@@ -190,7 +190,14 @@ class GpuBackend : public ProverBackend {
   // A code switch is held back the same way: the next message (pairs one apart) runs fused
   // with it; any other call first performs it on its own (lg_flush_fold does both).
   bool lg_pend_switch_ = false;
-  void lg_flush_fold();
+  // The basis eq fill is held back too: the first OOD sample's eq is added in the same pass
+  // over b (launch_lg_eq_fill2); any other use of b performs it alone first.
+  bool lg_pend_basis_ = false;
+  F128 lg_basis_gamma_;
+  std::vector<F128> lg_basis_rho_;
+  void lg_flush_basis();
+  void lg_flush_pending();  // the held-back code switch and fold
+  void lg_flush_fold();     // lg_flush_basis, then lg_flush_pending
   uint64_t lg_n_ = 0;
   // f (the folded committed vector) is zero from entry lg_live_ on: the committed vector's
   // zero tail, halved through the folds, doubled by the code switch

@@ -137,6 +137,10 @@ uint32_t launch_mo_build_w(const F128d* q, const F128d* er0, const F128d* ec0, c
 
 void launch_lg_eq_fill(const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi, uint64_t n, F128d* out, bool add,
                        cudaStream_t s);
+// b = eq_a + eq_b for two eq splits (lo tables unscaled, hi tables carrying the scales) with
+// the same lo_bits, in one pass.
+void launch_lg_eq_fill2(const F128d* lo_a, const F128d* hi_a, const F128d* lo_b, const F128d* hi_b, uint32_t lo_bits,
+                        uint64_t n, F128d* out, cudaStream_t s);
 uint32_t launch_lg_dot_eq(const F128d* f, uint32_t stride, const F128d* eq_lo, uint32_t lo_bits, const F128d* eq_hi,
                           uint64_t n, uint64_t live, F128d* part, cudaStream_t s);  // f zero from `live` on                                    // width 1
 // f_live: f is zero from that entry on (pairs wholly past it add nothing and are skipped).

@@ -1231,6 +1231,43 @@ lg_eq_fill_tbl_kernel(const F128d* __restrict__ eq_lo, uint32_t lo_bits, const F
     }
   }
 }
+// b[i] = eq_a(i) + eq_b(i) for two eq splits with the same lo_bits (the basis eq and the
+// first OOD eq in one pass over b): per chunk, the products by eq_hi_a[chunk] from its byte
+// tables and those by eq_hi_b[chunk] from its split form, one of each per entry.
+__global__ void __launch_bounds__(256, 2)
+lg_eq_fill2_tbl_kernel(const F128d* __restrict__ lo_a, const F128d* __restrict__ hi_a, const F128d* __restrict__ lo_b,
+                       const F128d* __restrict__ hi_b, uint32_t lo_bits, uint64_t n, F128d* __restrict__ out) {
+  extern __shared__ __align__(16) F128d htab[];  // build_byte_table's BYTE_TABLE_SMEM_ENTRIES
+  __shared__ F128split hs;
+  const uint64_t chunk = 1ull << lo_bits, n_chunks = n >> lo_bits;
+  for (uint64_t ch = blockIdx.x; ch < n_chunks; ch += gridDim.x) {
+    __syncthreads();  // the previous chunk's table and split are no longer read
+    if (threadIdx.x == 0) hs = split_factor(hi_b[ch]);
+    build_byte_table(hi_a[ch], htab);
+    F128d* o = out + ch * chunk;
+    for (uint64_t i = threadIdx.x; i < chunk; i += blockDim.x) o[i] = mul_table(lo_a[i], htab) + mul_split(lo_b[i], hs);
+  }
+}
+__global__ void lg_eq_fill2_kernel(const F128d* __restrict__ lo_a, const F128d* __restrict__ hi_a,
+                                   const F128d* __restrict__ lo_b, const F128d* __restrict__ hi_b, uint32_t lo_bits,
+                                   uint64_t n, F128d* __restrict__ out) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = eq_at(lo_a, lo_bits, hi_a, i) + eq_at(lo_b, lo_bits, hi_b, i);
+}
+void launch_lg_eq_fill2(const F128d* lo_a, const F128d* hi_a, const F128d* lo_b, const F128d* hi_b, uint32_t lo_bits,
+                        uint64_t n, F128d* out, cudaStream_t s) {
+  if (lo_bits >= 12 && (n >> lo_bits) >= (uint64_t)sm_count() * 2 && (n & ((1ull << lo_bits) - 1)) == 0) {
+    const int smem = (int)(BYTE_TABLE_SMEM_ENTRIES * sizeof(F128d));
+    set_dynamic_smem((const void*)lg_eq_fill2_tbl_kernel, smem);
+    const uint32_t blocks = (uint32_t)std::min<uint64_t>(n >> lo_bits, (uint64_t)sm_count() * 2);
+    lg_eq_fill2_tbl_kernel<<<blocks, 256, smem, s>>>(lo_a, hi_a, lo_b, hi_b, lo_bits, n, out);
+    LAUNCH_OK();
+    return;
+  }
+  lg_eq_fill2_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(lo_a, hi_a, lo_b, hi_b, lo_bits, n, out);
+  LAUNCH_OK();
+}
 // Chunks of at least 2^12 entries (one table build per chunk), and enough of them to give
 // every SM two blocks, use the table form.
 constexpr uint32_t LG_EQ_FILL_TABLE_MIN_LO_BITS = 12;
