@@ -305,12 +305,22 @@ __global__ void witness_keccak_kernel(const uint64_t* __restrict__ in, uint32_t 
                                       uint64_t* z, uint64_t* a, uint64_t* b, uint32_t used_words) {
   uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= n_inst) return;
-  // input words -> Keccak lanes
+  // input words -> Keccak lanes: input bit j is bit j / 25 of lane j % 25. The input words
+  // are loaded once and every index below is a compile-time constant (fully unrolled), so
+  // the lanes stay in registers.
+  uint64_t iw[25];
+#pragma unroll
+  for (int i = 0; i < 25; ++i) iw[i] = in[(size_t)o * 25 + i];
   uint64_t st[25];
-  for (int i = 0; i < 25; ++i) st[i] = 0;
-  for (int j = 0; j < 1600; ++j) {
-    uint64_t wv = in[(size_t)o * 25 + (j >> 6)];
-    if ((wv >> (j & 63)) & 1) st[j % 25] |= 1ull << (j / 25);
+#pragma unroll
+  for (int l = 0; l < 25; ++l) {
+    uint64_t v = 0;
+#pragma unroll
+    for (int k = 0; k < 64; ++k) {
+      const int j = 25 * k + l;
+      v |= ((iw[j >> 6] >> (j & 63)) & 1ull) << k;
+    }
+    st[l] = v;
   }
   // u64 word w of the block sits at z[(((w >> 1) << nu) + o) * 2 + (w & 1)]
   auto put = [&](uint32_t w, uint64_t zv, uint64_t av, uint64_t bv) {
