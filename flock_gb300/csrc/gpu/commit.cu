@@ -352,7 +352,7 @@ __global__ void merkle_level_kernel(uint32_t* __restrict__ tree, uint64_t in_off
 // n_cap nodes (the cap), in one block: each level's nodes are hashed by the block's
 // threads, then a barrier.
 constexpr uint32_t MERKLE_TOP_NODES = 2048;
-__global__ void __launch_bounds__(256) merkle_top_kernel(uint32_t* __restrict__ tree, uint64_t in_off, uint32_t n_in,
+__global__ void __launch_bounds__(1024) merkle_top_kernel(uint32_t* __restrict__ tree, uint64_t in_off, uint32_t n_in,
                                                          uint32_t n_cap) {
   uint64_t off = in_off;
   for (uint32_t len = n_in; len > n_cap; len /= 2) {
@@ -385,7 +385,7 @@ void launch_merkle(const F128d* rows, uint32_t lanes, uint64_t n_leaves, uint32_
     len = nout;
   }
   if (len > n_cap) {
-    merkle_top_kernel<<<1, 256, 0, s>>>((uint32_t*)tree, off, (uint32_t)len, (uint32_t)n_cap);
+    merkle_top_kernel<<<1, 1024, 0, s>>>((uint32_t*)tree, off, (uint32_t)len, (uint32_t)n_cap);
     LAUNCH_OK();
   }
 }

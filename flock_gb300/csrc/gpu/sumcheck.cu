@@ -1768,6 +1768,41 @@ __global__ void lg_induced_fold_kernel(const F128d* __restrict__ y, uint32_t ln,
   if (threadIdx.x == 0) { part[blockIdx.x * 2] = A; part[blockIdx.x * 2 + 1] = Sm; }
   if (pub.out) publish_if_last(part, 2, pub, sh);
 }
+// Several consecutive transposed layers in one launch: layers layer_hi, layer_hi - 1, ...,
+// layer_hi - nl + 1 (pair distances 2^sh_min, ..., 2^(sh_min + nl - 1), sh_min =
+// log_d - 1 - layer_hi) act within groups of 2^nl positions spaced 2^sh_min apart, so one
+// block stages a group in shared memory and runs all nl layers there (one launch and one
+// global pass instead of nl). Group g: base = (g >> sh_min) << (sh_min + nl) | (g mod
+// 2^sh_min); position t of the group is base + t 2^sh_min. The butterfly is ntt_t_layer's.
+constexpr uint32_t NTT_T_FUSED = 6;  // layers per fused pass (64-position groups)
+constexpr uint32_t NTT_T_FUSED_MAX_LOG = 16;  // transforms of at most 2^16 positions use it
+__global__ void __launch_bounds__(256)
+ntt_t_fused_kernel(F128d* __restrict__ y, uint32_t log_d, uint32_t layer_hi, uint32_t nl,
+                   const F128d* __restrict__ tw) {
+  __shared__ F128d g[4][1u << NTT_T_FUSED];  // four groups per 256-thread block
+  const uint32_t P = 1u << nl, sh_min = log_d - 1 - layer_hi;
+  const uint64_t n_groups = 1ull << (log_d - nl);
+  const uint32_t sub = threadIdx.x >> 6, t = threadIdx.x & 63;  // 64 threads per group
+  const uint64_t gi = (uint64_t)blockIdx.x * 4 + sub;
+  const bool have = gi < n_groups;  // group-uniform
+  const uint64_t base = have ? (((gi >> sh_min) << (sh_min + nl)) | (gi & ((1ull << sh_min) - 1))) : 0;
+  if (have && t < P) g[sub][t] = y[base + ((uint64_t)t << sh_min)];
+  __syncthreads();
+  for (uint32_t k = 0; k < nl; ++k) {
+    const uint32_t layer = layer_hi - k, sh = sh_min + k;
+    if (have && t < P / 2) {
+      // pair t of the group at group distance 2^k
+      const uint32_t lo = ((t >> k) << (k + 1)) | (t & ((1u << k) - 1)), hi = lo + (1u << k);
+      const uint64_t i0 = base + ((uint64_t)lo << sh_min);
+      const uint64_t blk = i0 >> (sh + 1);
+      const F128d u = g[sub][lo], v = g[sub][hi], sum = u + v;
+      g[sub][lo] = sum;
+      g[sub][hi] = blk == 0 ? v : v + mul_call(tw[(1ull << layer) - 1 + blk], sum);  // first block: twiddle zero
+    }
+    __syncthreads();
+  }
+  if (have && t < P) y[base + ((uint64_t)t << sh_min)] = g[sub][t];
+}
 uint32_t launch_lg_induced(const uint64_t* pos, const F128d* w, uint32_t n_q, uint32_t ln, uint32_t log_rate,
                            const F128d* tw, const F256d* f, F128d* y, F128d* basis, F128d* part, cudaStream_t s,
                            FusedPublish pub) {
@@ -1776,9 +1811,20 @@ uint32_t launch_lg_induced(const uint64_t* pos, const F128d* w, uint32_t n_q, ui
   lg_scatter_kernel<<<(n_q + 127) / 128, 128, 0, s>>>(pos, w, n_q, y);
   LAUNCH_OK();
   uint64_t pairs = 1ull << (log_d - 1);
-  for (int layer = (int)log_d - 1; layer >= (int)log_rate; --layer) {
-    ntt_t_layer_kernel<<<(unsigned)((pairs + 255) / 256), 256, 0, s>>>(y, log_d, (uint32_t)layer, tw);
+  // transposed layers from log_d - 1 down to log_rate: for the small levels (launch-latency
+  // bound) up to NTT_T_FUSED per launch; the large ones one per launch (their fused groups
+  // would be strided and half the threads idle in every layer: slower, measured)
+  const uint32_t per_launch = log_d <= NTT_T_FUSED_MAX_LOG ? NTT_T_FUSED : 1;
+  for (int layer = (int)log_d - 1; layer >= (int)log_rate;) {
+    const uint32_t nl = std::min<uint32_t>(per_launch, (uint32_t)(layer - (int)log_rate + 1));
+    if (nl >= 2) {
+      const uint64_t n_groups = 1ull << (log_d - nl);
+      ntt_t_fused_kernel<<<(unsigned)((n_groups + 3) / 4), 256, 0, s>>>(y, log_d, (uint32_t)layer, nl, tw);
+    } else {
+      ntt_t_layer_kernel<<<(unsigned)((pairs + 255) / 256), 256, 0, s>>>(y, log_d, (uint32_t)layer, tw);
+    }
     LAUNCH_OK();
+    layer -= (int)nl;
   }
   uint64_t n = 1ull << ln;
   uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, (uint64_t)sm_count() * 8));
